@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Benchmark of the PCISPH particle step on GB300 (one JSON line on rank 0).
+
+Workload: the 1,048,576-particle PCISPH dam break (128 x 64 x 128 cubic lattice at
+spacing 0.008, +-0.1 spacing jitter, 2 x 1 x 1.2 box), FP32 state, tolerance-mode
+corrector (max density error < 1 % of rho0, at most 20 iterations), substep dt at the
+CFL speed limit of scale 5.  A step is one substep: grid rebuild, density,
+non-pressure force, the corrector to tolerance, integration with colliders.
+
+  value      particle-updates/s over the timed substeps, inputs resident in HBM, L2
+             flushed (256 MB write) between steps, CUDA events on the launching stream
+  e2e        the same metric through the C ABI with host buffers: upload positions and
+             velocities from pinned memory, one substep, download them, every step
+  roofline   dominant kernel: algorithmic bytes per launch / its average duration
+  cpu_baseline  the CPU oracle (restatement of the reference's CPU path) on the box's
+             host cores, on a bounded sample of the same workload
+
+`--impl reference` times the reference's CPU implementation of the path (the oracle
+port, all host threads) on the same workload and prints the same line with
+"impl": "reference".  Under torchrun every rank runs an independent replica of the
+scene ("replicas only": the step has no exchange); rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-updates/s PCISPH 1M, learned+batched vs plain at ≤1% density err"
+UNIT = "particle-updates/s"
+L2_FLUSH_BYTES = 256 << 20
+
+# Algorithmic (compulsory) HBM bytes per particle per launch: every FP32 SoA array a
+# kernel reads or writes counted once; neighbour re-reads are served by L1/L2.
+ALG_BYTES = {
+    "k_hash_count": 16 + 4 + 4,                    # pos in; cell, arrival index out
+    "k_place": 4 + 4 + 4 + 4 + 8,                  # cell, index, start, id in; (id, slot) out
+    "k_rank_gather": 8 + 4 + 8 + 32 + 32 + 4 + 4 + 4,  # tmp, cell, start, pos+vel in/out, id, slot, cell
+    "k_density": 16 + 4 + 4 + 4,                   # pos, cell in; density, neighbour count out
+    "k_non_pressure": 16 + 16 + 4 + 4 + 16 + 16 + 16 + 4,  # pos, vel, rho, cell; F, x*, Fp, p out
+    "k_pred_density": 16 + 16 + 4 + 4 + 4 + 4 + 4,  # pos, x*, cell, p in; p, rho*, err out
+    "k_pressure_force": 16 + 16 + 4 + 4 + 4 + 16 + 16 + 16,  # pos, vel, cell, p, rho*, F; Fp, x*
+    "k_sph_forces": 16 + 16 + 4 + 4 + 4 + 16 + 32,
+    "k_integrate": 16 + 16 + 16 + 32,
+}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(workload_key):
+    """Per-particle DRAM bytes per launch from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "%s_ncu.md" % workload_key)
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == "traffic_bytes_per_particle:":
+                out[parts[1]] = float(parts[2])
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[5 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def aggregate(dist, units, seconds):
+    """Whole-job throughput: units summed over ranks / the slowest rank's time."""
+    if dist is None:
+        return units / seconds, seconds, units
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds], dtype=torch.float64, device=dev)
+    u = torch.tensor([units], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return u.item() / t.item(), t.item(), u.item()
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_rate(scene, pos, vel, budget_s, threads, max_steps=50):
+    """Time the CPU oracle on substeps of (scene, pos, vel) until `budget_s`."""
+    from oracle import oracle as O
+    sim = O.OracleSim(scene, pos, vel, variant="f32", threads=threads)
+    steps, iters, t = 0, 0, 0.0
+    while t < budget_s and steps < max_steps:
+        t0 = time.perf_counter()
+        it, _ = sim.pcisph_substep(scene["dt"], scene["max_density_error_ratio"],
+                                   scene["max_iterations"], O.PCISPH_TOLERANCE)
+        t += time.perf_counter() - t0
+        steps += 1
+        iters += it
+    sim.close()
+    return len(pos) * steps / t, steps, iters, t
+
+
+def slab(pos, block, depth):
+    """The first `depth` z-layers of the lattice block (x fastest, then y, then z)."""
+    nx, ny, nz = block
+    return pos.reshape(nz, ny, nx, 3)[:depth].reshape(-1, 3)
+
+
+def run_reference(args, scene, pos):
+    """Reference arm: the oracle port of the reference CPU path, all host threads."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    block = scene["block"]
+    # size the per-step sample so the whole run stays within ~150 s of CPU time
+    probe = slab(pos, block, 8)
+    rate, _, _, _ = cpu_oracle_rate(scene, probe, None, 0.0, threads, max_steps=1)
+    per_step_budget = 150.0 / max(1, args.steps + args.warmup)
+    depth = int(np.clip((per_step_budget * rate) / (block[0] * block[1]) // 8 * 8, 8, block[2]))
+    sample = slab(pos, block, depth)
+    from oracle import oracle as O
+    sim = O.OracleSim(scene, sample, None, variant="f32", threads=threads)
+    for _ in range(args.warmup):
+        sim.pcisph_substep(scene["dt"], scene["max_density_error_ratio"], scene["max_iterations"],
+                           O.PCISPH_TOLERANCE)
+    t, iters = 0.0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        it, _ = sim.pcisph_substep(scene["dt"], scene["max_density_error_ratio"],
+                                   scene["max_iterations"], O.PCISPH_TOLERANCE)
+        t += time.perf_counter() - t0
+        iters += it
+    sim.close()
+    value = len(sample) * args.steps / t
+    desc = ("%d-layer slab (%d particles) of the dam-break block, one tolerance-mode substep "
+            "per step from t=0 (%d warm-up substeps), %.2f corrector iterations per substep"
+            % (depth, len(sample), args.warmup, iters / max(1, args.steps)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": scene["workload"], "variant": "plain", "solver": "pcisph",
+                   "tolerance": scene["max_density_error_ratio"],
+                   "max_iterations": scene["max_iterations"], "dt": scene["dt"],
+                   "parallelism": "cpu threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, scene, pos):
+    import torch
+
+    import bubbles_gb300 as bb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    n = len(pos)
+    dt = scene["dt"]
+    stream = torch.cuda.Stream(device=local)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        g = bb.Solver(scene, pos=pos, device=local)
+        g.set_stream(stream)
+        for _ in range(args.warmup):
+            g.advance_time_step(dt)
+        torch.cuda.synchronize()
+        barrier(dist)
+
+        sampler = ClockSampler(local)
+        sampler.start()
+        g.profiler_enable(True)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        iters, max_err = [], []
+        torch.cuda.synchronize()
+        barrier(dist)
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            g.advance_time_step(dt)
+            ends[k].record(stream)
+            st = g.stats()
+            iters.append(st["iterations"])
+            max_err.append(st["max_density_error_ratio"])
+        torch.cuda.synchronize()
+        barrier(dist)
+        g.profiler_enable(False)
+        prof, launches = g.profiler_report()
+        step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        total_s = sum(step_ms) / 1e3
+        value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
+
+        # end to end through the C ABI with pinned host buffers
+        pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        g.download(pos_h, vel_h)
+        for _ in range(max(1, args.warmup)):
+            g.upload(pos_h, vel_h)
+            g.advance_time_step(dt)
+            g.download(pos_h, vel_h)
+        e2e_steps = args.steps
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            g.upload(pos_h, vel_h)
+            g.advance_time_step(dt)
+            g.download(pos_h, vel_h)
+        e2e_s = time.perf_counter() - t0
+        e2e_value, _, _ = aggregate(dist, float(n * e2e_steps), e2e_s)
+        sampler.stop()
+        final_pos, final_vel = pos_h.copy(), vel_h.copy()
+        g.close()
+
+    if rank != 0:
+        barrier(dist)
+        return
+
+    # roofline of the dominant kernel
+    peak, peak_kind = load_peaks()
+    traffic_table = load_traffic(args.config)
+    kern = {k: v for k, v in prof.items() if k in ALG_BYTES}
+    top = max(kern, key=lambda k: kern[k][0]) if kern else None
+    roof = None
+    if top:
+        ms, cnt = kern[top]
+        avg_s = ms / cnt / 1e3
+        alg = ALG_BYTES[top] * n
+        achieved = alg / avg_s / 1e9
+        tr = traffic_table.get(top)
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": tr * n if tr is not None else None,
+                "algorithmic_bytes": alg, "avg_launch_us": avg_s * 1e6,
+                "share_of_step": ms / sum(v[0] for v in prof.values())}
+
+    # CPU baseline: oracle on the host cores, bounded sample of the same state
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        block = scene["block"]
+        depth = args.cpu_slab
+        sample_p = slab(final_pos, block, depth) if depth < block[2] else final_pos
+        sample_v = slab(final_vel, block, depth) if depth < block[2] else final_vel
+        rate, steps_c, iters_c, t_c = cpu_oracle_rate(scene, sample_p.astype(np.float64),
+                                                      sample_v.astype(np.float64),
+                                                      args.cpu_budget, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": ("%d substep(s) (%.1f s, %.2f corrector iterations each) of a %d-particle "
+                          "slab of the same dam-break state, FP32 oracle, %d threads"
+                          % (steps_c, t_c, iters_c / max(1, steps_c), len(sample_p), threads))}
+
+    per_kernel = {k: {"ms_total": v[0], "launches": v[1], "avg_us": 1e3 * v[0] / max(1, v[1])}
+                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": scene["workload"], "variant": "plain", "solver": "pcisph",
+                   "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
+                   "max_iterations": scene["max_iterations"],
+                   "corrector_iterations_mean": float(np.mean(iters)),
+                   "max_density_error_ratio_last": max_err[-1],
+                   "l2": "flushed between timed steps (256 MB write, outside the events)",
+                   "parallelism": "replicas" if world > 1 else "single gpu"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * 24},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": sampler.summary(),
+        "kernels": per_kernel,
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="pcisph_1m")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from bubbles_gb300 import scenes
+    rank, _, _ = dist_env()
+    scene, pos = scenes.config(args.config, seed=args.seed + rank)
+    if args.impl == "reference":
+        run_reference(args, scene, pos)
+    else:
+        run_ours(args, scene, pos)
+
+
+if __name__ == "__main__":
+    main()

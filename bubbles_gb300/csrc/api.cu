@@ -1,0 +1,905 @@
+// api.cu -- the C ABI of bubbles_gb300 (include/bbg.h): solver lifetime, the
+// substep launch sequences and field access.  Host code only; kernels live in
+// grid.cu and sph.cu.
+#include "../../include/bbg.h"
+#include "bbg_kernels.h"
+#include "host_math.h"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+using namespace bbg;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+bbg_status fail(bbg_status code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CK(call)                                                                           \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            if (e_ == cudaErrorMemoryAllocation)                                           \
+                return fail(BBG_ERR_OUT_OF_MEMORY, "%s: %s", #call, cudaGetErrorString(e_)); \
+            return fail(BBG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));            \
+        }                                                                                  \
+    } while (0)
+
+#define CK_LAUNCH() CK(cudaGetLastError())
+
+// bit per field id: valid in the current sorted-slot order
+constexpr unsigned bit(int f) { return 1u << f; }
+constexpr unsigned kPosVel = bit(BBG_FIELD_POSITION) | bit(BBG_FIELD_VELOCITY);
+
+}  // namespace
+
+struct bbg_solver_s {
+    bbg_solver_desc desc;
+    int capacity = 0, n = 0;
+    Params P;
+    DevBufs B;
+    int state = 0;     // ping-pong buffer holding the current positions / velocities
+    int pid_cur = 0;   // pid buffer of the current sorted order
+    unsigned cells = 0;
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+    bool setup_done = false, grid_valid = false;
+    unsigned valid = 0;
+    float mass = 0, kernel_radius = 0, delta_denom = 0, mod2 = 0;
+    float dims_geo[12];
+    int dims[3];
+    StepState *h_st = nullptr;   // pinned host mirror of the device step state
+    unsigned *h_u = nullptr;     // pinned scratch
+    int last_max_it = 1;
+    float last_tol = 0.01f;
+    int pcisph_last_substep = 0;
+    bbg_step_stats acc;          // accumulated over the current advance call
+    Prof prof;
+};
+
+namespace {
+
+bbg_status check_solver(bbg_solver s) {
+    if (!s) return fail(BBG_ERR_INVALID_ARGUMENT, "null solver");
+    return BBG_OK;
+}
+
+void fill_params(bbg_solver s) {
+    Params &P = s->P;
+    const bbg_solver_desc &d = s->desc;
+    P.n = s->n;
+    P.mass = s->mass;
+    P.radius = (float)d.target_spacing;
+    P.h = s->kernel_radius;
+    P.h2 = P.h * P.h;
+    P.inv_h = 1.0f / P.h;
+    P.inv_h2 = 1.0f / P.h2;
+    P.target_density = (float)d.target_density;
+    P.iz = float_above(1e-8);
+    P.iz6 = float_above(1e-6);
+    const double T = (double)P.h2 - (double)P.iz;
+    float lo = (float)(T * (1.0 - 1e-6));
+    if ((double)lo > T * (1.0 - 1e-6)) lo = nextafterf(lo, 0.f);
+    float hi = (float)(T * (1.0 + 1e-6));
+    if ((double)hi < T * (1.0 + 1e-6)) hi = nextafterf(hi, 3.4e38f);
+    P.nb_lo = lo;
+    P.nb_hi = hi;
+    P.h2mz = (float)T;
+    const double kPi = 3.14159265358979323846;
+    const float h3 = P.h2 * P.h, h4 = P.h2 * P.h2, h5 = P.h2 * h3;
+    P.std_c = (float)(315.0 / (64.0 * kPi * (double)h3));
+    P.spiky_dw_c = (float)(45.0 / (kPi * (double)h4));
+    P.spiky_d2w_c = (float)(90.0 / (kPi * (double)h5));
+    P.spiky_w_c = (float)(15.0 / (kPi * (double)h3));
+    const float visc = (float)d.viscosity > 0 ? (float)d.viscosity : 0.f;
+    P.m2 = P.mass * P.mass;
+    P.visc_m2 = visc * P.m2;
+    P.drag = (float)d.drag_coefficient;
+    P.gx = (float)d.gravity[0];
+    P.gy = (float)d.gravity[1];
+    P.gz = (float)d.gravity[2];
+    const float rho0 = (float)d.target_density, c = (float)d.sound_speed;
+    const float eosScale = rho0 * c * c;
+    P.eos_scale_over_exp = eosScale / (float)d.eos_exponent;
+    P.eos_exp = (float)d.eos_exponent;
+    P.neg_scale = (float)d.negative_pressure_scale;
+    P.rest_int = 0.6f;
+    P.rest_c1_int = (float)(-1.0 - (double)0.6f);
+    P.max_err_ratio = (float)d.max_density_error_ratio;
+}
+
+template <class T>
+bbg_status dalloc(T **p, size_t count) {
+    CK(cudaMalloc((void **)p, sizeof(T) * (count ? count : 1)));
+    return BBG_OK;
+}
+
+bbg_status free_all(bbg_solver s) {
+    DevBufs &B = s->B;
+    void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
+                    B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
+                    B.cell_old, B.sub, B.count, B.start, B.partials, B.tmp, B.nbr, B.st, B.stage,
+                    B.red};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    Prof *keep = B.prof;
+    memset(&B, 0, sizeof(B));
+    B.prof = keep;
+    if (s->h_st) cudaFreeHost(s->h_st);
+    if (s->h_u) cudaFreeHost(s->h_u);
+    s->h_st = nullptr;
+    s->h_u = nullptr;
+    return BBG_OK;
+}
+
+bbg_status require_grid(bbg_solver s) {
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (!s->grid_valid) return fail(BBG_ERR_STATE, "no grid distribution yet (call bbg_update_grid_distribution)");
+    return BBG_OK;
+}
+
+bbg_status reset_step_state(bbg_solver s) {
+    CK(cudaMemsetAsync(s->B.st, 0, sizeof(StepState), s->stream));
+    return BBG_OK;
+}
+
+bbg_status grid_update(bbg_solver s) {
+    bbg_status r = reset_step_state(s);
+    if (r) return r;
+    launch_grid_update(s->P, s->B, s->state, s->pid_cur, s->stream);
+    CK_LAUNCH();
+    s->state = 1 - s->state;
+    s->pid_cur = 1 - s->pid_cur;
+    s->grid_valid = true;
+    s->valid = kPosVel | bit(BBG_FIELD_INTERACTION);
+    return BBG_OK;
+}
+
+// Iterations used by the last corrector, from the per-iteration maxima (host copy).
+int iterations_from(const bbg_solver s, const StepState *st, int max_it, float tol, float *err_out,
+                    double *mean_out) {
+    int it = max_it;
+    for (int k = 0; k < max_it; k++) {
+        float e;
+        memcpy(&e, &st->err_bits[k], 4);
+        if (e / s->P.target_density < tol || k == max_it - 1) {
+            it = k + 1;
+            *err_out = e / s->P.target_density;
+            *mean_out = st->err_sum[k] / (double)s->n / (double)s->P.target_density;
+            break;
+        }
+    }
+    return it;
+}
+
+bbg_status read_step_state(bbg_solver s) {
+    CK(cudaMemcpyAsync(s->h_st, s->B.st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+void add_substep_stats(bbg_solver s, float dt) {
+    bbg_step_stats &a = s->acc;
+    const StepState *st = s->h_st;
+    a.substeps += 1;
+    a.last_dt = dt;
+    if (s->desc.solver_kind == BBG_SOLVER_PCISPH) {
+        float err = 0;
+        double mean = 0;
+        int it = iterations_from(s, st, s->last_max_it, s->last_tol, &err, &mean);
+        s->prof.mark_iterations(it);
+        a.iterations += it;
+        if (it > a.max_iterations_in_substep) a.max_iterations_in_substep = it;
+        if (!(err < s->last_tol) && s->desc.pcisph_mode == BBG_PCISPH_TOLERANCE) a.not_converged += 1;
+        a.max_density_error_ratio = err;
+        a.mean_density_error_ratio = mean;
+    }
+    a.neighbor_overflow = (int)st->nbr_overflow;
+    a.out_of_grid = (int)st->out_of_grid;
+    float f;
+    memcpy(&f, &st->max_force_bits, 4);
+    a.max_force = f;
+}
+
+// Corrector loop of ComputePressureForceAndIntegrate: max_it x (predicted density,
+// pressure force); the kernels decide on device when to stop and integrate.
+bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
+    if (max_it < 1) max_it = 1;
+    if (max_it > kMaxIterations) max_it = kMaxIterations;
+    const float dt_over_m = dt / s->mass;
+    s->last_max_it = max_it;
+    s->last_tol = s->P.max_err_ratio;
+    for (int k = 0; k < max_it; k++) {
+        launch_pred_density(s->P, s->B, s->state, k, delta, s->stream);
+        launch_pressure_force(s->P, s->B, s->state, k, max_it, dt, dt_over_m, s->stream);
+    }
+    CK_LAUNCH();
+    s->state = 1 - s->state;
+    s->valid |= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE) |
+                bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_PRED_DENSITY) |
+                bit(BBG_FIELD_DENSITY_ERROR) | bit(BBG_FIELD_PRED_POSITION);
+    return BBG_OK;
+}
+
+bbg_status pseudo_viscosity(bbg_solver s, float dt) {
+    const float scale = (float)s->desc.pseudo_viscosity * dt;
+    if (scale > 0.1) {
+        float t = dt * (float)s->desc.pseudo_viscosity;
+        t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+        launch_pseudo_viscosity(s->P, s->B, s->state, t, s->stream);
+        CK_LAUNCH();
+    }
+    return BBG_OK;
+}
+
+bbg_status substep(bbg_solver s, float dt) {
+    s->prof.substep++;
+    bbg_status r = grid_update(s);
+    if (r) return r;
+    if (s->desc.solver_kind == BBG_SOLVER_SPH) {
+        launch_density(s->P, s->B, s->state, 1, s->stream);
+        launch_sph_forces(s->P, s->B, s->state, dt, s->stream);
+        CK_LAUNCH();
+        s->state = 1 - s->state;
+        s->valid |= kPosVel | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_FORCE);
+        return pseudo_viscosity(s, dt);
+    }
+    const bool shipped = s->desc.pcisph_mode == BBG_PCISPH_AS_SHIPPED;
+    const int max_it = shipped ? 1 : s->desc.max_iterations;
+    s->P.max_err_ratio = shipped ? 0.01f : (float)s->desc.max_density_error_ratio;
+    const float delta = compute_delta(s->mod2, s->delta_denom, dt);
+    launch_density(s->P, s->B, s->state, 0, s->stream);
+    launch_non_pressure(s->P, s->B, s->state, 1, dt, dt / s->mass, s->stream);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE);
+    r = corrector(s, dt, delta, max_it);
+    if (r) return r;
+    return pseudo_viscosity(s, dt);
+}
+
+bbg_status max_force(bbg_solver s, float *out) {
+    if (!(s->valid & bit(BBG_FIELD_FORCE))) return fail(BBG_ERR_STATE, "forces not valid");
+    launch_max_force(s->B.force, s->n, s->B.red, s->stream);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(s->h_u, s->B.red, 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    memcpy(out, s->h_u, 4);
+    return BBG_OK;
+}
+
+int field_components(int f) {
+    switch (f) {
+        case BBG_FIELD_POSITION: case BBG_FIELD_VELOCITY: case BBG_FIELD_FORCE:
+        case BBG_FIELD_INTERACTION: case BBG_FIELD_PRED_POSITION: case BBG_FIELD_PRESSURE_FORCE:
+            return 3;
+        case BBG_FIELD_DENSITY: case BBG_FIELD_PRESSURE: case BBG_FIELD_PRED_DENSITY:
+        case BBG_FIELD_DENSITY_ERROR:
+            return 1;
+        default:
+            return 0;
+    }
+}
+
+float4 *vec_field(bbg_solver s, int f) {
+    switch (f) {
+        case BBG_FIELD_POSITION: return s->B.pos[s->state];
+        case BBG_FIELD_VELOCITY: return s->B.vel[s->state];
+        case BBG_FIELD_FORCE: return s->B.force;
+        case BBG_FIELD_PRED_POSITION: return s->B.xstar;
+        case BBG_FIELD_PRESSURE_FORCE: return s->B.pforce;
+        default: return nullptr;
+    }
+}
+
+float *scalar_field(bbg_solver s, int f) {
+    switch (f) {
+        case BBG_FIELD_DENSITY: return s->B.rho;
+        case BBG_FIELD_PRESSURE: return s->B.press;
+        case BBG_FIELD_PRED_DENSITY: return s->B.rhostar;
+        case BBG_FIELD_DENSITY_ERROR: return s->B.derr;
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char *bbg_version(void) { return "bubbles_gb300 0.1 (sm_103a)"; }
+
+const char *bbg_status_string(bbg_status s) {
+    switch (s) {
+        case BBG_OK: return "ok";
+        case BBG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case BBG_ERR_CUDA: return "CUDA error";
+        case BBG_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case BBG_ERR_CAPACITY: return "capacity exceeded";
+        case BBG_ERR_STATE: return "invalid solver state";
+        case BBG_ERR_NO_DEVICE: return "no CUDA device";
+        case BBG_ERR_NOT_FOUND: return "not found";
+        default: return "unknown status";
+    }
+}
+
+const char *bbg_last_error(void) { return g_err; }
+
+bbg_status bbg_device_count(int *count) {
+    if (!count) return fail(BBG_ERR_INVALID_ARGUMENT, "null count");
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        c = 0;
+    }
+    *count = c;
+    return BBG_OK;
+}
+
+bbg_status bbg_solver_desc_default(bbg_solver_desc *d, int kind) {
+    if (!d) return fail(BBG_ERR_INVALID_ARGUMENT, "null desc");
+    if (kind != BBG_SOLVER_PCISPH && kind != BBG_SOLVER_SPH)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "unknown solver kind %d", kind);
+    memset(d, 0, sizeof(*d));
+    d->solver_kind = kind;
+    d->eos_exponent = 7.0;
+    d->negative_pressure_scale = 0.0;
+    d->viscosity = 0.04;
+    d->pseudo_viscosity = 10.0;
+    d->sound_speed = 100.0;
+    d->drag_coefficient = 0.0001;
+    d->gravity[0] = 0.0;
+    d->gravity[1] = (double)-9.8f;   // vec3f(0.f, -9.8f, 0.f)
+    d->gravity[2] = 0.0;
+    d->target_density = 1000.0;
+    d->target_spacing = 0.1;
+    d->relative_kernel_radius = 2.0;
+    d->mass = 0.0;
+    d->grid_spacing_scale = 2.0;
+    d->time_step_limit_scale = kind == BBG_SOLVER_PCISPH ? 5.0 : 1.0;
+    d->pcisph_mode = BBG_PCISPH_AS_SHIPPED;
+    d->max_iterations = 5;
+    d->max_density_error_ratio = 0.01;
+    d->device = 0;
+    return BBG_OK;
+}
+
+bbg_status bbg_build_grid(const double dmin[3], const double dmax[3], double spacing, double scale,
+                          int dims[3], double geo[12]) {
+    if (!dmin || !dmax || !dims || !geo || !(spacing > 0) || !(scale > 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "invalid grid arguments");
+    float minp[3], len[3], bmin[3], bmax[3];
+    build_grid(dmin, dmax, spacing, scale, dims, minp, len, bmin, bmax);
+    for (int k = 0; k < 3; k++) {
+        geo[k] = minp[k];
+        geo[3 + k] = len[k];
+        geo[6 + k] = bmin[k];
+        geo[9 + k] = bmax[k];
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_mass(int lattice, double target_density, double spacing, double kernel_radius,
+                            double *mass) {
+    if (!mass || (lattice != 0 && lattice != 1) || !(spacing > 0) || !(kernel_radius > 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "invalid mass arguments");
+    *mass = compute_mass(lattice, (float)target_density, (float)spacing, (float)kernel_radius);
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_delta_denom(double spacing, double kernel_radius, double *denom) {
+    if (!denom || !(spacing > 0) || !(kernel_radius > 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "invalid delta arguments");
+    *denom = compute_delta_denom((float)spacing, (float)kernel_radius);
+    return BBG_OK;
+}
+
+bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out) {
+    if (!desc || !out || capacity <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "invalid create arguments");
+    *out = nullptr;
+    if (!(desc->target_spacing > 0) || !(desc->relative_kernel_radius > 0) ||
+        !(desc->grid_spacing_scale > 0) || !(desc->target_density > 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "spacing, kernel radius, grid scale and density must be > 0");
+    if (desc->solver_kind != BBG_SOLVER_PCISPH && desc->solver_kind != BBG_SOLVER_SPH)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "unknown solver kind");
+    for (int k = 0; k < 3; k++)
+        if (!(desc->domain_max[k] > desc->domain_min[k]))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "empty domain on axis %d", k);
+    int ndev = 0;
+    bbg_device_count(&ndev);
+    if (ndev <= 0) return fail(BBG_ERR_NO_DEVICE, "no CUDA device visible; bubbles_gb300 has no CPU path");
+    if (desc->device < 0 || desc->device >= ndev) return fail(BBG_ERR_INVALID_ARGUMENT, "bad device ordinal");
+    CK(cudaSetDevice(desc->device));
+
+    bbg_solver s = new (std::nothrow) bbg_solver_s();
+    if (!s) return fail(BBG_ERR_OUT_OF_MEMORY, "host allocation failed");
+    memset(&s->B, 0, sizeof(s->B));
+    memset(&s->P, 0, sizeof(s->P));
+    memset(&s->acc, 0, sizeof(s->acc));
+    s->desc = *desc;
+    s->capacity = capacity;
+    // grid in the reference's FP32 arithmetic
+    float minp[3], len[3], bmin[3], bmax[3];
+    build_grid(desc->domain_min, desc->domain_max, desc->target_spacing, desc->grid_spacing_scale,
+               s->dims, minp, len, bmin, bmax);
+    const unsigned long long total = (unsigned long long)s->dims[0] * s->dims[1] * s->dims[2];
+    if (total == 0 || total > 0x7fffffffull) {
+        delete s;
+        return fail(BBG_ERR_INVALID_ARGUMENT, "grid of %llu cells is out of range", total);
+    }
+    s->cells = (unsigned)total;
+    GridDev &g = s->P.g;
+    g.nx = s->dims[0]; g.ny = s->dims[1]; g.nz = s->dims[2];
+    g.total = s->cells;
+    for (int k = 0; k < 3; k++) {
+        g.minp[k] = minp[k]; g.len[k] = len[k]; g.bmin[k] = bmin[k]; g.bmax[k] = bmax[k];
+        s->dims_geo[k] = minp[k]; s->dims_geo[3 + k] = len[k];
+        s->dims_geo[6 + k] = bmin[k]; s->dims_geo[9 + k] = bmax[k];
+    }
+    s->kernel_radius = (float)desc->relative_kernel_radius * (float)desc->target_spacing;
+
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail(BBG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    s->stream = s->own_stream;
+    DevBufs &B = s->B;
+    B.prof = &s->prof;
+    const size_t n = (size_t)capacity;
+    bbg_status r = BBG_OK;
+#define ALLOC(ptr, cnt) if (!r) r = dalloc(&(ptr), (cnt))
+    ALLOC(B.pos[0], n); ALLOC(B.pos[1], n); ALLOC(B.vel[0], n); ALLOC(B.vel[1], n);
+    ALLOC(B.pid[0], n); ALLOC(B.pid[1], n); ALLOC(B.slot, n);
+    ALLOC(B.force, n); ALLOC(B.xstar, n); ALLOC(B.pforce, n); ALLOC(B.smoothed, n);
+    ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
+    ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
+    ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
+    ALLOC(B.partials, scan_partials_needed(s->cells));
+    ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);
+#undef ALLOC
+    if (!r && cudaMallocHost((void **)&s->h_st, sizeof(StepState)) != cudaSuccess)
+        r = fail(BBG_ERR_OUT_OF_MEMORY, "pinned allocation failed");
+    if (!r && cudaMallocHost((void **)&s->h_u, 64) != cudaSuccess)
+        r = fail(BBG_ERR_OUT_OF_MEMORY, "pinned allocation failed");
+    if (!r && cudaMemsetAsync(B.count, 0, sizeof(unsigned) * s->cells, s->stream) != cudaSuccess)
+        r = fail(BBG_ERR_CUDA, "memset failed");
+    if (!r && cudaMemsetAsync(B.st, 0, sizeof(StepState), s->stream) != cudaSuccess)
+        r = fail(BBG_ERR_CUDA, "memset failed");
+    if (!r && cudaStreamSynchronize(s->stream) != cudaSuccess) r = fail(BBG_ERR_CUDA, "sync failed");
+    if (r) {
+        free_all(s);
+        cudaStreamDestroy(s->own_stream);
+        delete s;
+        return r;
+    }
+    *out = s;
+    return BBG_OK;
+}
+
+bbg_status bbg_destroy(bbg_solver s) {
+    if (!s) return BBG_OK;
+    cudaSetDevice(s->desc.device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_all(s);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+    return BBG_OK;
+}
+
+bbg_status bbg_set_stream(bbg_solver s, void *stream) {
+    if (bbg_status r = check_solver(s)) return r;
+    CK(cudaStreamSynchronize(s->stream));
+    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    return BBG_OK;
+}
+
+bbg_status bbg_synchronize(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (count < 0 || count > kMaxColliders || (count > 0 && !shapes))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "collider count must be in [0, %d]", kMaxColliders);
+    for (int i = 0; i < count; i++) {
+        const bbg_shape &sh = shapes[i];
+        if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE)
+            return fail(BBG_ERR_INVALID_ARGUMENT, "collider %d: unknown shape type", i);
+        ShapeDev &d = s->P.shapes[i];
+        d.type = sh.type;
+        d.reverse = sh.reverse ? 1 : 0;
+        for (int k = 0; k < 3; k++) d.t[k] = (float)sh.center[k];
+        d.hx = (float)((double)(float)sh.size[0] / 2.0);
+        d.hy = (float)((double)(float)sh.size[1] / 2.0);
+        d.hz = (float)((double)(float)sh.size[2] / 2.0);
+        d.radius = (float)sh.size[0];
+        d.friction = (float)sh.friction;
+    }
+    s->P.nshapes = count;
+    return BBG_OK;
+}
+
+static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d_vel, int n) {
+    launch_upload(s->B, s->state, s->pid_cur, d_pos, d_vel, n, s->stream);
+    CK_LAUNCH();
+    s->n = n;
+    s->P.n = n;
+    s->grid_valid = false;
+    s->valid = kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) |
+               bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
+    return BBG_OK;
+}
+
+bbg_status bbg_upload_particles(bbg_solver s, const float *pos, const float *vel, int n) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!pos || n <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 positions");
+    if (n > s->capacity) return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", n, s->capacity);
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    CK(cudaMemcpyAsync(dp, pos, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    if (vel) CK(cudaMemcpyAsync(dv, vel, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    return upload_common(s, dp, vel ? dv : nullptr, n);
+}
+
+bbg_status bbg_upload_particles_device(bbg_solver s, const float *d_pos, const float *d_vel, int n) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!d_pos || n <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 positions");
+    if (n > s->capacity) return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", n, s->capacity);
+    return upload_common(s, d_pos, d_vel, n);
+}
+
+bbg_status bbg_setup(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "upload particles before bbg_setup");
+    const bbg_solver_desc &d = s->desc;
+    float mass = compute_mass(0, (float)d.target_density, (float)d.target_spacing, s->kernel_radius);
+    if (d.mass > 0) mass = (float)d.mass;
+    s->mass = mass > 0 ? mass : 0.f;
+    const float mo = s->mass / (float)d.target_density;
+    s->mod2 = mo * mo;
+    s->delta_denom = compute_delta_denom((float)d.target_spacing, s->kernel_radius);
+    fill_params(s);
+    s->setup_done = true;
+    return BBG_OK;
+}
+
+bbg_status bbg_update_grid_distribution(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    return grid_update(s);
+}
+
+bbg_status bbg_compute_particle_interaction(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    s->valid |= bit(BBG_FIELD_INTERACTION);
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_density(bbg_solver s, int compute_pressure) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    launch_density(s->P, s->B, s->state, compute_pressure ? 1 : 0, s->stream);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_DENSITY) | (compute_pressure ? bit(BBG_FIELD_PRESSURE) : 0u);
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_non_pressure_force(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_DENSITY))) return fail(BBG_ERR_STATE, "density not computed");
+    launch_non_pressure(s->P, s->B, s->state, 0, 0.f, 0.f, s->stream);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_FORCE);
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_delta(bbg_solver s, double dt, double *delta) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!delta) return fail(BBG_ERR_INVALID_ARGUMENT, "null delta");
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    *delta = compute_delta(s->mod2, s->delta_denom, (float)dt);
+    return BBG_OK;
+}
+
+bbg_status bbg_profiler_enable(bbg_solver s, int enable) {
+    if (bbg_status r = check_solver(s)) return r;
+    s->prof.on = enable != 0;
+    return BBG_OK;
+}
+
+bbg_status bbg_profiler_report(bbg_solver s, int max_kernels, char *names, double *total_ms,
+                               int32_t *launches, int32_t *kernel_count, int64_t *total_launches) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (max_kernels < 0 || (max_kernels > 0 && (!names || !total_ms || !launches)))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "invalid report buffers");
+    CK(cudaStreamSynchronize(s->stream));
+    double ms[KID_COUNT] = {0};
+    int cnt[KID_COUNT] = {0};
+    for (auto &r : s->prof.recs) {
+        if (r.skipped) continue;
+        float e = 0.f;
+        CK(cudaEventElapsedTime(&e, r.a, r.b));
+        ms[r.id] += e;
+        cnt[r.id] += 1;
+    }
+    int k = 0;
+    for (int id = 0; id < KID_COUNT && k < max_kernels; id++) {
+        if (!cnt[id]) continue;
+        memset(names + 32 * k, 0, 32);
+        strncpy(names + 32 * k, kernel_name(id), 31);
+        total_ms[k] = ms[id];
+        launches[k] = cnt[id];
+        k++;
+    }
+    if (kernel_count) *kernel_count = k;
+    if (total_launches) *total_launches = (int64_t)s->prof.launches;
+    s->prof.release();
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_pressure_force_and_integrate(bbg_solver s, double dt, double max_err,
+                                                    double delta, int max_it,
+                                                    bbg_step_stats *stats) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_FORCE)) || !(s->valid & bit(BBG_FIELD_DENSITY)))
+        return fail(BBG_ERR_STATE, "density and non-pressure force must be computed first");
+    if (max_it < 1 || max_it > kMaxIterations)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "max_iterations must be in [1, %d]", kMaxIterations);
+    const float fdt = (float)dt;
+    // PredictVelocityAndPositionFor with is_first = 1: p = 0, Fp = 0, x* from F only
+    CK(cudaMemsetAsync(s->B.st->err_bits, 0, sizeof(s->B.st->err_bits), s->stream));
+    CK(cudaMemsetAsync(s->B.st->err_sum, 0, sizeof(s->B.st->err_sum), s->stream));
+    CK(cudaMemsetAsync(&s->B.st->max_force_bits, 0, 4, s->stream));
+    s->P.max_err_ratio = (float)max_err;
+    launch_predict_first(s->P, s->B, s->state, fdt, fdt / s->mass, s->stream);
+    CK_LAUNCH();
+    bbg_status r = corrector(s, fdt, (float)delta, max_it);
+    if (r) return r;
+    r = pseudo_viscosity(s, fdt);
+    if (r) return r;
+    if (stats) {
+        memset(&s->acc, 0, sizeof(s->acc));
+        if ((r = read_step_state(s))) return r;
+        add_substep_stats(s, fdt);
+        *stats = s->acc;
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_pressure_force(bbg_solver s, double dt) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_DENSITY)) || !(s->valid & bit(BBG_FIELD_PRESSURE)))
+        return fail(BBG_ERR_STATE, "density and pressure must be computed first");
+    launch_sph_forces(s->P, s->B, s->state, (float)dt, s->stream);
+    CK_LAUNCH();
+    s->state = 1 - s->state;
+    s->valid |= kPosVel | bit(BBG_FIELD_FORCE);
+    return BBG_OK;
+}
+
+bbg_status bbg_time_integration(bbg_solver s, double dt) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (!(s->valid & bit(BBG_FIELD_FORCE))) return fail(BBG_ERR_STATE, "forces not valid");
+    launch_integrate(s->P, s->B, s->state, (float)dt, s->stream);
+    CK_LAUNCH();
+    // the other buffer now holds the integrated state in the same slot order
+    s->state = 1 - s->state;
+    return BBG_OK;
+}
+
+bbg_status bbg_compute_pseudo_viscosity_interpolation(bbg_solver s, double dt) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    return pseudo_viscosity(s, (float)dt);
+}
+
+bbg_status bbg_compute_number_of_time_steps(bbg_solver s, double remaining, double scale,
+                                            unsigned *count) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!count) return fail(BBG_ERR_INVALID_ARGUMENT, "null count");
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    float mf = 0;
+    if (bbg_status r = max_force(s, &mf)) return r;
+    *count = number_of_time_steps((float)remaining, (float)s->desc.sound_speed, (float)scale,
+                                  s->kernel_radius, s->mass, mf);
+    return BBG_OK;
+}
+
+bbg_status bbg_advance_time_step(bbg_solver s, double dt, bbg_step_stats *stats) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (!(dt > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    bbg_status r = substep(s, (float)dt);
+    if (r) return r;
+    if (stats) {
+        memset(&s->acc, 0, sizeof(s->acc));
+        if ((r = read_step_state(s))) return r;
+        add_substep_stats(s, (float)dt);
+        *stats = s->acc;
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_advance(bbg_solver s, double dt, bbg_step_stats *stats) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (!(dt > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    memset(&s->acc, 0, sizeof(s->acc));
+    float remaining = (float)dt;
+    while (remaining > 0.0001f) {   // Epsilon, src/core/geometry.h:44
+        float mf = 0;
+        bbg_status r = max_force(s, &mf);
+        if (r) return r;
+        unsigned nsteps = number_of_time_steps(remaining, (float)s->desc.sound_speed,
+                                               (float)s->desc.time_step_limit_scale,
+                                               s->kernel_radius, s->mass, mf);
+        if (nsteps == 0) nsteps = 1;
+        const float step = remaining / (float)nsteps;
+        if ((r = substep(s, step))) return r;
+        if ((r = read_step_state(s))) return r;
+        add_substep_stats(s, step);
+        remaining -= step;
+    }
+    if (stats) *stats = s->acc;
+    return BBG_OK;
+}
+
+bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!stats) return fail(BBG_ERR_INVALID_ARGUMENT, "null stats");
+    memset(&s->acc, 0, sizeof(s->acc));
+    if (bbg_status r = read_step_state(s)) return r;
+    add_substep_stats(s, 0.f);
+    s->acc.substeps = 0;
+    *stats = s->acc;
+    return BBG_OK;
+}
+
+bbg_status bbg_particle_count(bbg_solver s, int *n) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!n) return fail(BBG_ERR_INVALID_ARGUMENT, "null n");
+    *n = s->n;
+    return BBG_OK;
+}
+
+bbg_status bbg_get_field(bbg_solver s, int field, float *out) {
+    if (bbg_status r = check_solver(s)) return r;
+    const int comps = field_components(field);
+    if (!comps || !out) return fail(BBG_ERR_INVALID_ARGUMENT, "unknown field %d", field);
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    if (!(s->valid & bit(field)))
+        return fail(BBG_ERR_STATE, "field %d is not valid in the current particle order", field);
+    const size_t n = (size_t)s->n;
+    if (field == BBG_FIELD_INTERACTION) {
+        for (size_t i = 0; i < n; i++) {
+            out[3 * i] = (float)s->desc.gravity[0];
+            out[3 * i + 1] = (float)s->desc.gravity[1];
+            out[3 * i + 2] = (float)s->desc.gravity[2];
+        }
+        return BBG_OK;
+    }
+    if (comps == 3) launch_get_vec(vec_field(s, field), s->B.slot, s->B.stage, s->n, s->stream);
+    else launch_get_scalar(scalar_field(s, field), s->B.slot, s->B.stage, s->n, s->stream);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(out, s->B.stage, sizeof(float) * comps * n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_set_field(bbg_solver s, int field, const float *in) {
+    if (bbg_status r = check_solver(s)) return r;
+    const int comps = field_components(field);
+    if (!comps || !in || field == BBG_FIELD_INTERACTION)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "field %d cannot be set", field);
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    const size_t n = (size_t)s->n;
+    CK(cudaMemcpyAsync(s->B.stage, in, sizeof(float) * comps * n, cudaMemcpyHostToDevice, s->stream));
+    if (comps == 3) launch_set_vec(vec_field(s, field), s->B.slot, s->B.stage, s->n, s->stream);
+    else launch_set_scalar(scalar_field(s, field), s->B.slot, s->B.stage, s->n, s->stream);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->stream));
+    s->valid |= bit(field);
+    return BBG_OK;
+}
+
+bbg_status bbg_download(bbg_solver s, float *pos, float *vel) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    const size_t n = (size_t)s->n;
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    launch_download(s->B, s->state, s->pid_cur, pos ? dp : nullptr, vel ? dv : nullptr, s->n, s->stream);
+    CK_LAUNCH();
+    if (pos) CK(cudaMemcpyAsync(pos, dp, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    if (vel) CK(cudaMemcpyAsync(vel, dv, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_download_device(bbg_solver s, float *d_pos, float *d_vel) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    launch_download(s->B, s->state, s->pid_cur, d_pos, d_vel, s->n, s->stream);
+    CK_LAUNCH();
+    return BBG_OK;
+}
+
+bbg_status bbg_get_scalars(bbg_solver s, double out[8]) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!out) return fail(BBG_ERR_INVALID_ARGUMENT, "null out");
+    out[0] = s->mass;
+    out[1] = s->kernel_radius;
+    out[2] = s->delta_denom;
+    out[3] = s->mod2;
+    out[4] = (float)s->desc.target_spacing;
+    out[5] = (float)s->desc.target_density;
+    out[6] = (float)s->desc.target_spacing;
+    out[7] = (float)s->desc.relative_kernel_radius;
+    return BBG_OK;
+}
+
+bbg_status bbg_get_grid(bbg_solver s, int dims[3], double geo[12]) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!dims || !geo) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
+    for (int k = 0; k < 3; k++) dims[k] = s->dims[k];
+    for (int k = 0; k < 12; k++) geo[k] = s->dims_geo[k];
+    return BBG_OK;
+}
+
+bbg_status bbg_dump_grid(bbg_solver s, uint32_t *cell_of_particle, uint32_t *cell_counts,
+                         uint32_t *sorted_ids) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    const size_t n = (size_t)s->n;
+    if (cell_of_particle) {
+        launch_get_uint(s->B.cell, s->B.slot, (unsigned *)s->B.stage, s->n, s->stream);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(cell_of_particle, s->B.stage, 4 * n, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (sorted_ids) {
+        CK(cudaMemcpyAsync(sorted_ids, s->B.pid[s->pid_cur], 4 * n, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (cell_counts) {
+        unsigned *tmp = new (std::nothrow) unsigned[(size_t)s->cells + 1];
+        if (!tmp) return fail(BBG_ERR_OUT_OF_MEMORY, "host allocation failed");
+        cudaError_t e = cudaMemcpyAsync(tmp, s->B.start, 4 * ((size_t)s->cells + 1),
+                                        cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            delete[] tmp;
+            return fail(BBG_ERR_CUDA, "grid copy: %s", cudaGetErrorString(e));
+        }
+        for (unsigned c = 0; c < s->cells; c++) cell_counts[c] = tmp[c + 1] - tmp[c];
+        delete[] tmp;
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!counts) return fail(BBG_ERR_INVALID_ARGUMENT, "null counts");
+    if (!(s->valid & bit(BBG_FIELD_DENSITY))) return fail(BBG_ERR_STATE, "density not computed");
+    launch_get_int(s->B.nbr, s->B.slot, (int *)s->B.stage, s->n, s->stream);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(counts, s->B.stage, 4 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+}  // extern "C"

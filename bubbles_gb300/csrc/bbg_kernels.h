@@ -1,0 +1,67 @@
+// bbg_kernels.h -- host-callable launchers of the bubbles_gb300 kernels.
+#pragma once
+
+#include "bbg_internal.cuh"
+#include "prof.h"
+
+namespace bbg {
+
+// Device buffers of one solver (all sized for `capacity` particles / grid cells).
+struct DevBufs {
+    float4 *pos[2], *vel[2];   // ping-pong particle state
+    int *pid[2];               // original id of each sorted slot
+    int *slot;                 // sorted slot of each original id
+    float4 *force, *xstar, *pforce, *smoothed;
+    float *rho, *press, *rhostar, *derr;
+    unsigned *cell;            // cell id of each sorted slot (last grid update)
+    unsigned *cell_old;        // scratch: cell id of each pre-sort slot
+    unsigned *sub;             // scratch: arrival index inside the cell
+    unsigned *count;           // per-cell counts (kept zero between updates)
+    unsigned *start;           // cell start offsets, total + 1 entries
+    unsigned *partials;        // scan partials
+    uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
+    int *nbr;                  // neighbour count of each sorted slot
+    StepState *st;
+    float *stage;              // n * 3 floats of staging for host copies
+    unsigned *red;             // reduction scratch (max |F|)
+    Prof *prof;                // host-side launch profiler (may be null)
+};
+
+#define BBG_PBEGIN(B, id, s, it) do { if ((B).prof) (B).prof->begin((id), (s), (it)); } while (0)
+#define BBG_PEND(B, s) do { if ((B).prof) (B).prof->end(s); } while (0)
+
+// grid.cu
+size_t scan_partials_needed(unsigned cells);
+void launch_grid_update(const Params &P, const DevBufs &B, int src_buf, int pid_src,
+                        cudaStream_t s);
+void launch_upload(const DevBufs &B, int buf, int pid_buf, const float *d_pos, const float *d_vel,
+                   int n, cudaStream_t s);
+void launch_download(const DevBufs &B, int buf, int pid_buf, float *d_pos, float *d_vel, int n,
+                     cudaStream_t s);
+// field gather/scatter between caller order (n*3 or n floats) and sorted slots
+void launch_get_vec(const float4 *src, const int *slot, float *out, int n, cudaStream_t s);
+void launch_set_vec(float4 *dst, const int *slot, const float *in, int n, cudaStream_t s);
+void launch_get_scalar(const float *src, const int *slot, float *out, int n, cudaStream_t s);
+void launch_set_scalar(float *dst, const int *slot, const float *in, int n, cudaStream_t s);
+void launch_get_uint(const unsigned *src, const int *slot, unsigned *out, int n, cudaStream_t s);
+void launch_get_int(const int *src, const int *slot, int *out, int n, cudaStream_t s);
+void launch_fill_vec(float4 *dst, float x, float y, float z, int n, cudaStream_t s);
+void launch_max_force(const float4 *force, int n, unsigned *out_bits, cudaStream_t s);
+
+// sph.cu
+void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure,
+                    cudaStream_t s);
+void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
+                         float dt_over_m, cudaStream_t s);
+void launch_predict_first(const Params &P, const DevBufs &B, int buf, float dt, float dt_over_m,
+                          cudaStream_t s);
+void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
+                         cudaStream_t s);
+void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,
+                           float dt, float dt_over_m, cudaStream_t s);
+void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
+void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
+void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
+                             cudaStream_t s);
+
+}  // namespace bbg

@@ -1,0 +1,418 @@
+// sph.cu -- neighbour-sum passes of the 3D SPH / PCISPH step (FP32, one thread per
+// particle over the cell-sorted arrays).
+//
+// Neighbour sets follow the reference buckets: j is a neighbour of i when
+// IsWithinStd(|x_i - x_j|, h) holds at the positions of the last grid update
+// (src/core/grid.h:423-447).  Instead of materialising a 100-slot bucket per particle
+// (400 B) the kernels re-test the 27 neighbour cells (9 contiguous slot ranges) at
+// every pass with the exact FP32 membership test; the predicted-density pass tests
+// membership at step-start positions and sums at predicted positions, which is what
+// the reference does with its stale bucket (src/equations/pcisph_equations3.cpp:58-89).
+//
+// Fusions (per PCISPH substep: density, non-pressure, 2 per corrector iteration):
+//   - non-pressure force + the k = 0 prediction (PredictVelocityAndPositionFor);
+//   - pressure force of iteration k + either the prediction of iteration k+1 or, once
+//     the density error of iteration k is below tolerance (or k is the last allowed
+//     iteration), AccumulateForcesFor + TimeIntegrationFor into the other buffer.
+// The iteration decision is read from device memory (max error of each iteration), so
+// the host launches max_iterations x 2 kernels without synchronising; kernels of
+// iterations after convergence return immediately.
+#include "bbg_kernels.h"
+
+namespace bbg {
+
+constexpr int kThreads = 128;
+
+static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// True when some corrector iteration before k already met the tolerance
+// (ComputePressureForceAndIntegrate's break, pcisph_equations3.cpp:243-246).
+__device__ __forceinline__ bool converged_before(const Params &P, const StepState *st, int k) {
+    for (int q = 0; q < k; q++) {
+        float e = __uint_as_float(st->err_bits[q]);
+        if (fdv(e, P.target_density) < P.max_err_ratio) return true;
+    }
+    return false;
+}
+
+// ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58
+__global__ void __launch_bounds__(kThreads)
+k_density(Params P, const float4 *__restrict__ pos, const unsigned *__restrict__ cell,
+          const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ press,
+          int *__restrict__ nbr, int compute_pressure, StepState *st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 pi = pos[i];
+    float sum = 0.f;
+    int cnt = 0;
+    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+        const float4 pj = __ldg(&pos[j]);
+        const float r2 = dist2(pi, pj);
+        if (std_member(P, pi, pj, r2)) {
+            const float x = 1.f - r2 * P.inv_h2;
+            sum += x * x * x;
+            cnt++;
+        }
+    });
+    const float di = sum * P.std_c * P.mass;
+    if (compute_pressure) {
+        float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
+        if (p < 0.f) p *= P.neg_scale;
+        press[i] = p;
+    }
+    rho[i] = di;
+    nbr[i] = cnt;
+    if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
+}
+
+// ComputeNonPressureForceFor (sph_equations3.cpp:80-110), optionally followed by the
+// k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).
+__global__ void __launch_bounds__(kThreads)
+k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+               const float *__restrict__ rho, const unsigned *__restrict__ cell,
+               const unsigned *__restrict__ start, float4 *__restrict__ force,
+               float4 *__restrict__ xstar, float4 *__restrict__ pforce, float *__restrict__ press,
+               int predict, float dt, float dt_over_m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 pi = pos[i];
+    const float4 vi = vel[i];
+    float fx = P.mass * P.gx - P.drag * vi.x;
+    float fy = P.mass * P.gy - P.drag * vi.y;
+    float fz = P.mass * P.gz - P.drag * vi.z;
+    const float kv = P.visc_m2 * P.spiky_d2w_c;
+    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+        const float4 pj = __ldg(&pos[j]);
+        const float r2 = dist2(pi, pj);
+        if (std_member(P, pi, pj, r2)) {
+            const float d = sqrtf(r2);
+            const float w = kv * (1.f - d * P.inv_h) / __ldg(&rho[j]);
+            const float4 vj = __ldg(&vel[j]);
+            fx += (vj.x - vi.x) * w;
+            fy += (vj.y - vi.y) * w;
+            fz += (vj.z - vi.z) * w;
+        }
+    });
+    force[i] = make_float4(fx, fy, fz, 0.f);
+    if (predict) {
+        press[i] = 0.f;
+        pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        v3 xs;
+        predict_particle(P, dt, dt_over_m, V(fx, fy, fz), V(0.f, 0.f, 0.f), V(pi), V(vi), &xs);
+        xstar[i] = F4(xs);
+    }
+}
+
+// PredictVelocityAndPositionFor with is_first = 1 (pcisph_equations3.cpp:13-27) on the
+// forces already in `force`: p = 0, Fp = 0, x* from F alone.
+__global__ void __launch_bounds__(kThreads)
+k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                const float4 *__restrict__ force, float4 *__restrict__ xstar,
+                float4 *__restrict__ pforce, float *__restrict__ press, float dt, float dt_over_m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    press[i] = 0.f;
+    pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    v3 xs;
+    predict_particle(P, dt, dt_over_m, V(force[i]), V(0.f, 0.f, 0.f), V(pos[i]), V(vel[i]), &xs);
+    xstar[i] = F4(xs);
+}
+
+// PredictPressureFor (pcisph_equations3.cpp:60-90) with the density error stored
+// (tolerance mode) and reduced to max |err| and sum |err| for iteration k.
+__global__ void __launch_bounds__(kThreads)
+k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ xstar,
+               const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+               float *__restrict__ press, float *__restrict__ rhostar, float *__restrict__ derr,
+               StepState *st, int k, float delta) {
+    if (converged_before(P, st, k)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float aerr = 0.f;
+    if (i < P.n) {
+        const float4 pi = pos[i];
+        const float4 xi = xstar[i];
+        float sum = 0.f;
+        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+            const float4 pj = __ldg(&pos[j]);
+            if (std_member(P, pi, pj, dist2(pi, pj))) {
+                const float4 xj = __ldg(&xstar[j]);
+                const float r2 = dist2(xi, xj);
+                if (r2 < P.h2mz) {
+                    const float x = 1.f - r2 * P.inv_h2;
+                    sum += x * x * x;
+                }
+            }
+        });
+        const float density = sum * P.std_c * P.mass;
+        float err = density - P.target_density;
+        float pr = delta * err;
+        if (pr < 0.f) {
+            pr *= P.neg_scale;
+            err *= P.neg_scale;
+        }
+        press[i] += pr;
+        rhostar[i] = density;
+        derr[i] = err;
+        aerr = fabsf(err);
+    }
+    // block reduction: max |err| (exact as bits of non-negative floats), sum |err| in FP64
+    __shared__ unsigned smax[kThreads / 32];
+    __shared__ double ssum[kThreads / 32];
+    const unsigned m = warp_max_u(__float_as_uint(aerr));
+    const double s = warp_sum_d((double)aerr);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { smax[wid] = m; ssum[wid] = s; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned bm = 0;
+        double bs = 0.0;
+        for (int w = 0; w < kThreads / 32; w++) { bm = max(bm, smax[w]); bs += ssum[w]; }
+        if (bm) atomicMax(&st->err_bits[k], bm);
+        atomicAdd(&st->err_sum[k], bs);
+    }
+}
+
+// PredictPressureForceFor (pcisph_equations3.cpp:114-155) at the current positions,
+// then either the next prediction or AccumulateForcesFor + TimeIntegrationFor.
+__global__ void __launch_bounds__(kThreads)
+k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                 const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+                 const float *__restrict__ press, const float *__restrict__ rhostar,
+                 float4 *__restrict__ force, float4 *__restrict__ pforce,
+                 float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
+                 float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
+                 float dt_over_m) {
+    if (converged_before(P, st, k)) return;
+    const bool last = (k == max_it - 1) ||
+                      fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned fbits = 0;
+    if (i < P.n) {
+        const float4 pi = pos[i];
+        const float di = rhostar[i];
+        const float ai = press[i] / (di * di);
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        const float kg = P.m2 * P.spiky_dw_c;
+        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+            if (j == (unsigned)i) return;
+            const float4 pj = __ldg(&pos[j]);
+            const float r2 = dist2(pi, pj);
+            if (!std_member(P, pi, pj, r2)) return;
+            const float d = sqrtf(r2);
+            // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
+            if (d - P.h <= -P.iz && d >= P.iz) {
+                const float dj = __ldg(&rhostar[j]);
+                const float aj = __ldg(&press[j]) / (dj * dj);
+                const float x = 1.f - d * P.inv_h;
+                const float c = kg * (ai + aj) * x * x / d;
+                tx += (pj.x - pi.x) * c;
+                ty += (pj.y - pi.y) * c;
+                tz += (pj.z - pi.z) * c;
+            }
+        });
+        const v3 fp = V(-tx, -ty, -tz);
+        pforce[i] = F4(fp);
+        const float4 f4 = force[i];
+        const v3 f = V(f4);
+        if (last) {
+            const v3 ft = vadd(f, fp);
+            force[i] = F4(ft);
+            v3 x = V(pi), v = V(vel[i]);
+            integrate_particle(P, dt, ft, &x, &v);
+            pos_out[i] = F4(x);
+            vel_out[i] = F4(v);
+            fbits = __float_as_uint(vlen(ft));
+        } else {
+            v3 xs;
+            predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
+            xstar[i] = F4(xs);
+        }
+    }
+    if (last) {
+        fbits = warp_max_u(fbits);
+        if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
+    }
+}
+
+// ComputeAllForcesFor (sph_equations3.cpp:184-278, extended = 0) in Jacobi order: the
+// reference integrates each particle inside the force loop (:277), racing with its
+// neighbours' reads; here all forces read the step-start state and the integrated
+// state goes to the other buffer.
+__global__ void __launch_bounds__(kThreads)
+k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+             const float *__restrict__ rho, const float *__restrict__ press,
+             const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+             float4 *__restrict__ force, float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+             StepState *st, float dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned fbits = 0;
+    if (i < P.n) {
+        const float4 pi = pos[i];
+        const float4 vi = vel[i];
+        const float di = rho[i];
+        const float ai = press[i] / (di * di);
+        float fx = P.mass * P.gx - P.drag * vi.x;
+        float fy = P.mass * P.gy - P.drag * vi.y;
+        float fz = P.mass * P.gz - P.drag * vi.z;
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        const float kg = P.m2 * P.spiky_dw_c;
+        const float kv = P.visc_m2 * P.spiky_d2w_c;
+        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+            if (j == (unsigned)i) return;
+            const float4 pj = __ldg(&pos[j]);
+            const float r2 = dist2(pi, pj);
+            if (!std_member(P, pi, pj, r2)) return;
+            const float d = sqrtf(r2);
+            if (d - P.h <= -P.iz) {
+                const float dj = __ldg(&rho[j]);
+                const float x = 1.f - d * P.inv_h;
+                if (d >= P.iz) {
+                    const float aj = __ldg(&press[j]) / (dj * dj);
+                    const float c = kg * (ai + aj) * x * x / d;
+                    tx += (pj.x - pi.x) * c;
+                    ty += (pj.y - pi.y) * c;
+                    tz += (pj.z - pi.z) * c;
+                }
+                const float4 vj = __ldg(&vel[j]);
+                const float w = kv * x / dj;
+                fx += (vj.x - vi.x) * w;
+                fy += (vj.y - vi.y) * w;
+                fz += (vj.z - vi.z) * w;
+            }
+        });
+        const v3 f = V(fx - tx, fy - ty, fz - tz);
+        force[i] = F4(f);
+        v3 x = V(pi), v = V(vi);
+        integrate_particle(P, dt, f, &x, &v);
+        pos_out[i] = F4(x);
+        vel_out[i] = F4(v);
+        fbits = __float_as_uint(vlen(f));
+    }
+    fbits = warp_max_u(fbits);
+    if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
+}
+
+// TimeIntegrationFor over all particles (TimeIntegrationGPU, sph_equations3.cpp:622-634)
+__global__ void __launch_bounds__(kThreads)
+k_integrate(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+            const float4 *__restrict__ force, float4 *__restrict__ pos_out,
+            float4 *__restrict__ vel_out, float dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    v3 x = V(pos[i]), v = V(vel[i]);
+    integrate_particle(P, dt, V(force[i]), &x, &v);
+    pos_out[i] = F4(x);
+    vel_out[i] = F4(v);
+}
+
+// ComputePseudoViscosityAggregationKernelFor (sph_equations3.cpp:341-371): membership
+// from the step-start positions (the bucket), values at the integrated state.
+__global__ void __launch_bounds__(kThreads)
+k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
+               const float4 *__restrict__ vel, const float *__restrict__ rho,
+               const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+               float4 *__restrict__ smoothed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 oi = pos_old[i];
+    const float4 pi = pos[i];
+    float sx = 0.f, sy = 0.f, sz = 0.f, ws = 0.f;
+    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+        const float4 oj = __ldg(&pos_old[j]);
+        if (!std_member(P, oi, oj, dist2(oi, oj))) return;
+        const float4 pj = __ldg(&pos[j]);
+        const float d = sqrtf(dist2(pi, pj));
+        if (d - P.h <= -P.iz) {
+            const float x = 1.f - d * P.inv_h;
+            const float wj = P.mass / __ldg(&rho[j]) * (P.spiky_w_c * x * x * x);
+            const float4 vj = __ldg(&vel[j]);
+            ws += wj;
+            sx += wj * vj.x;
+            sy += wj * vj.y;
+            sz += wj * vj.z;
+        }
+    });
+    if (ws > 0.f) {
+        const float inv = 1.f / ws;
+        sx *= inv; sy *= inv; sz *= inv;
+    }
+    smoothed[i] = make_float4(sx, sy, sz, 0.f);
+}
+
+// ComputePseudoViscosityInterpolationKernelFor (sph_equations3.cpp:373-382)
+__global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *__restrict__ smoothed,
+                                 float t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = vel[i], s = smoothed[i];
+    const float a = 1.f - t;
+    vel[i] = make_float4(v.x * a + s.x * t, v.y * a + s.y * t, v.z * a + s.z * t, 0.f);
+}
+
+void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
+    BBG_PBEGIN(B, KID_DENSITY, s, -1);
+    k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.cell, B.start, B.rho,
+                                                             B.press, B.nbr, compute_pressure, B.st);
+    BBG_PEND(B, s);
+}
+
+void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
+                         float dt_over_m, cudaStream_t s) {
+    BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
+    k_non_pressure<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.vel[buf], B.rho, B.cell, B.start, B.force, B.xstar, B.pforce, B.press,
+        predict, dt, dt_over_m);
+    BBG_PEND(B, s);
+}
+
+void launch_predict_first(const Params &P, const DevBufs &B, int buf, float dt, float dt_over_m,
+                          cudaStream_t s) {
+    BBG_PBEGIN(B, KID_PREDICT_FIRST, s, -1);
+    k_predict_first<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.vel[buf], B.force, B.xstar, B.pforce, B.press, dt, dt_over_m);
+    BBG_PEND(B, s);
+}
+
+void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
+                         cudaStream_t s) {
+    BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
+    k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.xstar, B.cell, B.start, B.press, B.rhostar, B.derr, B.st, k, delta);
+    BBG_PEND(B, s);
+}
+
+void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it, float dt,
+                           float dt_over_m, cudaStream_t s) {
+    BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
+    k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.press, B.rhostar, B.force, B.pforce, B.xstar,
+        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m);
+    BBG_PEND(B, s);
+}
+
+void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
+    BBG_PBEGIN(B, KID_SPH_FORCES, s, -1);
+    k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.vel[buf], B.rho, B.press, B.cell, B.start, B.force, B.pos[1 - buf],
+        B.vel[1 - buf], B.st, dt);
+    BBG_PEND(B, s);
+}
+
+void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
+    BBG_PBEGIN(B, KID_INTEGRATE, s, -1);
+    k_integrate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.vel[buf], B.force,
+                                                               B.pos[1 - buf], B.vel[1 - buf], dt);
+    BBG_PEND(B, s);
+}
+
+void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
+                             cudaStream_t s) {
+    BBG_PBEGIN(B, KID_PSEUDO_VISCOSITY, s, -1);
+    k_pv_aggregate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.rho, B.cell, B.start, B.smoothed);
+    k_pv_interpolate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.vel[new_buf], B.smoothed,
+                                                                    factor);
+    BBG_PEND(B, s);
+}
+
+}  // namespace bbg

@@ -1,0 +1,304 @@
+"""Python mirror of the reference solver API over the bbg C ABI.
+
+`PciSphSolver3` and `SphSolver3` keep the reference's method names
+(src/core/pcisph_solver.h:56-83, src/core/sph_solver.h:76-96) and free-function
+passes (src/core/sph_solver.h:124-196, src/core/pcisph_solver.h:85-99).  Host arrays
+are numpy float32 (n, 3) / (n,); device variants take torch CUDA tensors.  Every
+failure raises `BbgError` -- there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+def _fptr(a):
+    return a.ctypes.data_as(N._FP)
+
+
+def desc_from_scene(scene, device=0):
+    """bbg_solver_desc from a scene dict (see bubbles_gb300.scenes)."""
+    d = N.SolverDesc()
+    kind = N.SOLVER_SPH if scene.get("solver", "pcisph") == "sph" else N.SOLVER_PCISPH
+    N.call("bbg_solver_desc_default", ctypes.byref(d), kind)
+    for key in ("eos_exponent", "negative_pressure_scale", "viscosity", "pseudo_viscosity",
+                "sound_speed", "drag_coefficient", "target_density", "relative_kernel_radius",
+                "grid_spacing_scale", "time_step_limit_scale", "max_density_error_ratio"):
+        if key in scene:
+            setattr(d, key, float(scene[key]))
+    d.target_spacing = float(scene["spacing"])
+    d.mass = float(scene.get("mass", 0.0) or 0.0)
+    if "gravity" in scene:
+        for k in range(3):
+            d.gravity[k] = float(scene["gravity"][k])
+    for k in range(3):
+        d.domain_min[k] = float(scene["domain_min"][k])
+        d.domain_max[k] = float(scene["domain_max"][k])
+    mode = scene.get("pcisph_mode", "tolerance")
+    d.pcisph_mode = N.PCISPH_TOLERANCE if mode == "tolerance" else N.PCISPH_AS_SHIPPED
+    d.max_iterations = int(scene.get("max_iterations", 20 if mode == "tolerance" else 5))
+    d.device = int(device)
+    return d
+
+
+def shapes_from_scene(scene):
+    cols = scene.get("colliders", [])
+    arr = (N.Shape * max(1, len(cols)))()
+    for i, c in enumerate(cols):
+        arr[i].type = N.SHAPE_BOX if c["type"] == "box" else N.SHAPE_SPHERE
+        arr[i].reverse = 1 if c.get("reverse", False) else 0
+        for k in range(3):
+            arr[i].center[k] = float(c.get("center", (0.0, 0.0, 0.0))[k])
+        if c["type"] == "box":
+            for k in range(3):
+                arr[i].size[k] = float(c["size"][k])
+        else:
+            arr[i].size[0] = float(c["radius"])
+        arr[i].friction = float(c.get("friction", 0.0))
+    return arr, len(cols)
+
+
+class Solver:
+    """One GPU particle system (PciSphSolver3 or SphSolver3 semantics)."""
+
+    def __init__(self, scene, capacity=None, device=0, pos=None, vel=None, setup=True):
+        self.scene = scene
+        self.desc = desc_from_scene(scene, device)
+        n = capacity if capacity is not None else (len(pos) if pos is not None else 0)
+        if n <= 0:
+            raise ValueError("need a capacity or initial positions")
+        h = ctypes.c_void_p()
+        N.call("bbg_create", ctypes.byref(self.desc), int(n), ctypes.byref(h))
+        self.h = h
+        shapes, count = shapes_from_scene(scene)
+        N.call("bbg_set_colliders", self.h, shapes, count)
+        self.n = 0
+        if pos is not None:
+            self.upload(pos, vel)
+            if setup:
+                self.setup()
+
+    # lifetime ---------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            N.load().bbg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # particles ---------------------------------------------------------------
+    def upload(self, pos, vel=None):
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+        N.call("bbg_upload_particles", self.h, _fptr(p), _fptr(v) if v is not None else None,
+               int(p.shape[0]))
+        self.n = int(p.shape[0])
+
+    def upload_device(self, pos, vel=None):
+        """pos/vel: contiguous float32 CUDA tensors of shape (n, 3)."""
+        n = int(pos.shape[0])
+        N.call("bbg_upload_particles_device", self.h, ctypes.c_void_p(pos.data_ptr()),
+               ctypes.c_void_p(vel.data_ptr()) if vel is not None else None, n)
+        self.n = n
+
+    def setup(self):
+        N.call("bbg_setup", self.h)
+
+    def set_colliders(self, colliders):
+        scene = dict(self.scene, colliders=colliders)
+        shapes, count = shapes_from_scene(scene)
+        N.call("bbg_set_colliders", self.h, shapes, count)
+
+    def set_stream(self, stream):
+        """stream: a torch.cuda.Stream (or None for the solver's own stream)."""
+        N.call("bbg_set_stream", self.h, ctypes.c_void_p(stream.cuda_stream) if stream else None)
+
+    def synchronize(self):
+        N.call("bbg_synchronize", self.h)
+
+    # stepping ----------------------------------------------------------------
+    def advance(self, dt):
+        st = N.StepStats()
+        N.call("bbg_advance", self.h, float(dt), ctypes.byref(st))
+        return st.as_dict()
+
+    def advance_time_step(self, dt, stats=False):
+        if not stats:
+            N.call("bbg_advance_time_step", self.h, float(dt), None)
+            return None
+        st = N.StepStats()
+        N.call("bbg_advance_time_step", self.h, float(dt), ctypes.byref(st))
+        return st.as_dict()
+
+    def stats(self):
+        st = N.StepStats()
+        N.call("bbg_get_stats", self.h, ctypes.byref(st))
+        return st.as_dict()
+
+    # passes --------------------------------------------------------------------
+    def update_grid_distribution(self):
+        N.call("bbg_update_grid_distribution", self.h)
+
+    def compute_particle_interaction(self):
+        N.call("bbg_compute_particle_interaction", self.h)
+
+    def compute_density(self, compute_pressure=1):
+        N.call("bbg_compute_density", self.h, int(compute_pressure))
+
+    def compute_non_pressure_force(self):
+        N.call("bbg_compute_non_pressure_force", self.h)
+
+    def compute_pressure_force(self, dt):
+        N.call("bbg_compute_pressure_force", self.h, float(dt))
+
+    def time_integration(self, dt):
+        N.call("bbg_time_integration", self.h, float(dt))
+
+    def compute_pseudo_viscosity_interpolation(self, dt):
+        N.call("bbg_compute_pseudo_viscosity_interpolation", self.h, float(dt))
+
+    def compute_pressure_force_and_integrate(self, dt, max_err, delta, max_it):
+        st = N.StepStats()
+        N.call("bbg_compute_pressure_force_and_integrate", self.h, float(dt), float(max_err),
+               float(delta), int(max_it), ctypes.byref(st))
+        return st.as_dict()
+
+    def compute_delta(self, dt):
+        d = ctypes.c_double()
+        N.call("bbg_compute_delta", self.h, float(dt), ctypes.byref(d))
+        return d.value
+
+    def compute_number_of_time_steps(self, remaining, scale):
+        c = ctypes.c_uint()
+        N.call("bbg_compute_number_of_time_steps", self.h, float(remaining), float(scale),
+               ctypes.byref(c))
+        return c.value
+
+    # state ---------------------------------------------------------------------
+    def get(self, field):
+        shape = (self.n, 3) if field in N.VECTOR_FIELDS else (self.n,)
+        out = np.zeros(shape, np.float32)
+        N.call("bbg_get_field", self.h, int(field), _fptr(out))
+        return out
+
+    def set(self, field, values):
+        shape = (self.n, 3) if field in N.VECTOR_FIELDS else (self.n,)
+        a = np.ascontiguousarray(values, dtype=np.float32).reshape(shape)
+        N.call("bbg_set_field", self.h, int(field), _fptr(a))
+
+    def download(self, out_pos=None, out_vel=None):
+        """Positions and velocities in the caller's particle order (float32 (n, 3))."""
+        p = out_pos if out_pos is not None else np.zeros((self.n, 3), np.float32)
+        v = out_vel if out_vel is not None else np.zeros((self.n, 3), np.float32)
+        for a in (p, v):
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != 3 * self.n:
+                raise ValueError("download buffers must be contiguous float32 (n, 3)")
+        N.call("bbg_download", self.h, _fptr(p), _fptr(v))
+        return p, v
+
+    def download_device(self, pos, vel):
+        N.call("bbg_download_device", self.h, ctypes.c_void_p(pos.data_ptr()),
+               ctypes.c_void_p(vel.data_ptr()))
+
+    def scalars(self):
+        out = (ctypes.c_double * 8)()
+        N.call("bbg_get_scalars", self.h, out)
+        keys = ["mass", "kernel_radius", "delta_denom", "mass_over_density_sq",
+                "target_spacing", "target_density", "radius", "relative_radius"]
+        return dict(zip(keys, list(out)))
+
+    def grid(self):
+        dims = (ctypes.c_int * 3)()
+        geo = (ctypes.c_double * 12)()
+        N.call("bbg_get_grid", self.h, dims, geo)
+        return np.array(list(dims), np.int32), np.array(list(geo))
+
+    def dump_grid(self):
+        dims, _ = self.grid()
+        total = int(np.prod(dims))
+        cell_of = np.zeros(self.n, np.uint32)
+        counts = np.zeros(total, np.uint32)
+        ids = np.zeros(self.n, np.uint32)
+        N.call("bbg_dump_grid", self.h, cell_of.ctypes.data_as(N._UP),
+               counts.ctypes.data_as(N._UP), ids.ctypes.data_as(N._UP))
+        return cell_of, counts, ids
+
+    def profiler_enable(self, on=True):
+        N.call("bbg_profiler_enable", self.h, int(bool(on)))
+
+    def profiler_report(self):
+        """{kernel: (total_ms, launches that did work)}, total kernel launches."""
+        m = 32
+        names = ctypes.create_string_buffer(32 * m)
+        ms = (ctypes.c_double * m)()
+        cnt = (ctypes.c_int * m)()
+        k = ctypes.c_int()
+        total = ctypes.c_int64()
+        N.call("bbg_profiler_report", self.h, m, names, ms, cnt, ctypes.byref(k), ctypes.byref(total))
+        out = {}
+        for i in range(k.value):
+            name = names.raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
+            out[name] = (ms[i], cnt[i])
+        return out, total.value
+
+    def neighbor_counts(self):
+        out = np.zeros(self.n, np.int32)
+        N.call("bbg_neighbor_counts", self.h, out.ctypes.data_as(N._IP))
+        return out
+
+
+class PciSphSolver3(Solver):
+    """Reference-named facade of PciSphSolver3 (src/core/pcisph_solver.h:56-83)."""
+
+    def Setup(self):
+        self.setup()
+
+    def SetColliders(self, colliders):
+        self.set_colliders(colliders)
+
+    def Advance(self, dt):
+        return self.advance(dt)
+
+    def GetParticleCount(self):
+        return self.n
+
+    def ComputeDelta(self, dt):
+        return self.compute_delta(dt)
+
+
+class SphSolver3(PciSphSolver3):
+    """Reference-named facade of SphSolver3 (src/core/sph_solver.h:76-96)."""
+
+
+def build_grid(domain_min, domain_max, spacing, scale):
+    """UtilBuildGridForDomain in the reference's FP32 arithmetic (host only)."""
+    a = (ctypes.c_double * 3)(*domain_min)
+    b = (ctypes.c_double * 3)(*domain_max)
+    dims = (ctypes.c_int * 3)()
+    geo = (ctypes.c_double * 12)()
+    N.call("bbg_build_grid", a, b, float(spacing), float(scale), dims, geo)
+    return np.array(list(dims), np.int32), np.array(list(geo))
+
+
+def compute_mass(lattice, density, spacing, kernel_radius):
+    m = ctypes.c_double()
+    N.call("bbg_compute_mass", int(lattice), float(density), float(spacing), float(kernel_radius),
+           ctypes.byref(m))
+    return m.value
+
+
+def compute_delta_denom(spacing, kernel_radius):
+    d = ctypes.c_double()
+    N.call("bbg_compute_delta_denom", float(spacing), float(kernel_radius), ctypes.byref(d))
+    return d.value

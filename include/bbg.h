@@ -1,0 +1,224 @@
+/*
+ * bbg.h -- C ABI of bubbles_gb300, the GB300-native (sm_103a) Bubbles 3D SPH /
+ * PCISPH particle step.
+ *
+ * The reference has no plugin or FFI layer; its seam is the free-function and class
+ * layer of src/core/sph_solver.h:76-196 and src/core/pcisph_solver.h:56-99, with the
+ * GPU/CPU choice made inside AdvanceTimeStep (src/solvers/pcisph_solver3.cpp:42-65,
+ * src/solvers/sph_solver3.cpp:48-67).  Every entry point below replaces one of those
+ * functions (cited beside it) with plain pointers, sizes and a status code.
+ *
+ * Conventions
+ *  - All functions return bbg_status; BBG_OK is 0.  bbg_last_error() gives a message.
+ *  - Host particle arrays are float xyz triples (n*3) in the caller's particle order
+ *    (the reference's vec3f with Float=float); scalar fields are n floats.
+ *  - "_device" variants take device pointers and never synchronise.
+ *  - Device state is FP32 structure-of-arrays, re-sorted by grid cell every substep;
+ *    the caller's particle order is kept through an id permutation.
+ *  - The library has no CPU fallback: without a CUDA device every compute call fails
+ *    with BBG_ERR_NO_DEVICE.
+ */
+#ifndef BBG_H
+#define BBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int bbg_status;
+#define BBG_OK 0
+#define BBG_ERR_INVALID_ARGUMENT 1
+#define BBG_ERR_CUDA 2
+#define BBG_ERR_OUT_OF_MEMORY 3
+#define BBG_ERR_CAPACITY 4
+#define BBG_ERR_STATE 5
+#define BBG_ERR_NO_DEVICE 6
+#define BBG_ERR_NOT_FOUND 7
+
+#define BBG_SOLVER_PCISPH 0
+#define BBG_SOLVER_SPH 1
+
+/* PCISPH corrector modes.  AS_SHIPPED reproduces the reference exactly: it never
+ * stores densityErrors (pcisph_equations3.cpp:17,82-89), so its convergence test
+ * always passes after one predict-correct pass.  TOLERANCE stores the per-particle
+ * density error the reference computes and iterates until
+ * max|err|/rho0 < max_density_error_ratio or max_iterations. */
+#define BBG_PCISPH_AS_SHIPPED 0
+#define BBG_PCISPH_TOLERANCE 1
+
+#define BBG_SHAPE_BOX 1
+#define BBG_SHAPE_SPHERE 2
+#define BBG_MAX_COLLIDERS 16
+
+/* Field ids for bbg_get_field / bbg_set_field (ParticleSet3 accessors,
+ * src/core/particle.h:154-401, and PciSphSolverData3, pcisph_solver.h:17-25). */
+#define BBG_FIELD_POSITION 0
+#define BBG_FIELD_VELOCITY 1
+#define BBG_FIELD_FORCE 2
+#define BBG_FIELD_INTERACTION 3
+#define BBG_FIELD_DENSITY 4
+#define BBG_FIELD_PRESSURE 5
+#define BBG_FIELD_PRED_POSITION 6
+#define BBG_FIELD_PRESSURE_FORCE 8
+#define BBG_FIELD_PRED_DENSITY 9
+#define BBG_FIELD_DENSITY_ERROR 10
+
+typedef struct bbg_solver_s *bbg_solver;
+
+/* Scene description: SphSolverData3 (sph_solver.h:31-50), SphParticleSet3
+ * (particle.h:508-609), the domain grid of UtilBuildGridForDomain (util.cpp:269-287)
+ * and the PciSphSolver3 corrector controls (pcisph_solver.h:56-83). */
+typedef struct {
+    int solver_kind;                 /* BBG_SOLVER_PCISPH / BBG_SOLVER_SPH */
+    double eos_exponent;             /* 7 */
+    double negative_pressure_scale;  /* 0 */
+    double viscosity;                /* 0.04 */
+    double pseudo_viscosity;         /* 10 */
+    double sound_speed;              /* 100 */
+    double drag_coefficient;         /* 1e-4 */
+    double gravity[3];               /* constant interaction; reference default (0,-9.8,0) */
+    double target_density;           /* 1000 */
+    double target_spacing;           /* particle spacing h0; also the particle radius */
+    double relative_kernel_radius;   /* 2: kernel radius = 2 h0 */
+    double mass;                     /* > 0 overrides the BCC-lattice mass of ComputeMass */
+    double domain_min[3];            /* domain bounds handed to UtilBuildGridForDomain */
+    double domain_max[3];
+    double grid_spacing_scale;       /* 2: cell length = spacing * scale */
+    double time_step_limit_scale;    /* Advance CFL scale: 5 (PCISPH), 1 (SPH) */
+    int pcisph_mode;                 /* BBG_PCISPH_AS_SHIPPED / BBG_PCISPH_TOLERANCE */
+    int max_iterations;              /* corrector cap (reference call site: 5) */
+    double max_density_error_ratio;  /* corrector tolerance (reference: 0.01) */
+    int device;                      /* CUDA device ordinal */
+} bbg_solver_desc;
+
+/* Analytic collider shape with a translation-only ObjectToWorld (MakeBox,
+ * src/shapes/box.cpp:6-10; MakeSphere, src/shapes/sphere.cpp:5-9). */
+typedef struct {
+    int type;            /* BBG_SHAPE_BOX / BBG_SHAPE_SPHERE */
+    int reverse;         /* reverseOrientation; 1 for a container box */
+    double center[3];
+    double size[3];      /* box edge lengths; size[0] is the sphere radius */
+    double friction;     /* Collider3::frictionCoefficient */
+} bbg_shape;
+
+typedef struct {
+    int substeps;                     /* substeps run by this call */
+    int iterations;                   /* corrector iterations summed over substeps */
+    int max_iterations_in_substep;
+    int not_converged;                /* substeps that hit max_iterations above tolerance */
+    double last_dt;                   /* last substep length */
+    double max_density_error_ratio;   /* last substep's final max|err|/rho0 */
+    double mean_density_error_ratio;  /* last substep's final mean|err|/rho0 (FP64 sum) */
+    int neighbor_overflow;            /* particles with > 100 neighbours (reference bucket cap) */
+    int out_of_grid;                  /* particles hashed outside the grid (clamped) */
+    double max_force;                 /* max |F| after the last substep (CFL input) */
+} bbg_step_stats;
+
+/* ----- library ----------------------------------------------------------- */
+const char *bbg_version(void);
+const char *bbg_status_string(bbg_status s);
+const char *bbg_last_error(void);
+/* Number of CUDA devices visible (0 without a GPU). */
+bbg_status bbg_device_count(int *count);
+
+/* ----- host-side setup math (no GPU needed) ------------------------------- */
+/* DefaultSphSolverData3 (sph_solver3.cpp:124-151) + PciSphSolver3::Initialize
+ * (pcisph_solver3.cpp:9-14). */
+bbg_status bbg_solver_desc_default(bbg_solver_desc *desc, int solver_kind);
+/* UtilBuildGridForDomain + Grid::Build (util.cpp:269-287, grid.h:627-666) in the
+ * reference's FP32 arithmetic.  geo = minPoint[3], cellsLen[3], bounds.pMin[3],
+ * bounds.pMax[3]. */
+bbg_status bbg_build_grid(const double domain_min[3], const double domain_max[3],
+                          double spacing, double spacing_scale, int dims[3], double geo[12]);
+/* SphParticleSet3::ComputeMass (particle.h:557-582): lattice 0 = BCC (the reference),
+ * 1 = simple cubic at the same spacing. */
+bbg_status bbg_compute_mass(int lattice, double target_density, double spacing,
+                            double kernel_radius, double *mass);
+/* PciSphSolver3::ComputeDeltaDenom (pcisph_solver3.cpp:148-180). */
+bbg_status bbg_compute_delta_denom(double spacing, double kernel_radius, double *denom);
+
+/* ----- solver lifetime (PciSphSolver3 / SphSolver3) ------------------------ */
+/* Initialize: allocates device state for up to `capacity` particles. */
+bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out);
+bbg_status bbg_destroy(bbg_solver s);
+/* SetColliders (pcisph_solver3.cpp:27-31). */
+bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count);
+/* ParticleSetBuilder3::MakeParticleSet (particle.h:685-709): host xyz arrays. */
+bbg_status bbg_upload_particles(bbg_solver s, const float *pos, const float *vel, int n);
+bbg_status bbg_upload_particles_device(bbg_solver s, const float *d_pos, const float *d_vel,
+                                       int n);
+/* Setup (pcisph_solver3.cpp:103-146): mass, delta denominator, first distribution. */
+bbg_status bbg_setup(bbg_solver s);
+/* Use the caller's cudaStream_t (NULL = the solver's own stream). */
+bbg_status bbg_set_stream(bbg_solver s, void *cuda_stream);
+bbg_status bbg_synchronize(bbg_solver s);
+
+/* ----- stepping ----------------------------------------------------------- */
+/* Advance(dt) with the CFL substep loop (pcisph_solver3.cpp:67-89,
+ * sph_solver3.cpp:69-93). */
+bbg_status bbg_advance(bbg_solver s, double dt, bbg_step_stats *stats);
+/* AdvanceTimeStep: one substep of length dt (pcisph_solver3.cpp:42-65,
+ * sph_solver3.cpp:48-67).  Asynchronous when stats is NULL. */
+bbg_status bbg_advance_time_step(bbg_solver s, double dt, bbg_step_stats *stats);
+/* Read the statistics of the last substep (synchronises). */
+bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
+
+/* ----- individual passes (sph_solver.h:124-196, pcisph_solver.h:85-99) ------- */
+bbg_status bbg_update_grid_distribution(bbg_solver s);          /* UpdateGridDistributionGPU */
+bbg_status bbg_compute_particle_interaction(bbg_solver s);      /* ComputeParticleInteractionGPU */
+bbg_status bbg_compute_density(bbg_solver s, int compute_pressure); /* ComputeDensityGPU */
+bbg_status bbg_compute_non_pressure_force(bbg_solver s);        /* ComputeNonPressureForceGPU */
+bbg_status bbg_compute_pressure_force(bbg_solver s, double dt); /* ComputePressureForceGPU (SPH,
+                                                                   Jacobi order) */
+bbg_status bbg_time_integration(bbg_solver s, double dt);       /* TimeIntegrationGPU */
+bbg_status bbg_compute_pseudo_viscosity_interpolation(bbg_solver s, double dt);
+/* ComputePressureForceAndIntegrate (pcisph_equations3.cpp:218-256). */
+bbg_status bbg_compute_pressure_force_and_integrate(bbg_solver s, double dt,
+                                                    double max_density_error_ratio,
+                                                    double delta, int max_iterations,
+                                                    bbg_step_stats *stats);
+bbg_status bbg_compute_delta(bbg_solver s, double dt, double *delta);  /* ComputeDelta */
+/* SphParticleSet3::ComputeNumberOfTimeSteps (particle.h:584-608). */
+bbg_status bbg_compute_number_of_time_steps(bbg_solver s, double remaining, double scale,
+                                            unsigned *count);
+
+/* ----- state access ------------------------------------------------------- */
+bbg_status bbg_particle_count(bbg_solver s, int *n);
+/* Host arrays in the caller's order.  Fields other than position and velocity are
+ * permuted by every grid update; reading one that has not been recomputed since
+ * returns BBG_ERR_STATE. */
+bbg_status bbg_get_field(bbg_solver s, int field, float *out);
+bbg_status bbg_set_field(bbg_solver s, int field, const float *in);
+/* Position and velocity, host (synchronising) or device (asynchronous). */
+bbg_status bbg_download(bbg_solver s, float *pos, float *vel);
+bbg_status bbg_download_device(bbg_solver s, float *d_pos, float *d_vel);
+/* Solver scalars: mass, kernel radius, delta denominator, (m/rho0)^2, spacing,
+ * target density, particle radius, relative kernel radius. */
+bbg_status bbg_get_scalars(bbg_solver s, double out[8]);
+bbg_status bbg_get_grid(bbg_solver s, int dims[3], double geo[12]);
+/* Grid state after the last update: cell id of each particle (caller order),
+ * particle count per cell, and particle ids in cell-sorted order (stable by id). */
+bbg_status bbg_dump_grid(bbg_solver s, uint32_t *cell_of_particle, uint32_t *cell_counts,
+                         uint32_t *sorted_ids);
+/* Neighbour count of each particle (caller order) at the last grid update. */
+bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts);
+
+/* ----- profiling (ProfilerPrepare / ProfilerFinish around every GPULaunch,
+ *       src/cuda/cutil.h:237-244; ProfilerReport, src/core/profiler.cpp:175-247) ---- */
+/* Record CUDA events around every kernel launch on the solver's stream. */
+bbg_status bbg_profiler_enable(bbg_solver s, int enable);
+/* Drain the records (synchronises): per kernel its name (32 chars each), total device
+ * milliseconds and launch count over launches that did work, plus the number of
+ * kernel launches of every kind, including corrector launches that returned at once
+ * because an earlier iteration had converged. */
+bbg_status bbg_profiler_report(bbg_solver s, int max_kernels, char *names, double *total_ms,
+                               int32_t *launches, int32_t *kernel_count,
+                               int64_t *total_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BBG_H */

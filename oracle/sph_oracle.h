@@ -1,0 +1,157 @@
+/*
+ * sph_oracle.h -- CPU oracle for the Bubbles 3D SPH / PCISPH particle step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA path is compared
+ * against; nothing in the product links it.  Only tests/, __graft_entry__.smoke()
+ * and bench.py (its cpu_baseline leg and its --impl reference arm) may load it.
+ *
+ * It restates, in plain C, the reference's CPU implementation of the step:
+ *   - grid build and hashing        src/core/grid.h:259-298, 603-666; src/core/util.cpp:269-287
+ *   - double-buffered cell chains   src/core/grid.h:20-156, 391-500
+ *   - per-particle buckets (<=100)  src/core/grid.h:423-447; src/core/particle.h:22-60
+ *   - SPH kernels                   src/core/kernel.cpp:113-233
+ *   - density / EOS / forces        src/equations/sph_equations3.cpp:7-339
+ *   - PCISPH predict-correct        src/equations/pcisph_equations3.cpp:3-256
+ *   - colliders (box, sphere)       src/core/collider.cpp:4-45,238-264; src/shapes/box.cpp:74-172;
+ *                                   src/shapes/sphere.cpp:47-70; src/core/shape.cpp:206-288
+ *   - setup math                    src/core/particle.h:557-608; src/solvers/pcisph_solver3.cpp:103-189
+ * The chain order, bucket order and every mixed float/double promotion of the
+ * reference are kept, so that the FP32 build (-DORC_FLOAT=float) reproduces the
+ * reference compiled with `typedef float Float` and the FP64 build reproduces the
+ * reference as shipped (`typedef double Float`, src/core/geometry.h:68-69).
+ *
+ * Parity of this restatement is pinned against the reference itself, built
+ * host-only by oracle/ref/Makefile, and against the golden fixtures under
+ * tests/golden/ that were generated from that build.
+ *
+ * All arrays crossing this interface are double precision, xyz interleaved; they
+ * are rounded to the oracle's Float on the way in.
+ */
+#ifndef BUBBLES_SPH_ORACLE_H
+#define BUBBLES_SPH_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_COLLIDERS 16
+#define ORC_SHAPE_BOX 1
+#define ORC_SHAPE_SPHERE 2
+
+typedef struct {
+    int type;            /* ORC_SHAPE_BOX / ORC_SHAPE_SPHERE */
+    int reverse;         /* reverseOrientation (container boxes use 1) */
+    double center[3];    /* translation of ObjectToWorld */
+    double size[3];      /* box edge lengths; size[0] = sphere radius */
+    double friction;     /* Collider3::frictionCoefficient */
+} orc_shape;
+
+typedef struct {
+    /* SphSolverData3 (src/core/sph_solver.h:31-50; defaults sph_solver3.cpp:124-151) */
+    double eos_exponent;
+    double negative_pressure_scale;
+    double viscosity;
+    double pseudo_viscosity;
+    double sound_speed;
+    double drag_coefficient;
+    double gravity[3];
+    /* SphParticleSet3 */
+    double target_density;
+    double target_spacing;
+    double relative_kernel_radius;
+    double mass;                 /* > 0: ParticleSet::SetMass override after Setup */
+    /* Grid: UtilBuildGridForDomain(domain, spacing, spacing_scale) */
+    double domain_min[3];
+    double domain_max[3];
+    double grid_spacing_scale;
+    /* colliders */
+    int n_colliders;
+    orc_shape colliders[ORC_MAX_COLLIDERS];
+    /* Advance */
+    double time_step_limit_scale;   /* kDefaultTimeStepLimitScale (5) for PCISPH, 1 for SPH */
+} orc_params;
+
+typedef struct orc_sim orc_sim;
+
+/* field ids for orc_get_field / orc_set_field */
+enum {
+    ORC_POSITION = 0, ORC_VELOCITY = 1, ORC_FORCE = 2, ORC_INTERACTION = 3,
+    ORC_DENSITY = 4, ORC_PRESSURE = 5, ORC_PRED_POSITION = 6, ORC_PRED_VELOCITY = 7,
+    ORC_PRESSURE_FORCE = 8, ORC_PRED_DENSITY = 9, ORC_DENSITY_ERROR = 10,
+    ORC_SMOOTHED_VELOCITY = 11
+};
+
+/* PCISPH corrector modes */
+enum { ORC_PCISPH_AS_SHIPPED = 0, ORC_PCISPH_TOLERANCE = 1 };
+
+int      orc_float_bytes(void);
+void     orc_set_threads(int n);
+int      orc_get_threads(void);
+
+orc_sim *orc_create(const orc_params *p, int n, const double *pos, const double *vel);
+void     orc_destroy(orc_sim *s);
+
+/* Scalars after Setup: mass, kernel radius, delta denominator, (m/rho0)^2. */
+void     orc_scalars(const orc_sim *s, double out[8]);
+/* Grid: dims[3]; minp[3], len[3], bmin[3], bmax[3] packed into geo[12]. */
+void     orc_grid_info(const orc_sim *s, int dims[3], double geo[12]);
+/* Reference neighbour list of a cell (27 max), returns the count. */
+int      orc_cell_neighbors(const orc_sim *s, int cell, int out[27]);
+/* Hash arbitrary points with the grid rule (GetLinearHashedPosition). */
+void     orc_hash_points(const orc_sim *s, int n, const double *pts, uint32_t *cell_ids,
+                         uint32_t *ucoords);
+
+/* Stand-alone setup math (no simulation needed). */
+double   orc_compute_mass_bcc(double target_density, double spacing, double kernel_radius);
+double   orc_compute_delta_denom(double spacing, double kernel_radius);
+int      orc_build_grid(const double dmin[3], const double dmax[3], double spacing,
+                        double scale, int dims[3], double geo[12]);
+double   orc_kernel_eval(int which, double h, double r);
+
+/* Passes (each the reference CPU wrapper of the same name). */
+void     orc_update_grid_distribution(orc_sim *s);
+void     orc_compute_particle_interaction(orc_sim *s);
+void     orc_compute_density(orc_sim *s, int compute_pressure);
+void     orc_compute_non_pressure_force(orc_sim *s);
+double   orc_compute_delta(const orc_sim *s, double dt);
+/* Returns iterations run; *final_err = last max density-error ratio. */
+int      orc_pressure_force_and_integrate(orc_sim *s, double dt, double max_err_ratio,
+                                          double delta, int max_it, int mode,
+                                          double *final_err);
+void     orc_time_integration(orc_sim *s, double dt);
+/* SPH all-forces pass. inplace=1: the reference as shipped (integrates each particle
+ * inside the force loop, sph_equations3.cpp:277); inplace=0: Jacobi order. */
+void     orc_sph_all_forces(orc_sim *s, double dt, int inplace);
+void     orc_pseudo_viscosity(orc_sim *s, double dt);
+unsigned orc_number_of_time_steps(const orc_sim *s, double remaining, double scale);
+/* One AdvanceTimeStep (PCISPH); returns corrector iterations. */
+int      orc_pcisph_substep(orc_sim *s, double dt, double max_err_ratio, int max_it, int mode,
+                            double *final_err);
+/* One AdvanceTimeStep (SPH). */
+void     orc_sph_substep(orc_sim *s, double dt, int inplace);
+/* Advance(dt) with the CFL substep loop; returns substeps taken. */
+int      orc_advance_pcisph(orc_sim *s, double dt, double max_err_ratio, int max_it, int mode,
+                            int *total_iters);
+int      orc_advance_sph(orc_sim *s, double dt, int inplace);
+
+/* Field access (n*3 for vectors, n for scalars). */
+void     orc_get_field(const orc_sim *s, int field, double *out);
+void     orc_set_field(orc_sim *s, int field, const double *in);
+int      orc_count(const orc_sim *s);
+int      orc_higher_level(const orc_sim *s);
+void     orc_set_higher_level(orc_sim *s, int v);
+
+/* Grid state: cell of each particle; per-cell chain length; chains concatenated in
+ * cell order (n ids).  Returns the number of cells. */
+int      orc_get_cells(const orc_sim *s, uint32_t *cell_of_particle, uint32_t *cell_counts,
+                       uint32_t *chain_concat);
+/* Buckets: counts[n], ids[n*100] (-1 padded).  Returns the number of particles whose
+ * neighbour count exceeded the 100-slot bucket (truncated, as the reference does). */
+int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
