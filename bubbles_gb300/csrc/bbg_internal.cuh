@@ -190,6 +190,55 @@ __device__ __forceinline__ void for_each_candidate(const GridDev &g, const unsig
     }
 }
 
+// Neighbour sets recorded by the density pass: for each of the 9 candidate ranges
+// (r = 3 * (dz + 1) + (dy + 1)) a 32-bit mask of the member slots, stored range-major
+// (masks[r * n + i]).  A particle whose range is longer than 32 slots has kWide set in
+// its cell word and is re-tested exactly on every pass instead.
+constexpr unsigned kWide = 0x80000000u;
+constexpr int kRows = 9;
+
+template <class F>
+__device__ __forceinline__ void for_each_neighbor(const Params &P, const unsigned *__restrict__ start,
+                                                  const unsigned *__restrict__ masks,
+                                                  const float4 *__restrict__ pos, unsigned cellw,
+                                                  int i, F &&f) {
+    const GridDev &g = P.g;
+    const unsigned c = cellw & ~kWide;
+    if (cellw & kWide) {
+        const float4 pi = pos[i];
+        for_each_candidate(g, start, c, [&](unsigned j) {
+            const float4 pj = __ldg(&pos[j]);
+            if (std_member(P, pi, pj, dist2(pi, pj))) f(j);
+        });
+        return;
+    }
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
+    const int cz = (int)(c / plane);
+    const unsigned rem = c - (unsigned)cz * plane;
+    const int cy = (int)(rem / (unsigned)nx);
+    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
+    const int x0 = cx > 0 ? cx - 1 : 0;
+    const unsigned n = (unsigned)P.n;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int z = cz + dz, y = cy + dy;
+            if (z < 0 || z >= nz || y < 0 || y >= ny) continue;
+            const int r = 3 * (dz + 1) + (dy + 1);
+            unsigned m = __ldg(&masks[(unsigned)r * n + (unsigned)i]);
+            if (!m) continue;
+            const unsigned b = __ldg(&start[(unsigned)y * (unsigned)nx + (unsigned)z * plane + (unsigned)x0]);
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                m &= m - 1u;
+                f(b + (unsigned)bit);
+            }
+        }
+    }
+}
+
 // ----------------------------------------------------------------------------
 // colliders: exact FP32 restatement of CollisionHandle / ColliderSet3::ResolveCollision
 // (src/core/collider.cpp:3-44, 238-264), Shape::BoxClosestPoint / BoxClosestDistance

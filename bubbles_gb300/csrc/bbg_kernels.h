@@ -21,6 +21,9 @@ struct DevBufs {
     unsigned *partials;        // scan partials
     uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
     int *nbr;                  // neighbour count of each sorted slot
+    unsigned *masks;           // 9 neighbour masks per slot (range-major)
+    float *inv_rho;            // 1 / density
+    float *acoef;              // pressure / density^2 (predicted density in PCISPH)
     StepState *st;
     float *stage;              // n * 3 floats of staging for host copies
     unsigned *red;             // reduction scratch (max |F|)

@@ -35,33 +35,69 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
     return false;
 }
 
-// ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58
+// ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
+// Tests every candidate of the 27 cells exactly once per substep and records the
+// neighbour set (the reference bucket, grid.h:423-447) as 9 range masks.
 __global__ void __launch_bounds__(kThreads)
-k_density(Params P, const float4 *__restrict__ pos, const unsigned *__restrict__ cell,
-          const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ press,
-          int *__restrict__ nbr, int compute_pressure, StepState *st) {
+k_density(Params P, const float4 *__restrict__ pos, unsigned *__restrict__ cell,
+          const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
+          float *__restrict__ press, float *__restrict__ acoef, int *__restrict__ nbr,
+          unsigned *__restrict__ masks, int compute_pressure, StepState *st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
+    const unsigned cw = cell[i];
+    const unsigned c = cw & ~kWide;
+    const GridDev &g = P.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
+    const int cz = (int)(c / plane);
+    const unsigned rem = c - (unsigned)cz * plane;
+    const int cy = (int)(rem / (unsigned)nx);
+    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
+    const int x0 = cx > 0 ? cx - 1 : 0;
+    const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+    const unsigned n = (unsigned)P.n;
     float sum = 0.f;
     int cnt = 0;
-    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
-        const float4 pj = __ldg(&pos[j]);
-        const float r2 = dist2(pi, pj);
-        if (std_member(P, pi, pj, r2)) {
-            const float x = 1.f - r2 * P.inv_h2;
-            sum += x * x * x;
-            cnt++;
+    bool wide = false;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int z = cz + dz, y = cy + dy;
+            const int r = 3 * (dz + 1) + (dy + 1);
+            unsigned m = 0;
+            if (z >= 0 && z < nz && y >= 0 && y < ny) {
+                const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
+                const unsigned b = __ldg(&start[row + (unsigned)x0]);
+                const unsigned e = __ldg(&start[row + (unsigned)x1 + 1u]);
+                if (e - b > 32u) wide = true;
+                for (unsigned j = b; j < e; ++j) {
+                    const float4 pj = __ldg(&pos[j]);
+                    const float r2 = dist2(pi, pj);
+                    if (std_member(P, pi, pj, r2)) {
+                        const float x = 1.f - r2 * P.inv_h2;
+                        sum += x * x * x;
+                        cnt++;
+                        if (j - b < 32u) m |= 1u << (j - b);
+                    }
+                }
+            }
+            masks[(unsigned)r * n + (unsigned)i] = m;
         }
-    });
+    }
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
         if (p < 0.f) p *= P.neg_scale;
         press[i] = p;
+        acoef[i] = p / (di * di);
     }
     rho[i] = di;
+    inv_rho[i] = 1.f / di;
     nbr[i] = cnt;
+    if (wide) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
@@ -69,10 +105,10 @@ k_density(Params P, const float4 *__restrict__ pos, const unsigned *__restrict__
 // k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).
 __global__ void __launch_bounds__(kThreads)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-               const float *__restrict__ rho, const unsigned *__restrict__ cell,
-               const unsigned *__restrict__ start, float4 *__restrict__ force,
-               float4 *__restrict__ xstar, float4 *__restrict__ pforce, float *__restrict__ press,
-               int predict, float dt, float dt_over_m) {
+               const float *__restrict__ inv_rho, const unsigned *__restrict__ cell,
+               const unsigned *__restrict__ start, const unsigned *__restrict__ masks,
+               float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
+               float *__restrict__ press, int predict, float dt, float dt_over_m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
@@ -81,17 +117,16 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     float fy = P.mass * P.gy - P.drag * vi.y;
     float fz = P.mass * P.gz - P.drag * vi.z;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
-    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+    for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
+        if (j == (unsigned)i) return;   // (v_i - v_i) contributes nothing
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
-        if (std_member(P, pi, pj, r2)) {
-            const float d = sqrtf(r2);
-            const float w = kv * (1.f - d * P.inv_h) / __ldg(&rho[j]);
-            const float4 vj = __ldg(&vel[j]);
-            fx += (vj.x - vi.x) * w;
-            fy += (vj.y - vi.y) * w;
-            fz += (vj.z - vi.z) * w;
-        }
+        const float d = r2 * rsqrtf(r2);
+        const float w = kv * (1.f - d * P.inv_h) * __ldg(&inv_rho[j]);
+        const float4 vj = __ldg(&vel[j]);
+        fx += (vj.x - vi.x) * w;
+        fy += (vj.y - vi.y) * w;
+        fz += (vj.z - vi.z) * w;
     });
     force[i] = make_float4(fx, fy, fz, 0.f);
     if (predict) {
@@ -118,29 +153,27 @@ k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restri
     xstar[i] = F4(xs);
 }
 
-// PredictPressureFor (pcisph_equations3.cpp:60-90) with the density error stored
-// (tolerance mode) and reduced to max |err| and sum |err| for iteration k.
+// PredictPressureFor (pcisph_equations3.cpp:60-90) over the step-start neighbour set at
+// predicted positions, with the density error stored (tolerance mode) and reduced to
+// max |err| and sum |err| for iteration k; also p / rho*^2 for the pressure force.
 __global__ void __launch_bounds__(kThreads)
 k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               float *__restrict__ press, float *__restrict__ rhostar, float *__restrict__ derr,
+               const unsigned *__restrict__ masks, float *__restrict__ press,
+               float *__restrict__ rhostar, float *__restrict__ derr, float *__restrict__ acoef,
                StepState *st, int k, float delta) {
     if (converged_before(P, st, k)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float aerr = 0.f;
     if (i < P.n) {
-        const float4 pi = pos[i];
         const float4 xi = xstar[i];
         float sum = 0.f;
-        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
-            const float4 pj = __ldg(&pos[j]);
-            if (std_member(P, pi, pj, dist2(pi, pj))) {
-                const float4 xj = __ldg(&xstar[j]);
-                const float r2 = dist2(xi, xj);
-                if (r2 < P.h2mz) {
-                    const float x = 1.f - r2 * P.inv_h2;
-                    sum += x * x * x;
-                }
+        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
+            const float4 xj = __ldg(&xstar[j]);
+            const float r2 = dist2(xi, xj);
+            if (r2 < P.h2mz) {
+                const float x = 1.f - r2 * P.inv_h2;
+                sum += x * x * x;
             }
         });
         const float density = sum * P.std_c * P.mass;
@@ -150,9 +183,11 @@ k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restric
             pr *= P.neg_scale;
             err *= P.neg_scale;
         }
-        press[i] += pr;
+        const float p = press[i] + pr;
+        press[i] = p;
         rhostar[i] = density;
         derr[i] = err;
+        acoef[i] = p / (density * density);
         aerr = fabsf(err);
     }
     // block reduction: max |err| (exact as bits of non-negative floats), sum |err| in FP64
@@ -177,7 +212,7 @@ k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restric
 __global__ void __launch_bounds__(kThreads)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const float *__restrict__ press, const float *__restrict__ rhostar,
+                 const unsigned *__restrict__ masks, const float *__restrict__ acoef,
                  float4 *__restrict__ force, float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
@@ -189,22 +224,19 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
-        const float di = rhostar[i];
-        const float ai = press[i] / (di * di);
+        const float ai = acoef[i];
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
-        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
             if (j == (unsigned)i) return;
             const float4 pj = __ldg(&pos[j]);
             const float r2 = dist2(pi, pj);
-            if (!std_member(P, pi, pj, r2)) return;
-            const float d = sqrtf(r2);
+            const float inv_d = rsqrtf(r2);
+            const float d = r2 * inv_d;
             // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
             if (d - P.h <= -P.iz && d >= P.iz) {
-                const float dj = __ldg(&rhostar[j]);
-                const float aj = __ldg(&press[j]) / (dj * dj);
                 const float x = 1.f - d * P.inv_h;
-                const float c = kg * (ai + aj) * x * x / d;
+                const float c = kg * (ai + __ldg(&acoef[j])) * x * x * inv_d;
                 tx += (pj.x - pi.x) * c;
                 ty += (pj.y - pi.y) * c;
                 tz += (pj.z - pi.z) * c;
@@ -212,8 +244,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
         });
         const v3 fp = V(-tx, -ty, -tz);
         pforce[i] = F4(fp);
-        const float4 f4 = force[i];
-        const v3 f = V(f4);
+        const v3 f = V(force[i]);
         if (last) {
             const v3 ft = vadd(f, fp);
             force[i] = F4(ft);
@@ -240,41 +271,38 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
 // state goes to the other buffer.
 __global__ void __launch_bounds__(kThreads)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-             const float *__restrict__ rho, const float *__restrict__ press,
+             const float *__restrict__ inv_rho, const float *__restrict__ acoef,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-             float4 *__restrict__ force, float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
-             StepState *st, float dt) {
+             const unsigned *__restrict__ masks, float4 *__restrict__ force,
+             float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
         const float4 vi = vel[i];
-        const float di = rho[i];
-        const float ai = press[i] / (di * di);
+        const float ai = acoef[i];
         float fx = P.mass * P.gx - P.drag * vi.x;
         float fy = P.mass * P.gy - P.drag * vi.y;
         float fz = P.mass * P.gz - P.drag * vi.z;
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
         const float kv = P.visc_m2 * P.spiky_d2w_c;
-        for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
+        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
             if (j == (unsigned)i) return;
             const float4 pj = __ldg(&pos[j]);
             const float r2 = dist2(pi, pj);
-            if (!std_member(P, pi, pj, r2)) return;
-            const float d = sqrtf(r2);
+            const float inv_d = rsqrtf(r2);
+            const float d = r2 * inv_d;
             if (d - P.h <= -P.iz) {
-                const float dj = __ldg(&rho[j]);
                 const float x = 1.f - d * P.inv_h;
                 if (d >= P.iz) {
-                    const float aj = __ldg(&press[j]) / (dj * dj);
-                    const float c = kg * (ai + aj) * x * x / d;
+                    const float c = kg * (ai + __ldg(&acoef[j])) * x * x * inv_d;
                     tx += (pj.x - pi.x) * c;
                     ty += (pj.y - pi.y) * c;
                     tz += (pj.z - pi.z) * c;
                 }
                 const float4 vj = __ldg(&vel[j]);
-                const float w = kv * x / dj;
+                const float w = kv * x * __ldg(&inv_rho[j]);
                 fx += (vj.x - vi.x) * w;
                 fy += (vj.y - vi.y) * w;
                 fz += (vj.z - vi.z) * w;
@@ -309,22 +337,19 @@ k_integrate(Params P, const float4 *__restrict__ pos, const float4 *__restrict__
 // from the step-start positions (the bucket), values at the integrated state.
 __global__ void __launch_bounds__(kThreads)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
-               const float4 *__restrict__ vel, const float *__restrict__ rho,
+               const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               float4 *__restrict__ smoothed) {
+               const unsigned *__restrict__ masks, float4 *__restrict__ smoothed) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const float4 oi = pos_old[i];
     const float4 pi = pos[i];
     float sx = 0.f, sy = 0.f, sz = 0.f, ws = 0.f;
-    for_each_candidate(P.g, start, cell[i], [&](unsigned j) {
-        const float4 oj = __ldg(&pos_old[j]);
-        if (!std_member(P, oi, oj, dist2(oi, oj))) return;
+    for_each_neighbor(P, start, masks, pos_old, cell[i], i, [&](unsigned j) {
         const float4 pj = __ldg(&pos[j]);
         const float d = sqrtf(dist2(pi, pj));
         if (d - P.h <= -P.iz) {
             const float x = 1.f - d * P.inv_h;
-            const float wj = P.mass / __ldg(&rho[j]) * (P.spiky_w_c * x * x * x);
+            const float wj = P.mass * __ldg(&inv_rho[j]) * (P.spiky_w_c * x * x * x);
             const float4 vj = __ldg(&vel[j]);
             ws += wj;
             sx += wj * vj.x;
@@ -352,7 +377,8 @@ __global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
     k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.cell, B.start, B.rho,
-                                                             B.press, B.nbr, compute_pressure, B.st);
+                                                             B.inv_rho, B.press, B.acoef, B.nbr,
+                                                             B.masks, compute_pressure, B.st);
     BBG_PEND(B, s);
 }
 
@@ -360,8 +386,8 @@ void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict
                          float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
     k_non_pressure<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.rho, B.cell, B.start, B.force, B.xstar, B.pforce, B.press,
-        predict, dt, dt_over_m);
+        P, B.pos[buf], B.vel[buf], B.inv_rho, B.cell, B.start, B.masks, B.force, B.xstar, B.pforce,
+        B.press, predict, dt, dt_over_m);
     BBG_PEND(B, s);
 }
 
@@ -377,7 +403,8 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
                          cudaStream_t s) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
     k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.xstar, B.cell, B.start, B.press, B.rhostar, B.derr, B.st, k, delta);
+        P, B.pos[buf], B.xstar, B.cell, B.start, B.masks, B.press, B.rhostar, B.derr, B.acoef, B.st,
+        k, delta);
     BBG_PEND(B, s);
 }
 
@@ -385,7 +412,7 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
                            float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.press, B.rhostar, B.force, B.pforce, B.xstar,
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.acoef, B.force, B.pforce, B.xstar,
         B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m);
     BBG_PEND(B, s);
 }
@@ -393,8 +420,8 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
     BBG_PBEGIN(B, KID_SPH_FORCES, s, -1);
     k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.rho, B.press, B.cell, B.start, B.force, B.pos[1 - buf],
-        B.vel[1 - buf], B.st, dt);
+        P, B.pos[buf], B.vel[buf], B.inv_rho, B.acoef, B.cell, B.start, B.masks, B.force,
+        B.pos[1 - buf], B.vel[1 - buf], B.st, dt);
     BBG_PEND(B, s);
 }
 
@@ -409,7 +436,8 @@ void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, flo
                              cudaStream_t s) {
     BBG_PBEGIN(B, KID_PSEUDO_VISCOSITY, s, -1);
     k_pv_aggregate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.rho, B.cell, B.start, B.smoothed);
+        P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.inv_rho, B.cell, B.start, B.masks,
+        B.smoothed);
     k_pv_interpolate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.vel[new_buf], B.smoothed,
                                                                     factor);
     BBG_PEND(B, s);

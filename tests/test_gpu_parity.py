@@ -26,6 +26,24 @@ def pair(sc, pos, vel=None, variant="f32"):
     return g, o
 
 
+def pressure_force_scale(o, x, mass, h):
+    """S_i = sum_j |m^2 (p_i / rho_i^2 + p_j / rho_j^2) grad W_spiky(x_i - x_j)| over the
+    oracle's bucket of i: the magnitude of the summands of the (cancelling) pressure force."""
+    counts, ids, _ = o.buckets()
+    p = o.get(O.PRESSURE)
+    r = o.get(O.PRED_DENSITY)
+    a = np.abs(p) / (r * r)
+    kg = 45.0 / (np.pi * h ** 4)
+    s = np.zeros(len(x))
+    for i in range(len(x)):
+        js = ids[i, :counts[i]]
+        js = js[js != i]
+        d = np.linalg.norm(x[js] - x[i], axis=1)
+        g = kg * np.clip(1.0 - d / h, 0.0, None) ** 2
+        s[i] = np.sum(mass * mass * (a[i] + a[js]) * g)
+    return s
+
+
 def rel_close(a, b, rtol=RTOL):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
@@ -176,16 +194,22 @@ def test_corrector_fixed_iterations(gpu, moved):
     o.set(O.FORCE, g.get(bb.FIELD_FORCE))
     delta = g.compute_delta(dt)
     assert delta == o.compute_delta(dt)
+    x0 = o.get(O.POSITION)
+    f_np = o.get(O.FORCE)
     # tolerance 0 never converges: exactly 3 predict-correct passes on both sides
     g.compute_pressure_force_and_integrate(dt, 0.0, delta, 3)
     o.pressure_force_and_integrate(dt, 0.0, delta, 3, O.PCISPH_TOLERANCE)
-    for fg, fo in ((bb.FIELD_PRED_DENSITY, O.PRED_DENSITY), (bb.FIELD_PRESSURE_FORCE, O.PRESSURE_FORCE)):
-        ok, worst = rel_close(g.get(fg), o.get(fo))
-        assert ok, (fg, worst)
+    ok, worst = rel_close(g.get(bb.FIELD_PRED_DENSITY), o.get(O.PRED_DENSITY))
+    assert ok, worst
     pg_, po_ = g.get(bb.FIELD_PRESSURE), o.get(O.PRESSURE)
     assert np.max(np.abs(pg_ - po_)) <= RTOL * max(1.0, np.abs(po_).max())
-    ok, worst = rel_close(g.get(bb.FIELD_FORCE), o.get(O.FORCE))
-    assert ok, worst
+    # pressure force: a cancelling sum, bounded relative to the sum of its |summands|
+    scale = pressure_force_scale(o, x0, g.scalars()["mass"], g.scalars()["kernel_radius"])
+    dfp = np.linalg.norm(g.get(bb.FIELD_PRESSURE_FORCE) - o.get(O.PRESSURE_FORCE), axis=1)
+    worst = float(np.max(dfp / (scale + 1e-30)))
+    assert worst <= RTOL, worst
+    df = np.linalg.norm(g.get(bb.FIELD_FORCE) - o.get(O.FORCE), axis=1)
+    assert np.all(df <= RTOL * (scale + np.linalg.norm(f_np, axis=1)))
     pg, vg = g.download()
     assert np.max(np.abs(pg - o.get(O.POSITION))) <= RTOL * sc["spacing"]
     assert np.max(np.abs(vg - o.get(O.VELOCITY))) <= RTOL * max(1.0, np.abs(vg).max())
