@@ -121,6 +121,7 @@ SIGNATURES = {
     "bbg_dump_grid": [_P, _UP, _UP, _UP],
     "bbg_neighbor_counts": [_P, _IP],
     "bbg_profiler_enable": [_P, _I],
+    "bbg_use_cuda_graphs": [_P, _I],
     "bbg_profiler_report": [_P, _I, ctypes.c_char_p, _DP, _IP, _IP,
                             ctypes.POINTER(ctypes.c_int64)],
 }

@@ -63,6 +63,18 @@ struct bbg_solver_s {
     int pcisph_last_substep = 0;
     bbg_step_stats acc;          // accumulated over the current advance call
     Prof prof;
+    // CUDA graphs of whole substeps, keyed by dt, corrector controls and ping-pong parity
+    struct SubstepGraph {
+        bool valid = false;
+        unsigned epoch = 0, dt_bits = 0, tol_bits = 0;
+        int state = -1, pid = -1, max_it = 0;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } graphs[4];
+    int graph_next = 0;
+    unsigned epoch = 1;          // bumped whenever captured launch arguments may change
+    bool use_graphs = true;
+    cudaStream_t aux = nullptr;  // capture stream of the corrector loop body
 };
 
 namespace {
@@ -122,12 +134,21 @@ bbg_status dalloc(T **p, size_t count) {
     return BBG_OK;
 }
 
+void drop_graphs(bbg_solver s) {
+    for (auto &g : s->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+        g = bbg_solver_s::SubstepGraph();
+    }
+}
+
 bbg_status free_all(bbg_solver s) {
+    drop_graphs(s);
     DevBufs &B = s->B;
     void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
                     B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
                     B.cell_old, B.sub, B.count, B.start, B.partials, B.tmp, B.nbr, B.st, B.stage,
-                    B.red, B.masks, B.inv_rho, B.acoef};
+                    B.red, B.masks, B.inv_rho};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     Prof *keep = B.prof;
@@ -240,8 +261,131 @@ bbg_status pseudo_viscosity(bbg_solver s, float dt) {
     return BBG_OK;
 }
 
+unsigned fbits(float f) {
+    unsigned u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+
+// Capture one whole substep (grid rebuild, density, forces, the corrector as a
+// conditional WHILE node driven by k_corrector_control, integration) into a graph.
+bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
+                           bbg_solver_s::SubstepGraph &g) {
+    const int st0 = s->state, pid0 = s->pid_cur, work = 1 - st0;
+    const Params &P = s->P;
+    const DevBufs &B = s->B;
+    cudaStream_t cs = s->stream;
+    if (!s->aux) CK(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(B.st, 0, sizeof(StepState), cs);
+    launch_grid_update(P, B, st0, pid0, cs);
+    if (s->desc.solver_kind == BBG_SOLVER_SPH) {
+        launch_density(P, B, work, 1, cs);
+        launch_sph_forces(P, B, work, dt, cs);
+    } else {
+        launch_density(P, B, work, 0, cs);
+        launch_non_pressure(P, B, work, 1, dt, dt / s->mass, cs);
+        cudaStreamCaptureStatus status;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;
+        size_t ndeps = 0;
+        cudaGraphConditionalHandle handle = 0;
+        cudaGraphNode_t cnode = nullptr;
+        if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg, &deps, &edges, &ndeps);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        np.conditional.handle = handle;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, cg, deps, edges, ndeps, &np);
+        if (e == cudaSuccess) {
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(s->aux, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                launch_pred_density(P, B, work, -1, delta, s->aux);
+                launch_pressure_force(P, B, work, -1, max_it, dt, dt / s->mass, s->aux);
+                launch_corrector_control(P, B, max_it, handle, s->aux);
+                cudaError_t e2 = cudaStreamEndCapture(s->aux, &body);
+                if (e == cudaSuccess) e = e2;
+            }
+        }
+        if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1,
+                                                                      cudaStreamSetCaptureDependencies);
+    }
+    const float pv = (float)s->desc.pseudo_viscosity * dt;
+    if (pv > 0.1) {
+        float t = dt * (float)s->desc.pseudo_viscosity;
+        t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+        launch_pseudo_viscosity(P, B, st0, t, cs);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e3 = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = e3;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return fail(BBG_ERR_CUDA, "substep graph capture: %s", cudaGetErrorString(e));
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return fail(BBG_ERR_CUDA, "substep graph instantiate: %s", cudaGetErrorString(e));
+    }
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+    g.graph = graph;
+    g.exec = exec;
+    g.valid = true;
+    return BBG_OK;
+}
+
+void after_substep(bbg_solver s, float dt) {
+    (void)dt;
+    s->pid_cur = 1 - s->pid_cur;
+    s->grid_valid = true;
+    s->valid = kPosVel | bit(BBG_FIELD_INTERACTION) | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE) |
+               bit(BBG_FIELD_PRESSURE);
+    if (s->desc.solver_kind == BBG_SOLVER_PCISPH)
+        s->valid |= bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_PRED_DENSITY) |
+                    bit(BBG_FIELD_DENSITY_ERROR) | bit(BBG_FIELD_PRED_POSITION);
+}
+
 bbg_status substep(bbg_solver s, float dt) {
     s->prof.substep++;
+    const bool shipped = s->desc.pcisph_mode == BBG_PCISPH_AS_SHIPPED;
+    int max_it = shipped ? 1 : s->desc.max_iterations;
+    if (max_it < 1) max_it = 1;
+    if (max_it > kMaxIterations) max_it = kMaxIterations;
+    s->P.max_err_ratio = shipped ? 0.01f : (float)s->desc.max_density_error_ratio;
+    const float delta = compute_delta(s->mod2, s->delta_denom, dt);
+    if (s->use_graphs && !s->prof.on) {
+        bbg_solver_s::SubstepGraph *hit = nullptr;
+        for (auto &g : s->graphs)
+            if (g.valid && g.epoch == s->epoch && g.dt_bits == fbits(dt) && g.state == s->state &&
+                g.pid == s->pid_cur && g.max_it == max_it && g.tol_bits == fbits(s->P.max_err_ratio))
+                hit = &g;
+        if (!hit) {
+            hit = &s->graphs[s->graph_next];
+            s->graph_next = (s->graph_next + 1) % 4;
+            bbg_status r = capture_substep(s, dt, max_it, delta, *hit);
+            if (r) return r;
+            hit->epoch = s->epoch;
+            hit->dt_bits = fbits(dt);
+            hit->state = s->state;
+            hit->pid = s->pid_cur;
+            hit->max_it = max_it;
+            hit->tol_bits = fbits(s->P.max_err_ratio);
+        }
+        CK(cudaGraphLaunch(hit->exec, s->stream));
+        s->last_max_it = max_it;
+        s->last_tol = s->P.max_err_ratio;
+        after_substep(s, dt);
+        return BBG_OK;
+    }
     bbg_status r = grid_update(s);
     if (r) return r;
     if (s->desc.solver_kind == BBG_SOLVER_SPH) {
@@ -252,10 +396,6 @@ bbg_status substep(bbg_solver s, float dt) {
         s->valid |= kPosVel | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_FORCE);
         return pseudo_viscosity(s, dt);
     }
-    const bool shipped = s->desc.pcisph_mode == BBG_PCISPH_AS_SHIPPED;
-    const int max_it = shipped ? 1 : s->desc.max_iterations;
-    s->P.max_err_ratio = shipped ? 0.01f : (float)s->desc.max_density_error_ratio;
-    const float delta = compute_delta(s->mod2, s->delta_denom, dt);
     launch_density(s->P, s->B, s->state, 0, s->stream);
     launch_non_pressure(s->P, s->B, s->state, 1, dt, dt / s->mass, s->stream);
     CK_LAUNCH();
@@ -463,7 +603,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.force, n); ALLOC(B.xstar, n); ALLOC(B.pforce, n); ALLOC(B.smoothed, n);
     ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
     ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
-    ALLOC(B.masks, (size_t)kRows * n); ALLOC(B.inv_rho, n); ALLOC(B.acoef, n);
+    ALLOC(B.masks, (size_t)kRows * n); ALLOC(B.inv_rho, n);
     ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);
@@ -492,6 +632,7 @@ bbg_status bbg_destroy(bbg_solver s) {
     cudaSetDevice(s->desc.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_all(s);
+    if (s->aux) cudaStreamDestroy(s->aux);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return BBG_OK;
@@ -501,6 +642,7 @@ bbg_status bbg_set_stream(bbg_solver s, void *stream) {
     if (bbg_status r = check_solver(s)) return r;
     CK(cudaStreamSynchronize(s->stream));
     s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    s->epoch++;
     return BBG_OK;
 }
 
@@ -529,6 +671,7 @@ bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count) {
         d.friction = (float)sh.friction;
     }
     s->P.nshapes = count;
+    s->epoch++;
     return BBG_OK;
 }
 
@@ -538,6 +681,7 @@ static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d
     s->n = n;
     s->P.n = n;
     s->grid_valid = false;
+    s->epoch++;
     s->valid = kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) |
                bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
     return BBG_OK;
@@ -572,6 +716,7 @@ bbg_status bbg_setup(bbg_solver s) {
     s->delta_denom = compute_delta_denom((float)d.target_spacing, s->kernel_radius);
     fill_params(s);
     s->setup_done = true;
+    s->epoch++;
     return BBG_OK;
 }
 
@@ -614,9 +759,21 @@ bbg_status bbg_compute_delta(bbg_solver s, double dt, double *delta) {
     return BBG_OK;
 }
 
+bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable) {
+    if (bbg_status r = check_solver(s)) return r;
+    s->use_graphs = enable != 0;
+    return BBG_OK;
+}
+
 bbg_status bbg_profiler_enable(bbg_solver s, int enable) {
     if (bbg_status r = check_solver(s)) return r;
     s->prof.on = enable != 0;
+    // create the events up front so none is created inside a timed region
+    while (s->prof.on && s->prof.pool.size() < 8192) {
+        cudaEvent_t e = nullptr;
+        CK(cudaEventCreate(&e));
+        s->prof.pool.push_back(e);
+    }
     return BBG_OK;
 }
 

@@ -71,6 +71,7 @@ struct StepState {
     unsigned out_of_grid;
     unsigned nbr_overflow;
     unsigned nonfinite;
+    int iter;                            // corrector iteration (graph-driven loop)
 };
 
 // ----------------------------------------------------------------------------
@@ -220,22 +221,30 @@ __device__ __forceinline__ void for_each_neighbor(const Params &P, const unsigne
     const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
     const int x0 = cx > 0 ? cx - 1 : 0;
     const unsigned n = (unsigned)P.n;
+    // Load the 9 (mask, range start) pairs, then walk all members as one flat sequence so
+    // a warp runs max-over-lanes of the total member count rather than per range.
+    unsigned m[kRows], b[kRows];
 #pragma unroll
-    for (int dz = -1; dz <= 1; ++dz) {
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int z = cz + dz, y = cy + dy;
-            if (z < 0 || z >= nz || y < 0 || y >= ny) continue;
-            const int r = 3 * (dz + 1) + (dy + 1);
-            unsigned m = __ldg(&masks[(unsigned)r * n + (unsigned)i]);
-            if (!m) continue;
-            const unsigned b = __ldg(&start[(unsigned)y * (unsigned)nx + (unsigned)z * plane + (unsigned)x0]);
-            while (m) {
-                const int bit = __ffs(m) - 1;
-                m &= m - 1u;
-                f(b + (unsigned)bit);
-            }
+    for (int r = 0; r < kRows; ++r) {
+        const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+        m[r] = 0u;
+        b[r] = 0u;
+        if (z >= 0 && z < nz && y >= 0 && y < ny) {
+            m[r] = __ldg(&masks[(unsigned)r * n + (unsigned)i]);
+            if (m[r]) b[r] = __ldg(&start[(unsigned)y * (unsigned)nx + (unsigned)z * plane + (unsigned)x0]);
         }
+    }
+    int left = kRows;
+    for (;;) {
+        while (m[0] == 0u) {
+            if (--left == 0) return;
+#pragma unroll
+            for (int r = 0; r < kRows - 1; ++r) { m[r] = m[r + 1]; b[r] = b[r + 1]; }
+            m[kRows - 1] = 0u;
+        }
+        const int bit = __ffs(m[0]) - 1;
+        m[0] &= m[0] - 1u;
+        f(b[0] + (unsigned)bit);
     }
 }
 
@@ -345,26 +354,49 @@ __device__ __forceinline__ Cpq sphere_closest_point(const ShapeDev &s, v3 point,
     return q;
 }
 
-__device__ __forceinline__ float shape_distance(const ShapeDev &s, v3 p, float iz6) {
-    return s.type == 1 ? box_closest_distance(s, p, iz6) : sphere_closest_distance(s, p);
+__device__ __forceinline__ Cpq shape_closest_point(const ShapeDev &s, v3 p, float iz, float iz6) {
+    return s.type == 1 ? box_closest_point(s, p, iz6) : sphere_closest_point(s, p, iz);
 }
 
-// ColliderSet3::ResolveCollision with restitution r (rc1 = (float)(-1.0 - r)).
+// Conservative test that shape s cannot penetrate particle p of radius r: true only when
+// the exact test (IsInside || |signed distance| < r) is false by a margin far above FP32
+// rounding, so skipping the exact evaluation never changes a result.
+__device__ __forceinline__ bool clearly_clear(const ShapeDev &s, v3 p, float r) {
+    const float m = r * 1.0001f + 1e-6f;
+    const float x = p.x - s.t[0], y = p.y - s.t[1], z = p.z - s.t[2];
+    if (s.type == 1) {
+        if (s.reverse)   // container: well inside on every axis
+            return fabsf(x) <= s.hx - m && fabsf(y) <= s.hy - m && fabsf(z) <= s.hz - m;
+        return fabsf(x) >= s.hx + m || fabsf(y) >= s.hy + m || fabsf(z) >= s.hz + m;
+    }
+    if (s.reverse) return false;
+    const float R = s.radius + m;
+    return x * x + y * y + z * z >= R * R * 1.0001f;
+}
+
+// ColliderSet3::ResolveCollision with restitution r (rc1 = (float)(-1.0 - r)).  The
+// reference evaluates each shape's closest distance, then the chosen shape's closest
+// point and IsInside (two more distance evaluations); Shape::ClosestDistance equals the
+// closest-point query's signed distance bit for bit for boxes and spheres, so one query
+// per shape gives the same answer.
 __device__ __forceinline__ void resolve_collision(const Params &P, float r, float rc1, v3 *pos,
                                                   v3 *vel) {
     if (P.nshapes <= 0) return;
+    bool all_clear = true;
+    for (int i = 0; i < P.nshapes; i++) all_clear = all_clear && clearly_clear(P.shapes[i], *pos, P.radius);
+    if (all_clear) return;
     int target = -1;
     float minD = 3.402823466e+38f;   // Infinity = FLT_MAX
+    Cpq q;
     for (int i = 0; i < P.nshapes; i++) {
-        float d = fabsf(shape_distance(P.shapes[i], *pos, P.iz6));
-        if (d < minD) { target = i; minD = d; }
+        const Cpq qi = shape_closest_point(P.shapes[i], *pos, P.iz, P.iz6);
+        const float d = fabsf(qi.sd);
+        if (d < minD) { target = i; minD = d; q = qi; }
     }
     if (target < 0) return;
     const ShapeDev &s = P.shapes[target];
-    Cpq q = s.type == 1 ? box_closest_point(s, *pos, P.iz6) : sphere_closest_point(s, *pos, P.iz);
-    bool inside = (s.reverse != 0) == !(shape_distance(s, *pos, P.iz6) < 0.f);
-    bool penetrating = inside || fabsf(q.sd) < P.radius;
-    if (!penetrating) return;
+    const bool inside = (s.reverse != 0) == !(q.sd < 0.f);
+    if (!(inside || minD < P.radius)) return;
     v3 n = q.normal;
     v3 targetPoint = vadd(q.point, vmul(n, P.radius));
     v3 rel = *vel;   // collider velocity is zero for static shapes

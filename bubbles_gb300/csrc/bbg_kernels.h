@@ -23,7 +23,6 @@ struct DevBufs {
     int *nbr;                  // neighbour count of each sorted slot
     unsigned *masks;           // 9 neighbour masks per slot (range-major)
     float *inv_rho;            // 1 / density
-    float *acoef;              // pressure / density^2 (predicted density in PCISPH)
     StepState *st;
     float *stage;              // n * 3 floats of staging for host copies
     unsigned *red;             // reduction scratch (max |F|)
@@ -62,6 +61,8 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
                          cudaStream_t s);
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,
                            float dt, float dt_over_m, cudaStream_t s);
+void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
+                              cudaGraphConditionalHandle handle, cudaStream_t s);
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
 void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,

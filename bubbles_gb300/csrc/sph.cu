@@ -39,10 +39,10 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
 // Tests every candidate of the 27 cells exactly once per substep and records the
 // neighbour set (the reference bucket, grid.h:423-447) as 9 range masks.
 __global__ void __launch_bounds__(kThreads)
-k_density(Params P, const float4 *__restrict__ pos, unsigned *__restrict__ cell,
+k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
-          float *__restrict__ press, float *__restrict__ acoef, int *__restrict__ nbr,
-          unsigned *__restrict__ masks, int compute_pressure, StepState *st) {
+          float *__restrict__ press, int *__restrict__ nbr, unsigned *__restrict__ masks,
+          int compute_pressure, StepState *st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
@@ -92,10 +92,12 @@ k_density(Params P, const float4 *__restrict__ pos, unsigned *__restrict__ cell,
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
         if (p < 0.f) p *= P.neg_scale;
         press[i] = p;
-        acoef[i] = p / (di * di);
+        reinterpret_cast<float *>(&pos[i])[3] = p / (di * di);   // pos.w = p / rho^2
     }
     rho[i] = di;
-    inv_rho[i] = 1.f / di;
+    const float ir = 1.f / di;
+    inv_rho[i] = ir;
+    reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
     nbr[i] = cnt;
     if (wide) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
@@ -105,7 +107,7 @@ k_density(Params P, const float4 *__restrict__ pos, unsigned *__restrict__ cell,
 // k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).
 __global__ void __launch_bounds__(kThreads)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-               const float *__restrict__ inv_rho, const unsigned *__restrict__ cell,
+               const unsigned *__restrict__ cell,
                const unsigned *__restrict__ start, const unsigned *__restrict__ masks,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
                float *__restrict__ press, int predict, float dt, float dt_over_m) {
@@ -122,8 +124,8 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
         const float d = r2 * rsqrtf(r2);
-        const float w = kv * (1.f - d * P.inv_h) * __ldg(&inv_rho[j]);
-        const float4 vj = __ldg(&vel[j]);
+        const float4 vj = __ldg(&vel[j]);   // vj.w = 1 / rho_j
+        const float w = kv * (1.f - d * P.inv_h) * vj.w;
         fx += (vj.x - vi.x) * w;
         fy += (vj.y - vi.y) * w;
         fz += (vj.z - vi.z) * w;
@@ -157,12 +159,15 @@ k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restri
 // predicted positions, with the density error stored (tolerance mode) and reduced to
 // max |err| and sum |err| for iteration k; also p / rho*^2 for the pressure force.
 __global__ void __launch_bounds__(kThreads)
-k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ xstar,
+k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                const unsigned *__restrict__ masks, float *__restrict__ press,
-               float *__restrict__ rhostar, float *__restrict__ derr, float *__restrict__ acoef,
-               StepState *st, int k, float delta) {
-    if (converged_before(P, st, k)) return;
+               float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
+               float delta) {
+    // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
+    // unconverged iterations); k >= 0: host-launched sequence, skip after convergence.
+    if (k < 0) k = st->iter;
+    else if (converged_before(P, st, k)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float aerr = 0.f;
     if (i < P.n) {
@@ -187,7 +192,7 @@ k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restric
         press[i] = p;
         rhostar[i] = density;
         derr[i] = err;
-        acoef[i] = p / (density * density);
+        reinterpret_cast<float *>(&pos[i])[3] = p / (density * density);   // pos.w = p / rho*^2
         aerr = fabsf(err);
     }
     // block reduction: max |err| (exact as bits of non-negative floats), sum |err| in FP64
@@ -212,31 +217,32 @@ k_pred_density(Params P, const float4 *__restrict__ pos, const float4 *__restric
 __global__ void __launch_bounds__(kThreads)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const unsigned *__restrict__ masks, const float *__restrict__ acoef,
-                 float4 *__restrict__ force, float4 *__restrict__ pforce,
+                 const unsigned *__restrict__ masks, float4 *__restrict__ force,
+                 float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
                  float dt_over_m) {
-    if (converged_before(P, st, k)) return;
+    if (k < 0) k = st->iter;
+    else if (converged_before(P, st, k)) return;
     const bool last = (k == max_it - 1) ||
                       fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
-        const float ai = acoef[i];
+        const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
         for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
             if (j == (unsigned)i) return;
-            const float4 pj = __ldg(&pos[j]);
+            const float4 pj = __ldg(&pos[j]);   // pj.w = p_j / rho*_j^2
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
             const float d = r2 * inv_d;
             // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
             if (d - P.h <= -P.iz && d >= P.iz) {
                 const float x = 1.f - d * P.inv_h;
-                const float c = kg * (ai + __ldg(&acoef[j])) * x * x * inv_d;
+                const float c = kg * (ai + pj.w) * x * x * inv_d;
                 tx += (pj.x - pi.x) * c;
                 ty += (pj.y - pi.y) * c;
                 tz += (pj.z - pi.z) * c;
@@ -265,13 +271,24 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
     }
 }
 
+// End of one corrector iteration in the graph-driven loop: stop when the density error
+// of iteration k is below tolerance or k was the last allowed iteration (the break of
+// ComputePressureForceAndIntegrate, pcisph_equations3.cpp:238-246).
+__global__ void k_corrector_control(Params P, StepState *st, int max_it,
+                                    cudaGraphConditionalHandle handle) {
+    const int k = st->iter;
+    const bool done = (k >= max_it - 1) ||
+                      fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio;
+    st->iter = k + 1;
+    cudaGraphSetConditional(handle, done ? 0u : 1u);
+}
+
 // ComputeAllForcesFor (sph_equations3.cpp:184-278, extended = 0) in Jacobi order: the
 // reference integrates each particle inside the force loop (:277), racing with its
 // neighbours' reads; here all forces read the step-start state and the integrated
 // state goes to the other buffer.
 __global__ void __launch_bounds__(kThreads)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-             const float *__restrict__ inv_rho, const float *__restrict__ acoef,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
              const unsigned *__restrict__ masks, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
@@ -280,7 +297,7 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
     if (i < P.n) {
         const float4 pi = pos[i];
         const float4 vi = vel[i];
-        const float ai = acoef[i];
+        const float ai = pi.w;   // p_i / rho_i^2
         float fx = P.mass * P.gx - P.drag * vi.x;
         float fy = P.mass * P.gy - P.drag * vi.y;
         float fz = P.mass * P.gz - P.drag * vi.z;
@@ -296,13 +313,13 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
             if (d - P.h <= -P.iz) {
                 const float x = 1.f - d * P.inv_h;
                 if (d >= P.iz) {
-                    const float c = kg * (ai + __ldg(&acoef[j])) * x * x * inv_d;
+                    const float c = kg * (ai + pj.w) * x * x * inv_d;
                     tx += (pj.x - pi.x) * c;
                     ty += (pj.y - pi.y) * c;
                     tz += (pj.z - pi.z) * c;
                 }
-                const float4 vj = __ldg(&vel[j]);
-                const float w = kv * x * __ldg(&inv_rho[j]);
+                const float4 vj = __ldg(&vel[j]);   // vj.w = 1 / rho_j
+                const float w = kv * x * vj.w;
                 fx += (vj.x - vi.x) * w;
                 fy += (vj.y - vi.y) * w;
                 fz += (vj.z - vi.z) * w;
@@ -376,9 +393,9 @@ __global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *
 
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
-    k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.cell, B.start, B.rho,
-                                                             B.inv_rho, B.press, B.acoef, B.nbr,
-                                                             B.masks, compute_pressure, B.st);
+    k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell,
+                                                             B.start, B.rho, B.inv_rho, B.press,
+                                                             B.nbr, B.masks, compute_pressure, B.st);
     BBG_PEND(B, s);
 }
 
@@ -386,8 +403,8 @@ void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict
                          float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
     k_non_pressure<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.inv_rho, B.cell, B.start, B.masks, B.force, B.xstar, B.pforce,
-        B.press, predict, dt, dt_over_m);
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.xstar, B.pforce, B.press,
+        predict, dt, dt_over_m);
     BBG_PEND(B, s);
 }
 
@@ -403,8 +420,8 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
                          cudaStream_t s) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
     k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.xstar, B.cell, B.start, B.masks, B.press, B.rhostar, B.derr, B.acoef, B.st,
-        k, delta);
+        P, B.pos[buf], B.xstar, B.cell, B.start, B.masks, B.press, B.rhostar, B.derr, B.st, k,
+        delta);
     BBG_PEND(B, s);
 }
 
@@ -412,16 +429,21 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
                            float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.acoef, B.force, B.pforce, B.xstar,
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pforce, B.xstar,
         B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m);
     BBG_PEND(B, s);
+}
+
+void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
+                              cudaGraphConditionalHandle handle, cudaStream_t s) {
+    k_corrector_control<<<1, 1, 0, s>>>(P, B.st, max_it, handle);
 }
 
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
     BBG_PBEGIN(B, KID_SPH_FORCES, s, -1);
     k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.inv_rho, B.acoef, B.cell, B.start, B.masks, B.force,
-        B.pos[1 - buf], B.vel[1 - buf], B.st, dt);
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pos[1 - buf],
+        B.vel[1 - buf], B.st, dt);
     BBG_PEND(B, s);
 }
 

@@ -234,6 +234,9 @@ class Solver:
                counts.ctypes.data_as(N._UP), ids.ctypes.data_as(N._UP))
         return cell_of, counts, ids
 
+    def use_cuda_graphs(self, on=True):
+        N.call("bbg_use_cuda_graphs", self.h, int(bool(on)))
+
     def profiler_enable(self, on=True):
         N.call("bbg_profiler_enable", self.h, int(bool(on)))
 

@@ -163,6 +163,11 @@ bbg_status bbg_advance(bbg_solver s, double dt, bbg_step_stats *stats);
 /* AdvanceTimeStep: one substep of length dt (pcisph_solver3.cpp:42-65,
  * sph_solver3.cpp:48-67).  Asynchronous when stats is NULL. */
 bbg_status bbg_advance_time_step(bbg_solver s, double dt, bbg_step_stats *stats);
+/* Replay whole substeps as CUDA graphs (default on): the corrector runs as a conditional
+ * WHILE node whose condition the device sets after each iteration, so a substep is one
+ * graph launch with no host round trip.  Graphs are cached per substep length, so the
+ * first substep of a new dt pays for a capture.  Profiling uses direct launches. */
+bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable);
 /* Read the statistics of the last substep (synchronises). */
 bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
 
