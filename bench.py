@@ -43,11 +43,11 @@ ALG_BYTES = {
     "k_hash_count": 16 + 4 + 4,                    # pos in; cell, arrival index out
     "k_place": 4 + 4 + 4 + 4 + 8,                  # cell, index, start, id in; (id, slot) out
     "k_rank_gather": 8 + 4 + 8 + 32 + 32 + 4 + 4 + 4,  # tmp, cell, start, pos+vel in/out, id, slot, cell
-    "k_density": 16 + 4 + 4 + 4,                   # pos, cell in; density, neighbour count out
-    "k_non_pressure": 16 + 16 + 4 + 4 + 16 + 16 + 16 + 4,  # pos, vel, rho, cell; F, x*, Fp, p out
-    "k_pred_density": 16 + 16 + 4 + 4 + 4 + 4 + 4,  # pos, x*, cell, p in; p, rho*, err out
-    "k_pressure_force": 16 + 16 + 4 + 4 + 4 + 16 + 16 + 16,  # pos, vel, cell, p, rho*, F; Fp, x*
-    "k_sph_forces": 16 + 16 + 4 + 4 + 4 + 16 + 32,
+    "k_density": 16 + 4 + 36 + 4 + 4 + 4 + 4,     # pos, cell in; 9 masks, rho, 1/rho, vel.w, count out
+    "k_non_pressure": 16 + 16 + 4 + 36 + 16 + 16 + 16 + 4,  # pos, vel, cell, masks; F, x*, Fp, p out
+    "k_pred_density": 16 + 4 + 36 + 8 + 4 + 4 + 4,  # x*, cell, masks, p in/out; rho*, err, pos.w out
+    "k_pressure_force": 16 + 16 + 4 + 36 + 16 + 16 + 16,  # pos, vel, cell, masks, F; Fp, x* out
+    "k_sph_forces": 16 + 16 + 4 + 36 + 16 + 32,
     "k_integrate": 16 + 16 + 16 + 32,
 }
 
