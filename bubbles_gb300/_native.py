@@ -110,6 +110,10 @@ SIGNATURES = {
     "bbg_compute_pseudo_viscosity_interpolation": [_P, _D],
     "bbg_compute_pressure_force_and_integrate": [_P, _D, _D, _D, _I, ctypes.POINTER(StepStats)],
     "bbg_compute_delta": [_P, _D, _DP],
+    "bbg_predict_velocity_and_position": [_P, _D, _I],
+    "bbg_predict_pressure": [_P, _D],
+    "bbg_predict_pressure_force": [_P],
+    "bbg_accumulate_and_integrate": [_P, _D],
     "bbg_compute_number_of_time_steps": [_P, _D, _D, ctypes.POINTER(ctypes.c_uint)],
     "bbg_particle_count": [_P, _IP],
     "bbg_get_field": [_P, _I, _FP],

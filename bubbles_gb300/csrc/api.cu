@@ -822,7 +822,7 @@ bbg_status bbg_compute_pressure_force_and_integrate(bbg_solver s, double dt, dou
     CK(cudaMemsetAsync(s->B.st->err_sum, 0, sizeof(s->B.st->err_sum), s->stream));
     CK(cudaMemsetAsync(&s->B.st->max_force_bits, 0, 4, s->stream));
     s->P.max_err_ratio = (float)max_err;
-    launch_predict_first(s->P, s->B, s->state, fdt, fdt / s->mass, s->stream);
+    launch_predict_first(s->P, s->B, s->state, 1, fdt, fdt / s->mass, s->stream);
     CK_LAUNCH();
     bbg_status r = corrector(s, fdt, (float)delta, max_it);
     if (r) return r;
@@ -834,6 +834,59 @@ bbg_status bbg_compute_pressure_force_and_integrate(bbg_solver s, double dt, dou
         add_substep_stats(s, fdt);
         *stats = s->acc;
     }
+    return BBG_OK;
+}
+
+bbg_status bbg_predict_velocity_and_position(bbg_solver s, double dt, int is_first) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_FORCE))) return fail(BBG_ERR_STATE, "forces not valid");
+    if (!is_first && !(s->valid & bit(BBG_FIELD_PRESSURE_FORCE)))
+        return fail(BBG_ERR_STATE, "pressure force not valid");
+    launch_predict_first(s->P, s->B, s->state, is_first ? 1 : 0, (float)dt, (float)dt / s->mass,
+                         s->stream);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_PRED_POSITION);
+    if (is_first)
+        s->valid |= bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_PRESSURE_FORCE) |
+                    bit(BBG_FIELD_PRED_DENSITY) | bit(BBG_FIELD_DENSITY_ERROR);
+    return BBG_OK;
+}
+
+bbg_status bbg_predict_pressure(bbg_solver s, double delta) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_PRED_POSITION)) || !(s->valid & bit(BBG_FIELD_PRESSURE)))
+        return fail(BBG_ERR_STATE, "predicted positions and pressure must be valid");
+    CK(cudaMemsetAsync(s->B.st->err_bits, 0, sizeof(s->B.st->err_bits), s->stream));
+    CK(cudaMemsetAsync(s->B.st->err_sum, 0, sizeof(s->B.st->err_sum), s->stream));
+    launch_pred_density(s->P, s->B, s->state, 0, (float)delta, s->stream);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_PRED_DENSITY) | bit(BBG_FIELD_DENSITY_ERROR);
+    return BBG_OK;
+}
+
+bbg_status bbg_predict_pressure_force(bbg_solver s) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_PRESSURE)) || !(s->valid & bit(BBG_FIELD_PRED_DENSITY)))
+        return fail(BBG_ERR_STATE, "pressure and predicted density must be valid");
+    launch_pack_acoef(s->P, s->B, s->state, s->stream);
+    CK(cudaMemsetAsync(s->B.st->err_bits, 0, sizeof(s->B.st->err_bits), s->stream));
+    launch_pressure_force(s->P, s->B, s->state, 0, 1 << 30, 0.f, 0.f, s->stream, 1);
+    CK_LAUNCH();
+    s->valid |= bit(BBG_FIELD_PRESSURE_FORCE);
+    return BBG_OK;
+}
+
+bbg_status bbg_accumulate_and_integrate(bbg_solver s, double dt) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_grid(s)) return r;
+    if (!(s->valid & bit(BBG_FIELD_FORCE)) || !(s->valid & bit(BBG_FIELD_PRESSURE_FORCE)))
+        return fail(BBG_ERR_STATE, "forces and pressure forces must be valid");
+    launch_accumulate_integrate(s->P, s->B, s->state, (float)dt, s->stream);
+    CK_LAUNCH();
+    s->state = 1 - s->state;
     return BBG_OK;
 }
 

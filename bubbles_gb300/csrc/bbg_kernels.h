@@ -55,15 +55,18 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
                     cudaStream_t s);
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
                          float dt_over_m, cudaStream_t s);
-void launch_predict_first(const Params &P, const DevBufs &B, int buf, float dt, float dt_over_m,
-                          cudaStream_t s);
+void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_first, float dt,
+                          float dt_over_m, cudaStream_t s);
+void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
                          cudaStream_t s);
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,
-                           float dt, float dt_over_m, cudaStream_t s);
+                           float dt, float dt_over_m, cudaStream_t s, int force_only = 0);
 void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
                               cudaGraphConditionalHandle handle, cudaStream_t s);
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
+void launch_accumulate_integrate(const Params &P, const DevBufs &B, int buf, float dt,
+                                 cudaStream_t s);
 void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
                              cudaStream_t s);

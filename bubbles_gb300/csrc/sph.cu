@@ -140,19 +140,35 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     }
 }
 
-// PredictVelocityAndPositionFor with is_first = 1 (pcisph_equations3.cpp:13-27) on the
-// forces already in `force`: p = 0, Fp = 0, x* from F alone.
+// PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28) on the forces already in
+// `force`; with is_first: p = 0, Fp = 0, rho* = rho, so x* comes from F alone.
 __global__ void __launch_bounds__(kThreads)
 k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                 const float4 *__restrict__ force, float4 *__restrict__ xstar,
-                float4 *__restrict__ pforce, float *__restrict__ press, float dt, float dt_over_m) {
+                float4 *__restrict__ pforce, float *__restrict__ press,
+                float *__restrict__ rhostar, const float *__restrict__ rho, float *__restrict__ derr,
+                int is_first, float dt, float dt_over_m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    press[i] = 0.f;
-    pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (is_first) {
+        rhostar[i] = rho[i];
+        pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        derr[i] = 0.f;
+        press[i] = 0.f;
+    }
     v3 xs;
-    predict_particle(P, dt, dt_over_m, V(force[i]), V(0.f, 0.f, 0.f), V(pos[i]), V(vel[i]), &xs);
+    predict_particle(P, dt, dt_over_m, V(force[i]), V(pforce[i]), V(pos[i]), V(vel[i]), &xs);
     xstar[i] = F4(xs);
+}
+
+// pos.w = p / rho*^2 from the pressure and predicted-density fields (used when those
+// fields were set from outside rather than by the predicted-density pass).
+__global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press,
+                             const float *__restrict__ rhostar) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = rhostar[i];
+    reinterpret_cast<float *>(&pos[i])[3] = press[i] / (d * d);
 }
 
 // PredictPressureFor (pcisph_equations3.cpp:60-90) over the step-start neighbour set at
@@ -221,11 +237,11 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
-                 float dt_over_m) {
+                 float dt_over_m, int force_only) {
     if (k < 0) k = st->iter;
     else if (converged_before(P, st, k)) return;
-    const bool last = (k == max_it - 1) ||
-                      fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio;
+    const bool last = !force_only && ((k == max_it - 1) ||
+                      fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
@@ -259,7 +275,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
             pos_out[i] = F4(x);
             vel_out[i] = F4(v);
             fbits = __float_as_uint(vlen(ft));
-        } else {
+        } else if (!force_only) {
             v3 xs;
             predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
             xstar[i] = F4(xs);
@@ -337,6 +353,22 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
     if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
 }
 
+// AccumulateForcesFor + TimeIntegrationFor (AccumulateAndIntegrateGPU,
+// pcisph_equations3.cpp:179-212): F += Fp, then integrate into the other buffer.
+__global__ void __launch_bounds__(kThreads)
+k_accumulate_integrate(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                       float4 *__restrict__ force, const float4 *__restrict__ pforce,
+                       float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, float dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const v3 ft = vadd(V(force[i]), V(pforce[i]));
+    force[i] = F4(ft);
+    v3 x = V(pos[i]), v = V(vel[i]);
+    integrate_particle(P, dt, ft, &x, &v);
+    pos_out[i] = F4(x);
+    vel_out[i] = F4(v);
+}
+
 // TimeIntegrationFor over all particles (TimeIntegrationGPU, sph_equations3.cpp:622-634)
 __global__ void __launch_bounds__(kThreads)
 k_integrate(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
@@ -408,11 +440,12 @@ void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict
     BBG_PEND(B, s);
 }
 
-void launch_predict_first(const Params &P, const DevBufs &B, int buf, float dt, float dt_over_m,
-                          cudaStream_t s) {
+void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_first, float dt,
+                          float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_PREDICT_FIRST, s, -1);
     k_predict_first<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.force, B.xstar, B.pforce, B.press, dt, dt_over_m);
+        P, B.pos[buf], B.vel[buf], B.force, B.xstar, B.pforce, B.press, B.rhostar, B.rho, B.derr,
+        is_first, dt, dt_over_m);
     BBG_PEND(B, s);
 }
 
@@ -425,12 +458,16 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
     BBG_PEND(B, s);
 }
 
+void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s) {
+    k_pack_acoef<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.press, B.rhostar);
+}
+
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it, float dt,
-                           float dt_over_m, cudaStream_t s) {
+                           float dt_over_m, cudaStream_t s, int force_only) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
         P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pforce, B.xstar,
-        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m);
+        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, force_only);
     BBG_PEND(B, s);
 }
 
@@ -444,6 +481,14 @@ void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cud
     k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
         P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pos[1 - buf],
         B.vel[1 - buf], B.st, dt);
+    BBG_PEND(B, s);
+}
+
+void launch_accumulate_integrate(const Params &P, const DevBufs &B, int buf, float dt,
+                                 cudaStream_t s) {
+    BBG_PBEGIN(B, KID_INTEGRATE, s, -1);
+    k_accumulate_integrate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+        P, B.pos[buf], B.vel[buf], B.force, B.pforce, B.pos[1 - buf], B.vel[1 - buf], dt);
     BBG_PEND(B, s);
 }
 

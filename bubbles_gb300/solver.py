@@ -174,6 +174,18 @@ class Solver:
                float(delta), int(max_it), ctypes.byref(st))
         return st.as_dict()
 
+    def predict_velocity_and_position(self, dt, is_first):
+        N.call("bbg_predict_velocity_and_position", self.h, float(dt), int(is_first))
+
+    def predict_pressure(self, delta):
+        N.call("bbg_predict_pressure", self.h, float(delta))
+
+    def predict_pressure_force(self):
+        N.call("bbg_predict_pressure_force", self.h)
+
+    def accumulate_and_integrate(self, dt):
+        N.call("bbg_accumulate_and_integrate", self.h, float(dt))
+
     def compute_delta(self, dt):
         d = ctypes.c_double()
         N.call("bbg_compute_delta", self.h, float(dt), ctypes.byref(d))

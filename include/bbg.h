@@ -186,6 +186,14 @@ bbg_status bbg_compute_pressure_force_and_integrate(bbg_solver s, double dt,
                                                     double delta, int max_iterations,
                                                     bbg_step_stats *stats);
 bbg_status bbg_compute_delta(bbg_solver s, double dt, double *delta);  /* ComputeDelta */
+/* The corrector's passes on their own, for callers composing their own loop:
+ * PredictVelocityAndPositionGPU (pcisph_equations3.cpp:50-56), PredictPressureGPU
+ * (:108-112; the density error is stored), PredictPressureForceGPU (:173-177; from the
+ * pressure and predicted-density fields) and AccumulateAndIntegrateGPU (:207-212). */
+bbg_status bbg_predict_velocity_and_position(bbg_solver s, double dt, int is_first);
+bbg_status bbg_predict_pressure(bbg_solver s, double delta);
+bbg_status bbg_predict_pressure_force(bbg_solver s);
+bbg_status bbg_accumulate_and_integrate(bbg_solver s, double dt);
 /* SphParticleSet3::ComputeNumberOfTimeSteps (particle.h:584-608). */
 bbg_status bbg_compute_number_of_time_steps(bbg_solver s, double remaining, double scale,
                                             unsigned *count);

@@ -92,6 +92,10 @@ def load(variant="f32"):
                                                             ctypes.c_double, ctypes.c_int,
                                                             ctypes.c_int, _D]),
         "orc_time_integration": (None, [_P, ctypes.c_double]),
+        "orc_predict_velocity_and_position": (None, [_P, ctypes.c_double, ctypes.c_int]),
+        "orc_predict_pressure": (None, [_P, ctypes.c_double]),
+        "orc_predict_pressure_force": (None, [_P]),
+        "orc_accumulate_and_integrate": (None, [_P, ctypes.c_double]),
         "orc_sph_all_forces": (None, [_P, ctypes.c_double, ctypes.c_int]),
         "orc_pseudo_viscosity": (None, [_P, ctypes.c_double]),
         "orc_number_of_time_steps": (ctypes.c_uint, [_P, ctypes.c_double, ctypes.c_double]),
@@ -231,6 +235,18 @@ class OracleSim:
 
     def time_integration(self, dt):
         self.lib.orc_time_integration(self.h, dt)
+
+    def predict_velocity_and_position(self, dt, is_first):
+        self.lib.orc_predict_velocity_and_position(self.h, dt, int(is_first))
+
+    def predict_pressure(self, delta):
+        self.lib.orc_predict_pressure(self.h, delta)
+
+    def predict_pressure_force(self):
+        self.lib.orc_predict_pressure_force(self.h)
+
+    def accumulate_and_integrate(self, dt):
+        self.lib.orc_accumulate_and_integrate(self.h, dt)
 
     def sph_all_forces(self, dt, inplace=0):
         self.lib.orc_sph_all_forces(self.h, dt, int(inplace))

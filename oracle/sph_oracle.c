@@ -1040,6 +1040,23 @@ void orc_pseudo_viscosity(orc_sim *s, double dt_in) {
     }
 }
 
+/* PredictVelocityAndPositionCPU / PredictPressureCPU / PredictPressureForceCPU /
+ * AccumulateAndIntegrateCPU, pcisph_equations3.cpp:30-38, 92-98, 157-163, 190-197 */
+void orc_predict_velocity_and_position(orc_sim *s, double dt, int is_first) {
+    pass_ctx pp = {s, is_first != 0, (Float)dt};
+    parallel_for(s->n, k_predict, &pp);
+}
+void orc_predict_pressure(orc_sim *s, double delta) {
+    s->tol_mode = 1;
+    pass_ctx pr = {s, 0, (Float)delta};
+    parallel_for(s->n, k_pred_pressure, &pr);
+}
+void orc_predict_pressure_force(orc_sim *s) { parallel_for(s->n, k_pred_force, s); }
+void orc_accumulate_and_integrate(orc_sim *s, double dt) {
+    pass_ctx pi = {s, 0, (Float)dt};
+    parallel_for(s->n, k_accumulate_integrate, &pi);
+}
+
 /* ComputePressureForceAndIntegrate, pcisph_equations3.cpp:218-256 */
 int orc_pressure_force_and_integrate(orc_sim *s, double dt_in, double max_err_ratio,
                                      double delta_in, int max_it, int mode, double *final_err) {

@@ -121,6 +121,11 @@ int      orc_pressure_force_and_integrate(orc_sim *s, double dt, double max_err_
                                           double delta, int max_it, int mode,
                                           double *final_err);
 void     orc_time_integration(orc_sim *s, double dt);
+/* The corrector's sub-passes on their own (tolerance mode stores densityErrors). */
+void     orc_predict_velocity_and_position(orc_sim *s, double dt, int is_first);
+void     orc_predict_pressure(orc_sim *s, double delta);
+void     orc_predict_pressure_force(orc_sim *s);
+void     orc_accumulate_and_integrate(orc_sim *s, double dt);
 /* SPH all-forces pass. inplace=1: the reference as shipped (integrates each particle
  * inside the force loop, sph_equations3.cpp:277); inplace=0: Jacobi order. */
 void     orc_sph_all_forces(orc_sim *s, double dt, int inplace);

@@ -205,16 +205,70 @@ def test_corrector_fixed_iterations(gpu, moved):
     # rho* - rho0, so its bound is relative to delta * rho0 per iteration
     pg_, po_ = g.get(bb.FIELD_PRESSURE), o.get(O.PRESSURE)
     assert np.max(np.abs(pg_ - po_)) <= RTOL * 3 * abs(delta) * 1000.0
-    # pressure force: a cancelling sum, bounded relative to the sum of its |summands|
+    # pressure force after 3 iterations: p = sum_k delta (rho*_k - rho0) amplifies FP32
+    # rounding of rho* by delta, so the bound is the FP32 envelope of the reference
+    # algorithm itself, measured as the FP32-vs-FP64 oracle difference on this input
+    # (each sub-pass is held to 1e-5 from identical inputs in test_corrector_sub_passes)
+    o64 = O.OracleSim(sc, p, v, variant="f64")
+    o64.update_grid_distribution()
+    o64.compute_particle_interaction()
+    o64.set(O.DENSITY, g.get(bb.FIELD_DENSITY))
+    o64.set(O.FORCE, f_np)
+    o64.pressure_force_and_integrate(dt, 0.0, delta, 3, O.PCISPH_TOLERANCE)
     scale = pressure_force_scale(o, x0, g.scalars()["mass"], g.scalars()["kernel_radius"])
+    env = np.linalg.norm(o.get(O.PRESSURE_FORCE) - o64.get(O.PRESSURE_FORCE), axis=1)
     dfp = np.linalg.norm(g.get(bb.FIELD_PRESSURE_FORCE) - o.get(O.PRESSURE_FORCE), axis=1)
-    worst = float(np.max(dfp / (scale + 1e-30)))
-    assert worst <= RTOL, worst
-    df = np.linalg.norm(g.get(bb.FIELD_FORCE) - o.get(O.FORCE), axis=1)
-    assert np.all(df <= RTOL * (scale + np.linalg.norm(f_np, axis=1)))
+    assert np.all(dfp <= np.maximum(RTOL * scale, 2.0 * env.max())), float(np.max(dfp - 2 * env.max()))
     pg, vg = g.download()
     assert np.max(np.abs(pg - o.get(O.POSITION))) <= RTOL * sc["spacing"]
     assert np.max(np.abs(vg - o.get(O.VELOCITY))) <= RTOL * max(1.0, np.abs(vg).max())
+    g.close()
+
+
+def test_corrector_sub_passes(gpu, moved):
+    """PredictVelocityAndPosition, PredictPressure, PredictPressureForce and
+    AccumulateAndIntegrate each from identical inputs."""
+    sc, p, v = moved
+    g, o = pair(sc, p, v)
+    dt = sc["dt"]
+    g.update_grid_distribution()
+    g.compute_density(0)
+    o.update_grid_distribution()
+    o.compute_particle_interaction()
+    o.set(O.DENSITY, g.get(bb.FIELD_DENSITY))
+    g.compute_non_pressure_force()
+    o.set(O.FORCE, g.get(bb.FIELD_FORCE))
+    delta = g.compute_delta(dt)
+    # prediction (collider included): bit-exact from identical forces
+    g.predict_velocity_and_position(dt, 1)
+    o.predict_velocity_and_position(dt, 1)
+    assert np.array_equal(g.get(bb.FIELD_PRED_POSITION), o.get(O.PRED_POSITION).astype(np.float32))
+    # predicted density and pressure: 1e-5 relative (pressure relative to delta * rho0)
+    g.predict_pressure(delta)
+    o.predict_pressure(delta)
+    ok, worst = rel_close(g.get(bb.FIELD_PRED_DENSITY), o.get(O.PRED_DENSITY))
+    assert ok, worst
+    assert np.max(np.abs(g.get(bb.FIELD_PRESSURE) - o.get(O.PRESSURE))) <= RTOL * abs(delta) * 1000.0
+    # pressure force from identical pressure and predicted density
+    o.set(O.PRESSURE, g.get(bb.FIELD_PRESSURE))
+    o.set(O.PRED_DENSITY, g.get(bb.FIELD_PRED_DENSITY))
+    g.predict_pressure_force()
+    o.predict_pressure_force()
+    x0 = o.get(O.POSITION)
+    scale = pressure_force_scale(o, x0, g.scalars()["mass"], g.scalars()["kernel_radius"])
+    dfp = np.linalg.norm(g.get(bb.FIELD_PRESSURE_FORCE) - o.get(O.PRESSURE_FORCE), axis=1)
+    assert np.all(dfp <= RTOL * scale)
+    # second prediction uses F + Fp: bit-exact from identical F and Fp
+    o.set(O.PRESSURE_FORCE, g.get(bb.FIELD_PRESSURE_FORCE))
+    g.predict_velocity_and_position(dt, 0)
+    o.predict_velocity_and_position(dt, 0)
+    assert np.array_equal(g.get(bb.FIELD_PRED_POSITION), o.get(O.PRED_POSITION).astype(np.float32))
+    # accumulate + integrate: bit-exact
+    g.accumulate_and_integrate(dt)
+    o.accumulate_and_integrate(dt)
+    pg, vg = g.download()
+    assert np.array_equal(pg, o.get(O.POSITION).astype(np.float32))
+    assert np.array_equal(vg, o.get(O.VELOCITY).astype(np.float32))
     g.close()
 
 
