@@ -126,6 +126,7 @@ SIGNATURES = {
     "bbg_neighbor_counts": [_P, _IP],
     "bbg_profiler_enable": [_P, _I],
     "bbg_use_cuda_graphs": [_P, _I],
+    "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P],
     "bbg_profiler_report": [_P, _I, ctypes.c_char_p, _DP, _IP, _IP,
                             ctypes.POINTER(ctypes.c_int64)],
 }

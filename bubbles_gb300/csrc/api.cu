@@ -42,6 +42,16 @@ constexpr unsigned kPosVel = bit(BBG_FIELD_POSITION) | bit(BBG_FIELD_VELOCITY);
 
 }  // namespace
 
+namespace bbg {
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+}  // namespace bbg
+
 struct bbg_solver_s {
     bbg_solver_desc desc;
     int capacity = 0, n = 0;

@@ -32,8 +32,14 @@ struct DevBufs {
 #define BBG_PBEGIN(B, id, s, it) do { if ((B).prof) (B).prof->begin((id), (s), (it)); } while (0)
 #define BBG_PEND(B, s) do { if ((B).prof) (B).prof->end(s); } while (0)
 
+// api.cu: record the message returned by bbg_last_error()
+int set_error(int code, const char *fmt, ...);
+
 // grid.cu
 size_t scan_partials_needed(unsigned cells);
+// exclusive scan of per-cell counts into start[0..cells] (zeroes the counts)
+void launch_cell_scan(unsigned *count, unsigned cells, unsigned *partials, unsigned *start,
+                      cudaStream_t s);
 void launch_grid_update(const Params &P, const DevBufs &B, int src_buf, int pid_src,
                         cudaStream_t s);
 void launch_upload(const DevBufs &B, int buf, int pid_buf, const float *d_pos, const float *d_vel,

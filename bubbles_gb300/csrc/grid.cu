@@ -158,6 +158,14 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
 
 size_t scan_partials_needed(unsigned cells) { return (size_t)blocks_for(cells, kScanTile) + 1; }
 
+void launch_cell_scan(unsigned *count, unsigned cells, unsigned *partials, unsigned *start,
+                      cudaStream_t s) {
+    const int nb = blocks_for(cells, kScanTile);
+    k_scan_reduce<<<nb, kScanThreads, 0, s>>>(count, cells, partials);
+    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, nb);
+    k_scan_apply<<<nb, kScanThreads, 0, s>>>(count, cells, partials, start);
+}
+
 void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src, cudaStream_t s) {
     const int n = P.n;
     const unsigned cells = P.g.total;

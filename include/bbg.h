@@ -219,6 +219,31 @@ bbg_status bbg_dump_grid(bbg_solver s, uint32_t *cell_of_particle, uint32_t *cel
 /* Neighbour count of each particle (caller order) at the last grid update. */
 bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts);
 
+/* ----- allocation-free grid sort ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc -- a host
+ * application that owns the device-memory budget and loads this library as a plugin,
+ * or code running where device allocation is forbidden.  It computes the grid of
+ * bbg_update_grid_distribution + bbg_dump_grid on caller-owned device buffers:
+ *   d_pos          n xyz float triples (caller order)
+ *   d_cell_of      n cell ids (caller order)
+ *   d_sorted_ids   n particle indices sorted by (cell id, index)
+ *   d_cell_start   cells + 1 offsets of each cell's range in d_sorted_ids
+ * with the grid of UtilBuildGridForDomain(domain, spacing, spacing_scale).  It never
+ * allocates: its scratch is one fixed __device__ array of BBG_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading the library holds until exit, so n and the cell count are
+ * capped (BBG_ERR_CAPACITY beyond).  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and must not be inside a stream capture.  All calls share the
+ * array: calls whose GPU work overlaps race and must be serialised.  Asynchronous on
+ * `cuda_stream` (NULL = the legacy default stream). */
+#define BBG_NOALLOC_MAX_PARTICLES 1048576
+#define BBG_NOALLOC_MAX_CELLS 1048576
+#define BBG_NOALLOC_SCRATCH_BYTES 20973576
+bbg_status bbg_grid_sort_noalloc(const float *d_pos, int n, const double domain_min[3],
+                                 const double domain_max[3], double spacing,
+                                 double spacing_scale, uint32_t *d_cell_of,
+                                 uint32_t *d_sorted_ids, uint32_t *d_cell_start,
+                                 void *cuda_stream);
+
 /* ----- profiling (ProfilerPrepare / ProfilerFinish around every GPULaunch,
  *       src/cuda/cutil.h:237-244; ProfilerReport, src/core/profiler.cpp:175-247) ---- */
 /* Record CUDA events around every kernel launch on the solver's stream. */
