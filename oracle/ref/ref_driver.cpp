@@ -1,0 +1,224 @@
+/*
+ * ref_driver.cpp -- C entry points over the reference's own solver classes and CPU
+ * passes, compiled together with the reference sources by build_ref.py (host-only,
+ * single thread).  Test infrastructure only: it pins the CPU oracle and generates the
+ * golden fixtures under tests/golden/.  Parameters use the oracle's orc_params layout.
+ */
+#include <collider.h>
+#include <cutil.h>
+#include <interaction.h>
+#include <pcisph_solver.h>
+#include <shape.h>
+#include <sph_solver.h>
+#include <transform.h>
+#include <util.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "../sph_oracle.h"
+
+/* Normally defined by src/solvers/pcisph_solver2.cpp:7, which this build leaves out. */
+extern const Float kDefaultTimeStepLimitScale = 5.0;
+
+/* Non-static reference functions without a header declaration. */
+void PredictVelocityAndPositionCPU(PciSphSolverData3 *data, Float timeIntervalInSeconds, int is_first);
+void PredictPressureCPU(PciSphSolverData3 *data, Float delta);
+void PredictPressureForceCPU(PciSphSolverData3 *data);
+void AccumulateAndIntegrateCPU(PciSphSolverData3 *data, Float timeStep);
+void AdvanceTimeStep(PciSphSolver3 *solver, Float timeStep, int use_cpu);
+void AdvanceTimeStep(SphSolver3 *solver, Float timeStep, int use_cpu);
+
+struct RefSim {
+    int n = 0, kind = 0;
+    PciSphSolver3 pci;
+    SphSolver3 sph;
+    SphSolverData3 *data = nullptr;
+    SphParticleSet3 *sphSet = nullptr;
+    ParticleSet3 *pSet = nullptr;
+    Grid3 *grid = nullptr;
+};
+
+static vec3f V3(const double *a) { return vec3f((Float)a[0], (Float)a[1], (Float)a[2]); }
+
+extern "C" {
+
+int ref_float_bytes(void) { return (int)sizeof(Float); }
+
+RefSim *ref_create(const orc_params *p, int n, const double *pos, const double *vel, int kind) {
+    SetCPUThreads(1);
+    SetSystemUseCPU();
+    RefSim *s = new RefSim();
+    s->n = n;
+    s->kind = kind;
+    ParticleSetBuilder3 builder;
+    for (int i = 0; i < n; i++) {
+        vec3f v = vel ? V3(&vel[3 * i]) : vec3f(0);
+        builder.AddParticle(V3(&pos[3 * i]), v);
+    }
+    SphSolverData3 *data = DefaultSphSolverData3(false);
+    data->eosExponent = p->eos_exponent;
+    data->negativePressureScale = p->negative_pressure_scale;
+    data->viscosity = p->viscosity;
+    data->pseudoViscosity = p->pseudo_viscosity;
+    data->soundSpeed = p->sound_speed;
+    data->dragCoefficient = p->drag_coefficient;
+    InteractionsBuilder3 ib;
+    AddConstantInteraction(ib, V3(p->gravity));
+    data->cInteractions = ib.MakeConstantInteractions(data->cInteractionsCount);
+    s->data = data;
+    s->sphSet = SphParticleSet3FromBuilder(&builder);
+    Bounds3f domain(V3(p->domain_min), V3(p->domain_max));
+    s->grid = UtilBuildGridForDomain(domain, p->target_spacing, p->grid_spacing_scale);
+    if (kind == 0) {
+        s->pci.Initialize(data);
+        s->pci.Setup(p->target_density, p->target_spacing, p->relative_kernel_radius, s->grid, s->sphSet);
+    } else {
+        s->sph.Initialize(data);
+        s->sph.Setup(p->target_density, p->target_spacing, p->relative_kernel_radius, s->grid, s->sphSet);
+    }
+    s->pSet = s->sphSet->GetParticleSet();
+    if (p->mass > 0) {
+        s->pSet->SetMass(p->mass);
+        Float mo = s->pSet->GetMass() / s->sphSet->GetTargetDensity();
+        s->pci.massOverTargetDensitySquared = mo * mo;
+    }
+    if (p->n_colliders > 0) {
+        ColliderSetBuilder3 cb;
+        for (int i = 0; i < p->n_colliders; i++) {
+            const orc_shape &c = p->colliders[i];
+            bool at_origin = c.center[0] == 0 && c.center[1] == 0 && c.center[2] == 0;
+            Transform t = at_origin ? Transform() : Translate(V3(c.center));
+            Shape *shape = c.type == ORC_SHAPE_BOX ? MakeBox(t, V3(c.size), c.reverse != 0)
+                                                   : MakeSphere(t, (Float)c.size[0], c.reverse != 0);
+            cb.AddCollider3(shape, c.friction);
+        }
+        ColliderSet3 *cs = cb.GetColliderSet();
+        if (kind == 0) s->pci.SetColliders(cs);
+        else s->sph.SetColliders(cs);
+    }
+    return s;
+}
+
+void ref_destroy(RefSim *s) { delete s; /* reference buffers live in its memory regions */ }
+
+void ref_scalars(RefSim *s, double out[8]) {
+    out[0] = s->pSet->GetMass();
+    out[1] = s->sphSet->GetKernelRadius();
+    out[2] = s->pci.deltaDenom;
+    out[3] = s->pci.massOverTargetDensitySquared;
+    out[4] = s->sphSet->GetTargetSpacing();
+    out[5] = s->sphSet->GetTargetDensity();
+    out[6] = s->pSet->GetRadius();
+    out[7] = s->sphSet->kernelRadiusOverTargetSpacing;
+}
+
+void ref_grid_info(RefSim *s, int dims[3], double geo[12]) {
+    for (int k = 0; k < 3; k++) {
+        dims[k] = s->grid->usizes[k];
+        geo[k] = s->grid->minPoint[k];
+        geo[3 + k] = s->grid->cellsLen[k];
+        geo[6 + k] = s->grid->bounds.pMin[k];
+        geo[9 + k] = s->grid->bounds.pMax[k];
+    }
+}
+
+/* --- passes ------------------------------------------------------------------ */
+void ref_update_grid_distribution(RefSim *s) { UpdateGridDistributionCPU(s->data); }
+void ref_reset_higher_level(RefSim *s) { s->sphSet->ResetHigherLevel(); }
+int ref_higher_level(RefSim *s) { return s->sphSet->requiresHigherLevelUpdate; }
+void ref_compute_particle_interaction(RefSim *s) { ComputeParticleInteractionCPU(s->data); }
+void ref_compute_density(RefSim *s, int cp) { ComputeDensityCPU(s->data, cp); }
+void ref_compute_non_pressure_force(RefSim *s) { ComputeNonPressureForceCPU(s->data); }
+double ref_compute_delta(RefSim *s, double dt) { return s->pci.ComputeDelta((Float)dt); }
+void ref_pressure_force_and_integrate(RefSim *s, double dt, double tol, double delta, int max_it) {
+    ComputePressureForceAndIntegrate(s->pci.solverData, dt, tol, delta, max_it, 1);
+}
+void ref_predict_velocity_and_position(RefSim *s, double dt, int first) {
+    PredictVelocityAndPositionCPU(s->pci.solverData, dt, first);
+}
+void ref_predict_pressure(RefSim *s, double delta) { PredictPressureCPU(s->pci.solverData, delta); }
+void ref_predict_pressure_force(RefSim *s) { PredictPressureForceCPU(s->pci.solverData); }
+void ref_accumulate_and_integrate(RefSim *s, double dt) { AccumulateAndIntegrateCPU(s->pci.solverData, dt); }
+void ref_pseudo_viscosity(RefSim *s, double dt) { ComputePseudoViscosityInterpolationCPU(s->data, dt); }
+void ref_time_integration(RefSim *s, double dt) { TimeIntegrationCPU(s->data, dt); }
+/* SPH ComputePressureForceCPU as shipped: all forces + in-place integration. */
+void ref_sph_pressure_force(RefSim *s, double dt) { ComputePressureForceCPU(s->data, dt); }
+unsigned ref_number_of_time_steps(RefSim *s, double remaining, double scale) {
+    return s->sphSet->ComputeNumberOfTimeSteps(remaining, s->data->soundSpeed, scale);
+}
+void ref_advance_time_step(RefSim *s, double dt) {
+    if (s->kind == 0) AdvanceTimeStep(&s->pci, dt, 1);
+    else AdvanceTimeStep(&s->sph, dt, 1);
+}
+void ref_advance(RefSim *s, double dt) {
+    if (s->kind == 0) s->pci.Advance(dt);
+    else s->sph.Advance(dt);
+}
+
+/* --- state ------------------------------------------------------------------- */
+static void put(const vec3f &v, double *o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+static vec3f get(const double *a) { return vec3f((Float)a[0], (Float)a[1], (Float)a[2]); }
+
+void ref_get_field(RefSim *s, int f, double *out) {
+    PciSphSolverData3 *pd = s->pci.solverData;
+    for (int i = 0; i < s->n; i++) {
+        switch (f) {
+            case ORC_POSITION: put(s->pSet->GetParticlePosition(i), &out[3 * i]); break;
+            case ORC_VELOCITY: put(s->pSet->GetParticleVelocity(i), &out[3 * i]); break;
+            case ORC_FORCE: put(s->pSet->GetParticleForce(i), &out[3 * i]); break;
+            case ORC_INTERACTION: put(s->pSet->GetParticleInteraction(i), &out[3 * i]); break;
+            case ORC_DENSITY: out[i] = s->pSet->GetParticleDensity(i); break;
+            case ORC_PRESSURE: out[i] = s->pSet->GetParticlePressure(i); break;
+            case ORC_PRED_POSITION: put(pd->tempPositions[i], &out[3 * i]); break;
+            case ORC_PRED_VELOCITY: put(pd->tempVelocities[i], &out[3 * i]); break;
+            case ORC_PRESSURE_FORCE: put(pd->pressureForces[i], &out[3 * i]); break;
+            case ORC_PRED_DENSITY: out[i] = pd->densityPredicted[i]; break;
+            case ORC_DENSITY_ERROR: out[i] = pd->densityErrors[i]; break;
+            default: break;
+        }
+    }
+}
+
+void ref_set_field(RefSim *s, int f, const double *in) {
+    PciSphSolverData3 *pd = s->pci.solverData;
+    for (int i = 0; i < s->n; i++) {
+        switch (f) {
+            case ORC_POSITION: s->pSet->SetParticlePosition(i, get(&in[3 * i])); break;
+            case ORC_VELOCITY: s->pSet->SetParticleVelocity(i, get(&in[3 * i])); break;
+            case ORC_FORCE: s->pSet->SetParticleForce(i, get(&in[3 * i])); break;
+            case ORC_DENSITY: s->pSet->SetParticleDensity(i, (Float)in[i]); break;
+            case ORC_PRESSURE: s->pSet->SetParticlePressure(i, (Float)in[i]); break;
+            case ORC_PRESSURE_FORCE: pd->pressureForces[i] = get(&in[3 * i]); break;
+            case ORC_PRED_DENSITY: pd->densityPredicted[i] = (Float)in[i]; break;
+            default: break;
+        }
+    }
+}
+
+int ref_get_cells(RefSim *s, uint32_t *cell_of, uint32_t *counts, uint32_t *chains) {
+    Grid3 *g = s->grid;
+    for (int i = 0; i < s->n; i++) cell_of[i] = g->GetLinearHashedPosition(s->pSet->GetParticlePosition(i));
+    size_t w = 0;
+    for (unsigned c = 0; c < g->GetCellCount(); c++) {
+        Cell3 *cell = g->GetCell(c);
+        int len = cell->GetChainLength();
+        counts[c] = (uint32_t)len;
+        ParticleChain *node = cell->GetChain();
+        for (int j = 0; j < len && node && w < (size_t)s->n; j++) {
+            chains[w++] = node->pId;
+            node = node->next;
+        }
+    }
+    return (int)g->GetCellCount();
+}
+
+void ref_get_buckets(RefSim *s, int32_t *counts, int32_t *ids) {
+    for (int i = 0; i < s->n; i++) {
+        Bucket *b = s->pSet->GetParticleBucket(i);
+        counts[i] = b->Count();
+        for (int q = 0; q < 100; q++) ids[100 * i + q] = q < b->Count() ? b->Get(q) : -1;
+    }
+}
+
+}  // extern "C"

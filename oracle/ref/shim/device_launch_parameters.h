@@ -1,0 +1,2 @@
+/* Host-only build of the reference: nothing to declare. */
+#pragma once

@@ -1,0 +1,137 @@
+"""ctypes wrapper of the host-only reference build (oracle/ref) -- test infrastructure.
+
+Only available where the reference checkout exists (the recipe builds from it); used to
+pin the CPU oracle and to generate tests/golden/ fixtures.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import oracle as O
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS = {}
+_D = ctypes.POINTER(ctypes.c_double)
+_U32 = ctypes.POINTER(ctypes.c_uint32)
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_P = ctypes.c_void_p
+
+
+def lib_path(variant):
+    return os.path.join(_HERE, "_ref", "libbbref_%s.so" % variant)
+
+
+def available(variant="f32"):
+    if os.path.exists(lib_path(variant)):
+        return True
+    try:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("build_ref", os.path.join(_HERE, "ref", "build_ref.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        if mod.available():
+            mod.build()
+    except Exception:
+        return False
+    return os.path.exists(lib_path(variant))
+
+
+def load(variant):
+    if variant in _LIBS:
+        return _LIBS[variant]
+    lib = ctypes.CDLL(lib_path(variant))
+    sig = {
+        "ref_float_bytes": (ctypes.c_int, []),
+        "ref_create": (_P, [ctypes.POINTER(O.Params), ctypes.c_int, _D, _D, ctypes.c_int]),
+        "ref_destroy": (None, [_P]),
+        "ref_scalars": (None, [_P, _D]),
+        "ref_grid_info": (None, [_P, _I32, _D]),
+        "ref_update_grid_distribution": (None, [_P]),
+        "ref_reset_higher_level": (None, [_P]),
+        "ref_higher_level": (ctypes.c_int, [_P]),
+        "ref_compute_particle_interaction": (None, [_P]),
+        "ref_compute_density": (None, [_P, ctypes.c_int]),
+        "ref_compute_non_pressure_force": (None, [_P]),
+        "ref_compute_delta": (ctypes.c_double, [_P, ctypes.c_double]),
+        "ref_pressure_force_and_integrate": (None, [_P, ctypes.c_double, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_int]),
+        "ref_predict_velocity_and_position": (None, [_P, ctypes.c_double, ctypes.c_int]),
+        "ref_predict_pressure": (None, [_P, ctypes.c_double]),
+        "ref_predict_pressure_force": (None, [_P]),
+        "ref_accumulate_and_integrate": (None, [_P, ctypes.c_double]),
+        "ref_pseudo_viscosity": (None, [_P, ctypes.c_double]),
+        "ref_time_integration": (None, [_P, ctypes.c_double]),
+        "ref_sph_pressure_force": (None, [_P, ctypes.c_double]),
+        "ref_number_of_time_steps": (ctypes.c_uint, [_P, ctypes.c_double, ctypes.c_double]),
+        "ref_advance_time_step": (None, [_P, ctypes.c_double]),
+        "ref_advance": (None, [_P, ctypes.c_double]),
+        "ref_get_field": (None, [_P, ctypes.c_int, _D]),
+        "ref_set_field": (None, [_P, ctypes.c_int, _D]),
+        "ref_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
+        "ref_get_buckets": (None, [_P, _I32, _I32]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIBS[variant] = lib
+    return lib
+
+
+class RefSim:
+    """One scene built and stepped by the reference's own classes (single thread)."""
+
+    def __init__(self, scene, pos, vel=None, variant="f32", kind=None):
+        self.lib = load(variant)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self.n = len(pos)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        if kind is None:
+            kind = 1 if scene.get("solver", "pcisph") == "sph" else 0
+        self._params = O.make_params(scene)
+        self.h = self.lib.ref_create(ctypes.byref(self._params), self.n,
+                                     pos.ctypes.data_as(_D), v.ctypes.data_as(_D) if v is not None else None,
+                                     kind)
+
+    def __getattr__(self, name):
+        fn = getattr(self.lib, "ref_" + name)
+        return lambda *a: fn(self.h, *a)
+
+    def get(self, field):
+        out = np.zeros((self.n, 3) if field in O.VECTOR_FIELDS else self.n)
+        self.lib.ref_get_field(self.h, field, out.ctypes.data_as(_D))
+        return out
+
+    def set(self, field, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self.lib.ref_set_field(self.h, field, a.ctypes.data_as(_D))
+
+    def scalars_dict(self):
+        out = np.zeros(8)
+        self.lib.ref_scalars(self.h, out.ctypes.data_as(_D))
+        keys = ["mass", "kernel_radius", "delta_denom", "mass_over_density_sq",
+                "target_spacing", "target_density", "radius", "relative_radius"]
+        return dict(zip(keys, out.tolist()))
+
+    def grid(self):
+        dims = np.zeros(3, np.int32)
+        geo = np.zeros(12)
+        self.lib.ref_grid_info(self.h, dims.ctypes.data_as(_I32), geo.ctypes.data_as(_D))
+        return dims, geo
+
+    def cells(self):
+        dims, _ = self.grid()
+        total = int(np.prod(dims))
+        cell_of = np.zeros(self.n, np.uint32)
+        counts = np.zeros(total, np.uint32)
+        chains = np.zeros(self.n, np.uint32)
+        self.lib.ref_get_cells(self.h, cell_of.ctypes.data_as(_U32), counts.ctypes.data_as(_U32),
+                               chains.ctypes.data_as(_U32))
+        return cell_of, counts, chains
+
+    def buckets(self):
+        counts = np.zeros(self.n, np.int32)
+        ids = np.zeros((self.n, 100), np.int32)
+        self.lib.ref_get_buckets(self.h, counts.ctypes.data_as(_I32), ids.ctypes.data_as(_I32))
+        return counts, ids

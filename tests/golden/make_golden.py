@@ -1,0 +1,105 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs only where the reference checkout exists: oracle/ref/build_ref.py compiles the
+reference's own SPH/PCISPH CPU path host-only, and oracle/refsim.py drives its classes
+(single thread).  For two small seeded scenes and both builds (FP32 = `typedef float
+Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
+
+  pcisph_<v>.npz  1,440-particle PCISPH dam break (box + sphere): setup scalars and grid,
+                  the cell chains after Setup and after 3 as-shipped substeps, bucket
+                  counts, every particle field after those substeps, the fields after a
+                  3-iteration corrector built from the reference's own sub-passes, and
+                  positions after Advance(2e-3) with its CFL substep loop.
+  sph_<v>.npz     800-particle SPH dam break: fields after 3 as-shipped substeps
+                  (ComputePressureForceCPU integrating in place, single thread).
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from bubbles_gb300 import scenes  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from oracle import refsim as R  # noqa: E402
+
+FIELDS = {"pos": O.POSITION, "vel": O.VELOCITY, "force": O.FORCE, "density": O.DENSITY,
+          "pressure": O.PRESSURE, "pred_density": O.PRED_DENSITY,
+          "pressure_force": O.PRESSURE_FORCE, "pred_pos": O.PRED_POSITION}
+
+
+def pcisph_scene():
+    return scenes.small_pcisph(seed=0)
+
+
+def sph_scene():
+    sc = scenes.base_scene("sph", 0.02, (0.6, 0.5, 0.6))
+    sc["dt"] = 1e-4
+    return sc, scenes.dam_block(sc, (10, 8, 10), seed=1)
+
+
+def clean(scene):
+    return json.loads(json.dumps(scene, default=lambda o: list(o) if hasattr(o, "__iter__") else float(o)))
+
+
+def make(variant):
+    out = {}
+    sc, pos = pcisph_scene()
+    r = R.RefSim(sc, pos, variant=variant)
+    out["scene"] = np.array(json.dumps(clean(sc)))
+    out["pos0"] = pos
+    s = r.scalars_dict()
+    out["scalars"] = np.array([s[k] for k in ("mass", "kernel_radius", "delta_denom",
+                                              "mass_over_density_sq")])
+    dims, geo = r.grid()
+    out["grid_dims"], out["grid_geo"] = dims, geo
+    out["setup_cell_of"], out["setup_counts"], out["setup_chains"] = r.cells()
+    for _ in range(3):
+        r.advance_time_step(sc["dt"])
+    out["step3_cell_of"], out["step3_counts"], out["step3_chains"] = r.cells()
+    out["step3_bucket_counts"], _ = r.buckets()
+    for name, f in FIELDS.items():
+        out["step3_" + name] = r.get(f)
+    # 3-iteration corrector from the reference's sub-passes, after a fresh grid update
+    r.update_grid_distribution()
+    r.reset_higher_level()
+    r.compute_particle_interaction()
+    r.compute_density(1)
+    r.compute_non_pressure_force()
+    delta = r.compute_delta(sc["dt"])
+    out["corr_delta"] = np.array(delta)
+    for k in range(3):
+        r.predict_velocity_and_position(sc["dt"], int(k == 0))
+        r.predict_pressure(delta)
+        r.predict_pressure_force()
+    for name in ("pred_density", "pressure", "pressure_force", "pred_pos"):
+        out["corr_" + name] = r.get(FIELDS[name])
+    r.accumulate_and_integrate(sc["dt"])
+    out["corr_pos"] = r.get(O.POSITION)
+    out["corr_vel"] = r.get(O.VELOCITY)
+    r.advance(2e-3)
+    out["advance_pos"] = r.get(O.POSITION)
+    np.savez_compressed(os.path.join(HERE, "pcisph_%s.npz" % variant), **out)
+
+    sc2, pos2 = sph_scene()
+    r2 = R.RefSim(sc2, pos2, variant=variant)
+    o2 = {"scene": np.array(json.dumps(clean(sc2))), "pos0": pos2}
+    for _ in range(3):
+        r2.advance_time_step(sc2["dt"])
+    for name in ("pos", "vel", "force", "density", "pressure"):
+        o2["step3_" + name] = r2.get(FIELDS[name])
+    np.savez_compressed(os.path.join(HERE, "sph_%s.npz" % variant), **o2)
+
+
+if __name__ == "__main__":
+    if not R.available():
+        sys.exit("the reference checkout is not available here; fixtures unchanged")
+    for v in ("f32", "f64"):
+        make(v)
+    print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))

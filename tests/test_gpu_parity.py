@@ -441,3 +441,53 @@ def test_full_size_invariants_1m(gpu):
         g.compute_density(0)
         rho = g.get(bb.FIELD_DENSITY)
         assert 300 < np.median(rho) < 1100
+
+
+def _golden(name):
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name)
+    d = np.load(path, allow_pickle=False)
+    return {k: d[k] for k in d.files}, json.loads(str(d["scene"]))
+
+
+def test_gpu_against_reference_fixtures(gpu):
+    """The CUDA path on the reference's own inputs and outputs (tests/golden, produced by
+    the reference's CPU path built with Float = float; FP64 gives the rounding envelope)."""
+    g32, sc = _golden("pcisph_f32.npz")
+    g64, _ = _golden("pcisph_f64.npz")
+    dt, h0 = sc["dt"], sc["spacing"]
+    shipped = dict(sc, pcisph_mode="as_shipped")
+    with bb.Solver(shipped, pos=g32["pos0"]) as g:
+        g.update_grid_distribution()
+        cell, counts, ids = g.dump_grid()
+        assert np.array_equal(cell, g32["setup_cell_of"])
+        assert np.array_equal(counts, g32["setup_counts"])
+        assert np.array_equal(ids, g32["setup_chains"])
+        for _ in range(3):
+            g.advance_time_step(dt)
+        p, v = g.download()
+        assert np.max(np.abs(p - g32["step3_pos"])) <= RTOL * h0
+        assert np.max(np.abs(v - g32["step3_vel"])) <= RTOL * max(1.0, np.abs(g32["step3_vel"]).max())
+        ok, worst = rel_close(g.get(bb.FIELD_DENSITY), g32["step3_density"])
+        assert ok, worst
+    # corrector from the reference's state after those substeps
+    with bb.Solver(sc, pos=g32["step3_pos"], vel=g32["step3_vel"]) as g:
+        g.update_grid_distribution()
+        g.compute_density(1)
+        g.compute_non_pressure_force()
+        delta = g.compute_delta(dt)
+        assert delta == float(g32["corr_delta"])
+        for k in range(3):
+            g.predict_velocity_and_position(dt, int(k == 0))
+            g.predict_pressure(delta)
+            g.predict_pressure_force()
+        ok, worst = rel_close(g.get(bb.FIELD_PRED_DENSITY), g32["corr_pred_density"])
+        assert ok, worst
+        assert np.max(np.abs(g.get(bb.FIELD_PRESSURE) - g32["corr_pressure"])) <= RTOL * 3 * abs(delta) * 1000.0
+        env = np.linalg.norm(g32["corr_pressure_force"] - g64["corr_pressure_force"], axis=1).max()
+        dfp = np.linalg.norm(g.get(bb.FIELD_PRESSURE_FORCE) - g32["corr_pressure_force"], axis=1)
+        assert np.all(dfp <= 2.0 * env + RTOL * np.linalg.norm(g32["corr_pressure_force"], axis=1))
+        g.accumulate_and_integrate(dt)
+        p, v = g.download()
+        assert np.max(np.abs(p - g32["corr_pos"])) <= RTOL * h0
