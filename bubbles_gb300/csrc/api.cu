@@ -240,8 +240,11 @@ void add_substep_stats(bbg_solver s, float dt) {
     a.max_force = f;
 }
 
-// Corrector loop of ComputePressureForceAndIntegrate: max_it x (predicted density,
-// pressure force); the kernels decide on device when to stop and integrate.
+// Corrector loop of ComputePressureForceAndIntegrate launched from the host: after each
+// iteration the host reads that iteration's max density error, as the reference's loop
+// does (pcisph_equations3.cpp:238-246), and stops once it is below tolerance.  The
+// kernels take the same decision on the device.  (Substeps normally run as CUDA graphs
+// whose conditional WHILE node keeps this loop on the device.)
 bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
     if (max_it < 1) max_it = 1;
     if (max_it > kMaxIterations) max_it = kMaxIterations;
@@ -251,8 +254,14 @@ bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
     for (int k = 0; k < max_it; k++) {
         launch_pred_density(s->P, s->B, s->state, k, delta, s->stream);
         launch_pressure_force(s->P, s->B, s->state, k, max_it, dt, dt_over_m, s->stream);
+        CK_LAUNCH();
+        if (k == max_it - 1) break;
+        CK(cudaMemcpyAsync(s->h_u, &s->B.st->err_bits[k], 4, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        float e;
+        memcpy(&e, s->h_u, 4);
+        if (e / s->P.target_density < s->P.max_err_ratio) break;
     }
-    CK_LAUNCH();
     s->state = 1 - s->state;
     s->valid |= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE) |
                 bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_PRED_DENSITY) |
@@ -688,10 +697,10 @@ bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count) {
 static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d_vel, int n) {
     launch_upload(s->B, s->state, s->pid_cur, d_pos, d_vel, n, s->stream);
     CK_LAUNCH();
+    if (n != s->n) s->epoch++;   // captured launches depend on n, not on the data
     s->n = n;
     s->P.n = n;
     s->grid_valid = false;
-    s->epoch++;
     s->valid = kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) |
                bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
     return BBG_OK;
