@@ -191,61 +191,34 @@ __device__ __forceinline__ void for_each_candidate(const GridDev &g, const unsig
     }
 }
 
-// Neighbour sets recorded by the density pass: for each of the 9 candidate ranges
-// (r = 3 * (dz + 1) + (dy + 1)) a 32-bit mask of the member slots, stored range-major
-// (masks[r * n + i]).  A particle whose range is longer than 32 slots has kWide set in
-// its cell word and is re-tested exactly on every pass instead.
+// Neighbour sets recorded by the density pass: the slots of each particle's bucket
+// members other than itself, member-major (list[q * n + i], q < kMaxList) so a warp reads
+// entry q of 32 particles in one coalesced load.  A particle with more than kMaxList
+// members has kWide set in its cell word and is re-tested exactly on every pass instead.
 constexpr unsigned kWide = 0x80000000u;
-constexpr int kRows = 9;
+constexpr int kMaxList = 64;
 
+// f(j) for every member j != i of particle i's step-start neighbour set.
 template <class F>
-__device__ __forceinline__ void for_each_neighbor(const Params &P, const unsigned *__restrict__ start,
-                                                  const unsigned *__restrict__ masks,
-                                                  const float4 *__restrict__ pos, unsigned cellw,
-                                                  int i, F &&f) {
-    const GridDev &g = P.g;
-    const unsigned c = cellw & ~kWide;
+__device__ __forceinline__ void for_each_member(const Params &P, const unsigned *__restrict__ start,
+                                                const unsigned *__restrict__ list,
+                                                const int *__restrict__ nbr,
+                                                const float4 *__restrict__ pos, unsigned cellw,
+                                                int i, F &&f) {
     if (cellw & kWide) {
         const float4 pi = pos[i];
-        for_each_candidate(g, start, c, [&](unsigned j) {
+        for_each_candidate(P.g, start, cellw & ~kWide, [&](unsigned j) {
+            if (j == (unsigned)i) return;
             const float4 pj = __ldg(&pos[j]);
             if (std_member(P, pi, pj, dist2(pi, pj))) f(j);
         });
         return;
     }
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const unsigned plane = (unsigned)nx * (unsigned)ny;
-    const int cz = (int)(c / plane);
-    const unsigned rem = c - (unsigned)cz * plane;
-    const int cy = (int)(rem / (unsigned)nx);
-    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
-    const int x0 = cx > 0 ? cx - 1 : 0;
+    const int cnt = __ldg(&nbr[i]) - 1;   // members other than i
     const unsigned n = (unsigned)P.n;
-    // Load the 9 (mask, range start) pairs, then walk all members as one flat sequence so
-    // a warp runs max-over-lanes of the total member count rather than per range.
-    unsigned m[kRows], b[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-        const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-        m[r] = 0u;
-        b[r] = 0u;
-        if (z >= 0 && z < nz && y >= 0 && y < ny) {
-            m[r] = __ldg(&masks[(unsigned)r * n + (unsigned)i]);
-            if (m[r]) b[r] = __ldg(&start[(unsigned)y * (unsigned)nx + (unsigned)z * plane + (unsigned)x0]);
-        }
-    }
-    int left = kRows;
-    for (;;) {
-        while (m[0] == 0u) {
-            if (--left == 0) return;
-#pragma unroll
-            for (int r = 0; r < kRows - 1; ++r) { m[r] = m[r + 1]; b[r] = b[r + 1]; }
-            m[kRows - 1] = 0u;
-        }
-        const int bit = __ffs(m[0]) - 1;
-        m[0] &= m[0] - 1u;
-        f(b[0] + (unsigned)bit);
-    }
+    const unsigned *l = list + i;
+#pragma unroll 4
+    for (int q = 0; q < cnt; ++q) f(__ldg(&l[(unsigned)q * n]));
 }
 
 // ----------------------------------------------------------------------------

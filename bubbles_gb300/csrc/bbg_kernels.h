@@ -21,7 +21,7 @@ struct DevBufs {
     unsigned *partials;        // scan partials
     uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
     int *nbr;                  // neighbour count of each sorted slot
-    unsigned *masks;           // 9 neighbour masks per slot (range-major)
+    unsigned *list;            // kMaxList member slots per particle (member-major)
     float *inv_rho;            // 1 / density
     StepState *st;
     float *stage;              // n * 3 floats of staging for host copies

@@ -37,56 +37,33 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
 
 // ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
 // Tests every candidate of the 27 cells exactly once per substep and records the
-// neighbour set (the reference bucket, grid.h:423-447) as 9 range masks.
+// neighbour set (the reference bucket, grid.h:423-447) as a member list.
 __global__ void __launch_bounds__(kThreads)
 k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
-          float *__restrict__ press, int *__restrict__ nbr, unsigned *__restrict__ masks,
+          float *__restrict__ press, int *__restrict__ nbr, unsigned *__restrict__ list,
           int compute_pressure, StepState *st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
-    const unsigned c = cw & ~kWide;
-    const GridDev &g = P.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const unsigned plane = (unsigned)nx * (unsigned)ny;
-    const int cz = (int)(c / plane);
-    const unsigned rem = c - (unsigned)cz * plane;
-    const int cy = (int)(rem / (unsigned)nx);
-    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
-    const int x0 = cx > 0 ? cx - 1 : 0;
-    const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
     const unsigned n = (unsigned)P.n;
     float sum = 0.f;
-    int cnt = 0;
-    bool wide = false;
-#pragma unroll 1
-    for (int dz = -1; dz <= 1; ++dz) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int z = cz + dz, y = cy + dy;
-            const int r = 3 * (dz + 1) + (dy + 1);
-            unsigned m = 0;
-            if (z >= 0 && z < nz && y >= 0 && y < ny) {
-                const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
-                const unsigned b = __ldg(&start[row + (unsigned)x0]);
-                const unsigned e = __ldg(&start[row + (unsigned)x1 + 1u]);
-                if (e - b > 32u) wide = true;
-                for (unsigned j = b; j < e; ++j) {
-                    const float4 pj = __ldg(&pos[j]);
-                    const float r2 = dist2(pi, pj);
-                    if (std_member(P, pi, pj, r2)) {
-                        const float x = 1.f - r2 * P.inv_h2;
-                        sum += x * x * x;
-                        cnt++;
-                        if (j - b < 32u) m |= 1u << (j - b);
-                    }
-                }
+    int cnt = 0;      // bucket members, i included
+    int listed = 0;   // members other than i written to the list
+    for_each_candidate(P.g, start, cw & ~kWide, [&](unsigned j) {
+        const float4 pj = __ldg(&pos[j]);
+        const float r2 = dist2(pi, pj);
+        if (std_member(P, pi, pj, r2)) {
+            const float x = 1.f - r2 * P.inv_h2;
+            sum += x * x * x;
+            cnt++;
+            if (j != (unsigned)i) {
+                if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
+                listed++;
             }
-            masks[(unsigned)r * n + (unsigned)i] = m;
         }
-    }
+    });
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
@@ -99,7 +76,7 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     inv_rho[i] = ir;
     reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
     nbr[i] = cnt;
-    if (wide) cell[i] = cw | kWide;
+    if (listed > kMaxList) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
@@ -108,7 +85,7 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
 __global__ void __launch_bounds__(kThreads)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
-               const unsigned *__restrict__ start, const unsigned *__restrict__ masks,
+               const unsigned *__restrict__ start, const unsigned *__restrict__ list, const int *__restrict__ nbr,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
                float *__restrict__ press, int predict, float dt, float dt_over_m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,8 +96,7 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     float fy = P.mass * P.gy - P.drag * vi.y;
     float fz = P.mass * P.gz - P.drag * vi.z;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
-    for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
-        if (j == (unsigned)i) return;   // (v_i - v_i) contributes nothing
+    for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
         const float d = r2 * rsqrtf(r2);
@@ -177,7 +153,7 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
 __global__ void __launch_bounds__(kThreads)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned *__restrict__ masks, float *__restrict__ press,
+               const unsigned *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
                float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
                float delta) {
     // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
@@ -188,8 +164,8 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     float aerr = 0.f;
     if (i < P.n) {
         const float4 xi = xstar[i];
-        float sum = 0.f;
-        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
+        float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
+        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 xj = __ldg(&xstar[j]);
             const float r2 = dist2(xi, xj);
             if (r2 < P.h2mz) {
@@ -233,7 +209,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
 __global__ void __launch_bounds__(kThreads)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const unsigned *__restrict__ masks, float4 *__restrict__ force,
+                 const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
@@ -249,8 +225,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
         const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
-        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
-            if (j == (unsigned)i) return;
+        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 pj = __ldg(&pos[j]);   // pj.w = p_j / rho*_j^2
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
@@ -306,7 +281,7 @@ __global__ void k_corrector_control(Params P, StepState *st, int max_it,
 __global__ void __launch_bounds__(kThreads)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-             const unsigned *__restrict__ masks, float4 *__restrict__ force,
+             const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
@@ -320,8 +295,7 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
         const float kv = P.visc_m2 * P.spiky_d2w_c;
-        for_each_neighbor(P, start, masks, pos, cell[i], i, [&](unsigned j) {
-            if (j == (unsigned)i) return;
+        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 pj = __ldg(&pos[j]);
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
@@ -388,12 +362,15 @@ __global__ void __launch_bounds__(kThreads)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
                const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned *__restrict__ masks, float4 *__restrict__ smoothed) {
+               const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
-    float sx = 0.f, sy = 0.f, sz = 0.f, ws = 0.f;
-    for_each_neighbor(P, start, masks, pos_old, cell[i], i, [&](unsigned j) {
+    // the particle itself (distance 0): W_spiky(0) m / rho_i
+    const float w0 = P.mass * __ldg(&inv_rho[i]) * P.spiky_w_c;
+    const float4 v0 = vel[i];
+    float ws = w0, sx = w0 * v0.x, sy = w0 * v0.y, sz = w0 * v0.z;
+    for_each_member(P, start, list, nbr, pos_old, cell[i], i, [&](unsigned j) {
         const float4 pj = __ldg(&pos[j]);
         const float d = sqrtf(dist2(pi, pj));
         if (d - P.h <= -P.iz) {
@@ -427,7 +404,7 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
     k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell,
                                                              B.start, B.rho, B.inv_rho, B.press,
-                                                             B.nbr, B.masks, compute_pressure, B.st);
+                                                             B.nbr, B.list, compute_pressure, B.st);
     BBG_PEND(B, s);
 }
 
@@ -435,7 +412,7 @@ void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict
                          float dt_over_m, cudaStream_t s) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
     k_non_pressure<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.xstar, B.pforce, B.press,
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
         predict, dt, dt_over_m);
     BBG_PEND(B, s);
 }
@@ -453,7 +430,7 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
                          cudaStream_t s) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
     k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.xstar, B.cell, B.start, B.masks, B.press, B.rhostar, B.derr, B.st, k,
+        P, B.pos[buf], B.xstar, B.cell, B.start, B.list, B.nbr, B.press, B.rhostar, B.derr, B.st, k,
         delta);
     BBG_PEND(B, s);
 }
@@ -466,7 +443,7 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
                            float dt_over_m, cudaStream_t s, int force_only) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pforce, B.xstar,
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,
         B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, force_only);
     BBG_PEND(B, s);
 }
@@ -479,7 +456,7 @@ void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
     BBG_PBEGIN(B, KID_SPH_FORCES, s, -1);
     k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.masks, B.force, B.pos[1 - buf],
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pos[1 - buf],
         B.vel[1 - buf], B.st, dt);
     BBG_PEND(B, s);
 }
@@ -503,7 +480,7 @@ void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, flo
                              cudaStream_t s) {
     BBG_PBEGIN(B, KID_PSEUDO_VISCOSITY, s, -1);
     k_pv_aggregate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.inv_rho, B.cell, B.start, B.masks,
+        P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.inv_rho, B.cell, B.start, B.list, B.nbr,
         B.smoothed);
     k_pv_interpolate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.vel[new_buf], B.smoothed,
                                                                     factor);
