@@ -356,7 +356,7 @@ def run_ours(args, scene, pos):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene["workload"], "variant": "plain", "solver": "pcisph",
+        "config": {"workload": scene["workload"], "variant": args.variant, "solver": "pcisph",
                    "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
                    "max_iterations": scene["max_iterations"],
                    "corrector_iterations_mean": float(np.mean(iters)),
@@ -386,12 +386,16 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", default="plain", choices=["plain", "warm"],
+                    help="corrector start: plain = zero pressure (reference), warm = the "
+                         "previous substep's pressure")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     from bubbles_gb300 import scenes
     rank, _, _ = dist_env()
     scene, pos = scenes.config(args.config, seed=args.seed + rank)
+    scene["pressure_init"] = {"plain": "zero", "warm": "previous"}[args.variant]
     if args.impl == "reference":
         run_reference(args, scene, pos)
     else:

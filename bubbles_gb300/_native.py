@@ -14,6 +14,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device mem
 
 SOLVER_PCISPH, SOLVER_SPH = 0, 1
 PCISPH_AS_SHIPPED, PCISPH_TOLERANCE = 0, 1
+PRESSURE_INIT_ZERO, PRESSURE_INIT_PREVIOUS, PRESSURE_INIT_LEARNED = 0, 1, 2
 SHAPE_BOX, SHAPE_SPHERE = 1, 2
 MAX_COLLIDERS = 16
 
@@ -44,7 +45,8 @@ class SolverDesc(ctypes.Structure):
                 ("pcisph_mode", ctypes.c_int),
                 ("max_iterations", ctypes.c_int),
                 ("max_density_error_ratio", ctypes.c_double),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int),
+                ("pressure_init", ctypes.c_int)]
 
 
 class Shape(ctypes.Structure):

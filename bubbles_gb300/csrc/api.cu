@@ -158,7 +158,7 @@ bbg_status free_all(bbg_solver s) {
     void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
                     B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
                     B.cell_old, B.sub, B.count, B.start, B.partials, B.tmp, B.nbr, B.st, B.stage,
-                    B.red, B.list, B.inv_rho};
+                    B.red, B.list, B.inv_rho, B.pprev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     Prof *keep = B.prof;
@@ -303,7 +303,12 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
         launch_sph_forces(P, B, work, dt, cs);
     } else {
         launch_density(P, B, work, 0, cs);
-        launch_non_pressure(P, B, work, 1, dt, dt / s->mass, cs);
+        const bool warm = s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO;
+        launch_non_pressure(P, B, work, warm ? 0 : 1, dt, dt / s->mass, cs);
+        if (warm) {
+            launch_warm_start(P, B, work, cs);
+            launch_pressure_force(P, B, work, 0, max_it, dt, dt / s->mass, cs, 2);
+        }
         cudaStreamCaptureStatus status;
         cudaGraph_t cg = nullptr;
         const cudaGraphNode_t *deps = nullptr;
@@ -416,7 +421,12 @@ bbg_status substep(bbg_solver s, float dt) {
         return pseudo_viscosity(s, dt);
     }
     launch_density(s->P, s->B, s->state, 0, s->stream);
-    launch_non_pressure(s->P, s->B, s->state, 1, dt, dt / s->mass, s->stream);
+    const bool warm = s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO;
+    launch_non_pressure(s->P, s->B, s->state, warm ? 0 : 1, dt, dt / s->mass, s->stream);
+    if (warm) {
+        launch_warm_start(s->P, s->B, s->state, s->stream);
+        launch_pressure_force(s->P, s->B, s->state, 0, max_it, dt, dt / s->mass, s->stream, 2);
+    }
     CK_LAUNCH();
     s->valid |= bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE);
     r = corrector(s, dt, delta, max_it);
@@ -622,7 +632,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.force, n); ALLOC(B.xstar, n); ALLOC(B.pforce, n); ALLOC(B.smoothed, n);
     ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
     ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
-    ALLOC(B.list, (size_t)kMaxList * n); ALLOC(B.inv_rho, n);
+    ALLOC(B.list, (size_t)kMaxList * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
     ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);

@@ -23,6 +23,7 @@ struct DevBufs {
     int *nbr;                  // neighbour count of each sorted slot
     unsigned *list;            // kMaxList member slots per particle (member-major)
     float *inv_rho;            // 1 / density
+    float *pprev;              // pressure of the previous substep, in the current order
     StepState *st;
     float *stage;              // n * 3 floats of staging for host copies
     unsigned *red;             // reduction scratch (max |F|)
@@ -66,8 +67,11 @@ void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_fir
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
                          cudaStream_t s);
+// mode 0: pressure force, then the next prediction or (converged) integration;
+// 1: pressure force only; 2: pressure force and prediction, never integration.
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,
-                           float dt, float dt_over_m, cudaStream_t s, int force_only = 0);
+                           float dt, float dt_over_m, cudaStream_t s, int mode = 0);
+void launch_warm_start(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
 void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
                               cudaGraphConditionalHandle handle, cudaStream_t s);
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);

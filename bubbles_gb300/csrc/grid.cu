@@ -140,7 +140,8 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
               const unsigned *__restrict__ start, const float4 *__restrict__ pos_in,
               const float4 *__restrict__ vel_in, float4 *__restrict__ pos_out,
               float4 *__restrict__ vel_out, int *__restrict__ pid_out, int *__restrict__ slot,
-              unsigned *__restrict__ cell) {
+              unsigned *__restrict__ cell, const float *__restrict__ press_in,
+              float *__restrict__ pprev) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const uint2 e = tmp[t];
@@ -154,6 +155,7 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
     pid_out[dst] = (int)e.x;
     slot[e.x] = (int)dst;
     cell[dst] = c;
+    pprev[dst] = press_in[e.y];   // carried for a warm-started corrector
 }
 
 size_t scan_partials_needed(unsigned cells) { return (size_t)blocks_for(cells, kScanTile) + 1; }
@@ -187,7 +189,7 @@ void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src,
     BBG_PBEGIN(B, KID_RANK_GATHER, s, -1);
     k_rank_gather<<<blocks_for(n, kThreads), kThreads, 0, s>>>(
         n, B.tmp, B.cell_old, B.start, B.pos[src], B.vel[src], B.pos[1 - src], B.vel[1 - src],
-        B.pid[1 - pid_src], B.slot, B.cell);
+        B.pid[1 - pid_src], B.slot, B.cell, B.press, B.pprev);
     BBG_PEND(B, s);
 }
 

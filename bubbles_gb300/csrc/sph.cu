@@ -48,22 +48,62 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
     const unsigned n = (unsigned)P.n;
+    const GridDev &g = P.g;
+    const unsigned c = cw & ~kWide;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
+    const int cz = (int)(c / plane);
+    const unsigned rem = c - (unsigned)cz * plane;
+    const int cy = (int)(rem / (unsigned)nx);
+    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
+    // Distances from the particle to the faces of its cell.  A neighbour cell whose
+    // nearest point is farther than h holds no member, so it is skipped.  The margin
+    // covers FP32 rounding and the 1e-4 boundary shift of the hash; a particle found
+    // outside its cell by more than that (clamped out-of-grid input) is not pruned.
+    const float margin = 2e-4f;
+    const float lx = (pi.x - g.minp[0]) - (float)cx * g.len[0];
+    const float ly = (pi.y - g.minp[1]) - (float)cy * g.len[1];
+    const float lz = (pi.z - g.minp[2]) - (float)cz * g.len[2];
+    const bool inside_cell = lx > -margin && lx < g.len[0] + margin && ly > -margin &&
+                             ly < g.len[1] + margin && lz > -margin && lz < g.len[2] + margin;
+    const float reach = inside_cell ? P.h2 * 1.0001f : 3.4e38f;
+    const float gx0 = fmaxf(lx - margin, 0.f), gx1 = fmaxf(g.len[0] - lx - margin, 0.f);
+    const float gy0 = fmaxf(ly - margin, 0.f), gy1 = fmaxf(g.len[1] - ly - margin, 0.f);
+    const float gz0 = fmaxf(lz - margin, 0.f), gz1 = fmaxf(g.len[2] - lz - margin, 0.f);
     float sum = 0.f;
     int cnt = 0;      // bucket members, i included
     int listed = 0;   // members other than i written to the list
-    for_each_candidate(P.g, start, cw & ~kWide, [&](unsigned j) {
-        const float4 pj = __ldg(&pos[j]);
-        const float r2 = dist2(pi, pj);
-        if (std_member(P, pi, pj, r2)) {
-            const float x = 1.f - r2 * P.inv_h2;
-            sum += x * x * x;
-            cnt++;
-            if (j != (unsigned)i) {
-                if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
-                listed++;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z >= nz) continue;
+        const float gz = dz < 0 ? gz0 : (dz > 0 ? gz1 : 0.f);
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = cy + dy;
+            if (y < 0 || y >= ny) continue;
+            const float gy = dy < 0 ? gy0 : (dy > 0 ? gy1 : 0.f);
+            const float base = gy * gy + gz * gz;
+            if (base > reach) continue;
+            const int xa = (cx > 0 && gx0 * gx0 + base <= reach) ? cx - 1 : cx;
+            const int xb = (cx + 1 < nx && gx1 * gx1 + base <= reach) ? cx + 1 : cx;
+            const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
+            const unsigned b = __ldg(&start[row + (unsigned)xa]);
+            const unsigned e = __ldg(&start[row + (unsigned)xb + 1u]);
+#pragma unroll 2
+            for (unsigned j = b; j < e; ++j) {
+                const float4 pj = __ldg(&pos[j]);
+                const float r2 = dist2(pi, pj);
+                if (std_member(P, pi, pj, r2)) {
+                    const float x = 1.f - r2 * P.inv_h2;
+                    sum += x * x * x;
+                    cnt++;
+                    if (j != (unsigned)i) {
+                        if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
+                        listed++;
+                    }
+                }
             }
         }
-    });
+    }
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
@@ -135,6 +175,21 @@ k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restri
     v3 xs;
     predict_particle(P, dt, dt_over_m, V(force[i]), V(pforce[i]), V(pos[i]), V(vel[i]), &xs);
     xstar[i] = F4(xs);
+}
+
+// Warm start of the corrector: p = the previous substep's pressure, rho* = rho, and
+// pos.w = p / rho^2 for the pressure-force pass that predicts x* from F + Fp(p).
+__global__ void k_warm_start(int n, float4 *pos, const float *__restrict__ rho,
+                             const float *__restrict__ pinit, float *__restrict__ press,
+                             float *__restrict__ rhostar, float *__restrict__ derr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = rho[i];
+    const float p = pinit[i];
+    press[i] = p;
+    rhostar[i] = d;
+    derr[i] = 0.f;
+    reinterpret_cast<float *>(&pos[i])[3] = p / (d * d);
 }
 
 // pos.w = p / rho*^2 from the pressure and predicted-density fields (used when those
@@ -213,10 +268,10 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
-                 float dt_over_m, int force_only) {
+                 float dt_over_m, int mode) {
     if (k < 0) k = st->iter;
     else if (converged_before(P, st, k)) return;
-    const bool last = !force_only && ((k == max_it - 1) ||
+    const bool last = mode == 0 && ((k == max_it - 1) ||
                       fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
@@ -250,7 +305,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
             pos_out[i] = F4(x);
             vel_out[i] = F4(v);
             fbits = __float_as_uint(vlen(ft));
-        } else if (!force_only) {
+        } else if (mode != 1) {
             v3 xs;
             predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
             xstar[i] = F4(xs);
@@ -435,16 +490,21 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
     BBG_PEND(B, s);
 }
 
+void launch_warm_start(const Params &P, const DevBufs &B, int buf, cudaStream_t s) {
+    k_warm_start<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.rho, B.pprev,
+                                                                B.press, B.rhostar, B.derr);
+}
+
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s) {
     k_pack_acoef<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.press, B.rhostar);
 }
 
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it, float dt,
-                           float dt_over_m, cudaStream_t s, int force_only) {
+                           float dt_over_m, cudaStream_t s, int mode) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
         P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,
-        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, force_only);
+        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, mode);
     BBG_PEND(B, s);
 }
 

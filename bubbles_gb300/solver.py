@@ -39,6 +39,7 @@ def desc_from_scene(scene, device=0):
     d.pcisph_mode = N.PCISPH_TOLERANCE if mode == "tolerance" else N.PCISPH_AS_SHIPPED
     d.max_iterations = int(scene.get("max_iterations", 20 if mode == "tolerance" else 5))
     d.device = int(device)
+    d.pressure_init = {"zero": 0, "previous": 1, "learned": 2}[scene.get("pressure_init", "zero")]
     return d
 
 

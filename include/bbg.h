@@ -49,6 +49,15 @@ typedef int bbg_status;
 #define BBG_PCISPH_AS_SHIPPED 0
 #define BBG_PCISPH_TOLERANCE 1
 
+/* Initial pressure of the corrector.  ZERO is the reference (p = 0, Fp = 0 at k = 0,
+ * pcisph_equations3.cpp:13-19).  PREVIOUS starts from each particle's converged pressure
+ * of the previous substep, and LEARNED from the per-particle MLP estimate; both then run
+ * one pressure-force pass to predict positions and continue with the unchanged corrector
+ * to the same tolerance, so only the number of iterations changes. */
+#define BBG_PRESSURE_INIT_ZERO 0
+#define BBG_PRESSURE_INIT_PREVIOUS 1
+#define BBG_PRESSURE_INIT_LEARNED 2
+
 #define BBG_SHAPE_BOX 1
 #define BBG_SHAPE_SPHERE 2
 #define BBG_MAX_COLLIDERS 16
@@ -92,6 +101,7 @@ typedef struct {
     int max_iterations;              /* corrector cap (reference call site: 5) */
     double max_density_error_ratio;  /* corrector tolerance (reference: 0.01) */
     int device;                      /* CUDA device ordinal */
+    int pressure_init;               /* BBG_PRESSURE_INIT_* (reference: ZERO) */
 } bbg_solver_desc;
 
 /* Analytic collider shape with a translation-only ObjectToWorld (MakeBox,

@@ -23,6 +23,7 @@ VECTOR_FIELDS = {POSITION, VELOCITY, FORCE, INTERACTION, PRED_POSITION, PRED_VEL
 
 PCISPH_AS_SHIPPED = 0
 PCISPH_TOLERANCE = 1
+PCISPH_WARM = 2
 BUCKET = 100
 
 

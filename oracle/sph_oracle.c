@@ -1065,9 +1065,15 @@ int orc_pressure_force_and_integrate(orc_sim *s, double dt_in, double max_err_ra
     Float targetDensity = s->targetDensity;
     Float densityErrorRatio = 0;
     int it = 0;
-    s->tol_mode = (mode == ORC_PCISPH_TOLERANCE);
+    s->tol_mode = (mode != ORC_PCISPH_AS_SHIPPED);
+    if (mode == ORC_PCISPH_WARM) {
+        /* warm start: keep each particle's pressure from the previous substep, rho* = rho,
+         * and predict the first positions from F + Fp(p) instead of F alone */
+        for (int i = 0; i < s->n; i++) { s->dpred[i] = s->density[i]; s->derr[i] = 0; }
+        parallel_for(s->n, k_pred_force, s);
+    }
     for (int k = 0; k < max_it; k++) {
-        pass_ctx pp = {s, k == 0, dt};
+        pass_ctx pp = {s, k == 0 && mode != ORC_PCISPH_WARM, dt};
         parallel_for(s->n, k_predict, &pp);
         pass_ctx pr = {s, 0, delta};
         parallel_for(s->n, k_pred_pressure, &pr);

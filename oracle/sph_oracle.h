@@ -84,7 +84,8 @@ enum {
 };
 
 /* PCISPH corrector modes */
-enum { ORC_PCISPH_AS_SHIPPED = 0, ORC_PCISPH_TOLERANCE = 1 };
+/* WARM: tolerance mode started from the pressure left by the previous substep. */
+enum { ORC_PCISPH_AS_SHIPPED = 0, ORC_PCISPH_TOLERANCE = 1, ORC_PCISPH_WARM = 2 };
 
 int      orc_float_bytes(void);
 void     orc_set_threads(int n);
