@@ -252,7 +252,8 @@ bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
     s->last_max_it = max_it;
     s->last_tol = s->P.max_err_ratio;
     for (int k = 0; k < max_it; k++) {
-        launch_pred_density(s->P, s->B, s->state, k, delta, s->stream);
+        launch_pred_density(s->P, s->B, s->state, k, delta, s->stream,
+                            s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO);
         launch_pressure_force(s->P, s->B, s->state, k, max_it, dt, dt_over_m, s->stream);
         CK_LAUNCH();
         if (k == max_it - 1) break;
@@ -328,7 +329,8 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
             e = cudaStreamBeginCaptureToGraph(s->aux, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                launch_pred_density(P, B, work, -1, delta, s->aux);
+                launch_pred_density(P, B, work, -1, delta, s->aux,
+                                    s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO);
                 launch_pressure_force(P, B, work, -1, max_it, dt, dt / s->mass, s->aux);
                 launch_corrector_control(P, B, max_it, handle, s->aux);
                 cudaError_t e2 = cudaStreamEndCapture(s->aux, &body);

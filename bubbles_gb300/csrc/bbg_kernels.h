@@ -65,8 +65,9 @@ void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict
 void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_first, float dt,
                           float dt_over_m, cudaStream_t s);
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
+// clamp_total: warm-started corrector (the total pressure, not the increment, is clamped)
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
-                         cudaStream_t s);
+                         cudaStream_t s, int clamp_total = 0);
 // mode 0: pressure force, then the next prediction or (converged) integration;
 // 1: pressure force only; 2: pressure force and prediction, never integration.
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,

@@ -48,62 +48,22 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
     const unsigned n = (unsigned)P.n;
-    const GridDev &g = P.g;
-    const unsigned c = cw & ~kWide;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const unsigned plane = (unsigned)nx * (unsigned)ny;
-    const int cz = (int)(c / plane);
-    const unsigned rem = c - (unsigned)cz * plane;
-    const int cy = (int)(rem / (unsigned)nx);
-    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
-    // Distances from the particle to the faces of its cell.  A neighbour cell whose
-    // nearest point is farther than h holds no member, so it is skipped.  The margin
-    // covers FP32 rounding and the 1e-4 boundary shift of the hash; a particle found
-    // outside its cell by more than that (clamped out-of-grid input) is not pruned.
-    const float margin = 2e-4f;
-    const float lx = (pi.x - g.minp[0]) - (float)cx * g.len[0];
-    const float ly = (pi.y - g.minp[1]) - (float)cy * g.len[1];
-    const float lz = (pi.z - g.minp[2]) - (float)cz * g.len[2];
-    const bool inside_cell = lx > -margin && lx < g.len[0] + margin && ly > -margin &&
-                             ly < g.len[1] + margin && lz > -margin && lz < g.len[2] + margin;
-    const float reach = inside_cell ? P.h2 * 1.0001f : 3.4e38f;
-    const float gx0 = fmaxf(lx - margin, 0.f), gx1 = fmaxf(g.len[0] - lx - margin, 0.f);
-    const float gy0 = fmaxf(ly - margin, 0.f), gy1 = fmaxf(g.len[1] - ly - margin, 0.f);
-    const float gz0 = fmaxf(lz - margin, 0.f), gz1 = fmaxf(g.len[2] - lz - margin, 0.f);
     float sum = 0.f;
     int cnt = 0;      // bucket members, i included
     int listed = 0;   // members other than i written to the list
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z >= nz) continue;
-        const float gz = dz < 0 ? gz0 : (dz > 0 ? gz1 : 0.f);
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = cy + dy;
-            if (y < 0 || y >= ny) continue;
-            const float gy = dy < 0 ? gy0 : (dy > 0 ? gy1 : 0.f);
-            const float base = gy * gy + gz * gz;
-            if (base > reach) continue;
-            const int xa = (cx > 0 && gx0 * gx0 + base <= reach) ? cx - 1 : cx;
-            const int xb = (cx + 1 < nx && gx1 * gx1 + base <= reach) ? cx + 1 : cx;
-            const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
-            const unsigned b = __ldg(&start[row + (unsigned)xa]);
-            const unsigned e = __ldg(&start[row + (unsigned)xb + 1u]);
-#pragma unroll 2
-            for (unsigned j = b; j < e; ++j) {
-                const float4 pj = __ldg(&pos[j]);
-                const float r2 = dist2(pi, pj);
-                if (std_member(P, pi, pj, r2)) {
-                    const float x = 1.f - r2 * P.inv_h2;
-                    sum += x * x * x;
-                    cnt++;
-                    if (j != (unsigned)i) {
-                        if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
-                        listed++;
-                    }
-                }
+    for_each_candidate(P.g, start, cw & ~kWide, [&](unsigned j) {
+        const float4 pj = __ldg(&pos[j]);
+        const float r2 = dist2(pi, pj);
+        if (std_member(P, pi, pj, r2)) {
+            const float x = 1.f - r2 * P.inv_h2;
+            sum += x * x * x;
+            cnt++;
+            if (j != (unsigned)i) {
+                if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
+                listed++;
             }
         }
-    }
+    });
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
@@ -210,7 +170,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                const unsigned *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
                float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
-               float delta) {
+               float delta, int clamp_total) {
     // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
     // unconverged iterations); k >= 0: host-launched sequence, skip after convergence.
     if (k < 0) k = st->iter;
@@ -231,11 +191,20 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
         const float density = sum * P.std_c * P.mass;
         float err = density - P.target_density;
         float pr = delta * err;
-        if (pr < 0.f) {
-            pr *= P.neg_scale;
-            err *= P.neg_scale;
+        float p;
+        if (clamp_total) {
+            // warm-started corrector: the increment may be negative, the total is scaled
+            // like a negative pressure, so an overestimated start can be corrected
+            if (err < 0.f) err *= P.neg_scale;
+            p = press[i] + pr;
+            if (p < 0.f) p *= P.neg_scale;
+        } else {
+            if (pr < 0.f) {
+                pr *= P.neg_scale;
+                err *= P.neg_scale;
+            }
+            p = press[i] + pr;
         }
-        const float p = press[i] + pr;
         press[i] = p;
         rhostar[i] = density;
         derr[i] = err;
@@ -482,11 +451,11 @@ void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_fir
 }
 
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
-                         cudaStream_t s) {
+                         cudaStream_t s, int clamp_total) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
     k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
         P, B.pos[buf], B.xstar, B.cell, B.start, B.list, B.nbr, B.press, B.rhostar, B.derr, B.st, k,
-        delta);
+        delta, clamp_total);
     BBG_PEND(B, s);
 }
 

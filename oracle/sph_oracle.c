@@ -591,6 +591,7 @@ struct orc_sim {
     int higher;
     int frame_index;
     int tol_mode;   /* PredictPressure stores densityErrors (tolerance mode) */
+    int clamp_total; /* warm start: negative total pressure scaled instead of the increment */
 };
 
 static v3 *alloc_v3(int n) { return (v3 *)calloc((size_t)(n > 0 ? n : 1), sizeof(v3)); }
@@ -937,11 +938,17 @@ static void k_pred_pressure(void *ctx, int b, int e) {
         Float density = weightSum * s->mass;
         Float densityError = (density - s->targetDensity);
         Float pressure = delta * densityError;
-        if (pressure < 0) {
-            pressure *= s->negScale;
-            densityError *= s->negScale;
+        if (s->clamp_total) {
+            if (densityError < 0) densityError *= s->negScale;
+            ppi += pressure;
+            if (ppi < 0) ppi *= s->negScale;
+        } else {
+            if (pressure < 0) {
+                pressure *= s->negScale;
+                densityError *= s->negScale;
+            }
+            ppi += pressure;
         }
-        ppi += pressure;
         s->pressure[i] = ppi;
         s->dpred[i] = density;
         if (s->tol_mode) s->derr[i] = densityError;
@@ -1066,6 +1073,7 @@ int orc_pressure_force_and_integrate(orc_sim *s, double dt_in, double max_err_ra
     Float densityErrorRatio = 0;
     int it = 0;
     s->tol_mode = (mode != ORC_PCISPH_AS_SHIPPED);
+    s->clamp_total = (mode == ORC_PCISPH_WARM);
     if (mode == ORC_PCISPH_WARM) {
         /* warm start: keep each particle's pressure from the previous substep, rho* = rho,
          * and predict the first positions from F + Fp(p) instead of F alone */
