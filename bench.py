@@ -39,17 +39,23 @@ L2_FLUSH_BYTES = 256 << 20
 
 # Algorithmic (compulsory) HBM bytes per particle per launch: every FP32 SoA array a
 # kernel reads or writes counted once; neighbour re-reads are served by L1/L2.
-ALG_BYTES = {
-    "k_hash_count": 16 + 4 + 4,                    # pos in; cell, arrival index out
-    "k_place": 4 + 4 + 4 + 4 + 8,                  # cell, index, start, id in; (id, slot) out
-    "k_rank_gather": 8 + 4 + 8 + 32 + 32 + 4 + 4 + 4,  # tmp, cell, start, pos+vel in/out, id, slot, cell
-    "k_density": 16 + 4 + 36 + 4 + 4 + 4 + 4,     # pos, cell in; 9 masks, rho, 1/rho, vel.w, count out
-    "k_non_pressure": 16 + 16 + 4 + 36 + 16 + 16 + 16 + 4,  # pos, vel, cell, masks; F, x*, Fp, p out
-    "k_pred_density": 16 + 4 + 36 + 8 + 4 + 4 + 4,  # x*, cell, masks, p in/out; rho*, err, pos.w out
-    "k_pressure_force": 16 + 16 + 4 + 36 + 16 + 16 + 16,  # pos, vel, cell, masks, F; Fp, x* out
-    "k_sph_forces": 16 + 16 + 4 + 36 + 16 + 32,
-    "k_integrate": 16 + 16 + 16 + 32,
-}
+def alg_bytes(list_len):
+    """Compulsory DRAM bytes per particle of each kernel: the particle's own fields read
+    and written once, its member list (`list_len` 4-byte ids on average) read or written
+    once; neighbours' fields are re-reads of data other threads already brought on chip
+    (cell-sorted order) and are not counted."""
+    L = 4.0 * list_len
+    return {
+        "k_hash_count": 16 + 4 + 4,                        # pos in; cell, arrival index out
+        "k_place": 4 + 4 + 4 + 4 + 8,                      # cell, index, start, id in; (id, slot) out
+        "k_rank_gather": 8 + 4 + 4 + 32 + 32 + 4 + 4 + 4 + 4 + 4,  # + pressure in, previous pressure out
+        "k_density": 16 + 4 + 4 + 4 + 4 + 4 + L,          # pos, cell in; rho, 1/rho, vel.w, count, list out
+        "k_non_pressure": 16 + 16 + 4 + 4 + 16 + 4 + 16 + 16 + L,  # pos, vel, cell, count, list; F, p, Fp, x* out
+        "k_pred_density": 16 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + L,     # x*, cell, count, list, p; p, rho*, err, pos.w
+        "k_pressure_force": 16 + 16 + 4 + 4 + 16 + 16 + 16 + L,   # pos, vel, cell, count, list, F; Fp, x* out
+        "k_sph_forces": 16 + 16 + 4 + 4 + 16 + 32 + L,
+        "k_integrate": 16 + 16 + 16 + 32,
+    }
 
 
 def load_peaks():
@@ -247,6 +253,17 @@ def run_ours(args, scene, pos):
         for _ in range(args.warmup):
             g.advance_time_step(dt)
         torch.cuda.synchronize()
+        # every region below replays the same K substeps from this state
+        warm = scene.get("pressure_init", "zero") != "zero"
+        snap_p, snap_v = g.download()
+        snap_pr = g.get(bb.FIELD_PRESSURE) if warm else None
+        list_len = float(np.minimum(g.neighbor_counts() - 1, 64).mean())
+
+        def restore():
+            g.upload(snap_p, snap_v)
+            if warm:
+                g.set(bb.FIELD_PRESSURE, snap_pr)
+            torch.cuda.synchronize()
         barrier(dist)
 
         sampler = ClockSampler(local)
@@ -278,6 +295,7 @@ def run_ours(args, scene, pos):
         # per-kernel breakdown: the same substeps launched directly with CUDA events
         # around every kernel on the launching stream
         g.use_cuda_graphs(False)
+        restore()
         g.profiler_enable(True)
         torch.cuda.synchronize()
         for k in range(args.steps):
@@ -289,23 +307,39 @@ def run_ours(args, scene, pos):
         prof, _ = g.profiler_report()
         g.use_cuda_graphs(True)
 
-        # end to end through the C ABI with pinned host buffers
+        # end to end through the C ABI with pinned host buffers: every step uploads the
+        # particles, advances one substep and downloads them (warm variant: the pressure
+        # the next start needs travels with them)
         pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
         vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-        g.download(pos_h, vel_h)
-        for _ in range(max(1, args.warmup)):
+        pr_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+
+        def e2e_step():
             g.upload(pos_h, vel_h)
+            if warm:
+                g.set(bb.FIELD_PRESSURE, pr_h)
             g.advance_time_step(dt)
             g.download(pos_h, vel_h)
-        e2e_steps = args.steps
+            if warm:
+                pr_h[:] = g.get(bb.FIELD_PRESSURE)
+
+        def e2e_reset():
+            pos_h[:] = snap_p
+            vel_h[:] = snap_v
+            if warm:
+                pr_h[:] = snap_pr
+        e2e_reset()
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        e2e_reset()
+        e2e_iters = []
         barrier(dist)
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            g.upload(pos_h, vel_h)
-            g.advance_time_step(dt)
-            g.download(pos_h, vel_h)
+        for _ in range(args.steps):
+            e2e_step()
+            e2e_iters.append(g.stats()["iterations"])
         e2e_s = time.perf_counter() - t0
-        e2e_value, _, _ = aggregate(dist, float(n * e2e_steps), e2e_s)
+        e2e_value, _, _ = aggregate(dist, float(n * args.steps), e2e_s)
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
         g.close()
@@ -317,13 +351,14 @@ def run_ours(args, scene, pos):
     # roofline of the dominant kernel
     peak, peak_kind = load_peaks()
     traffic_table = load_traffic(args.config)
-    kern = {k: v for k, v in prof.items() if k in ALG_BYTES}
+    table = alg_bytes(list_len)
+    kern = {k: v for k, v in prof.items() if k in table}
     top = max(kern, key=lambda k: kern[k][0]) if kern else None
     roof = None
     if top:
         ms, cnt = kern[top]
         avg_s = ms / cnt / 1e3
-        alg = ALG_BYTES[top] * n
+        alg = table[top] * n
         achieved = alg / avg_s / 1e9
         tr = traffic_table.get(top)
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -360,11 +395,15 @@ def run_ours(args, scene, pos):
                    "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
                    "max_iterations": scene["max_iterations"],
                    "corrector_iterations_mean": float(np.mean(iters)),
+                   "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
+                   "member_list_mean": list_len,
+                   "regions": "timed, per-kernel and e2e regions each replay the same substeps "
+                              "from one snapshot taken after warm-up",
                    "max_density_error_ratio_last": max_err[-1],
                    "l2": "flushed between timed steps (256 MB write, outside the events)",
                    "parallelism": "replicas" if world > 1 else "single gpu"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 24,
-                "d2h_bytes_per_step": n * 24},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (28 if warm else 24),
+                "d2h_bytes_per_step": n * (28 if warm else 24)},
         "roofline": roof,
         "cpu_baseline": cpu,
         "gpu_launches": launches_timed,

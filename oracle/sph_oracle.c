@@ -1177,7 +1177,9 @@ int orc_pcisph_substep(orc_sim *s, double dt, double max_err_ratio, int max_it, 
     orc_update_grid_distribution(s);
     s->higher = 0;   /* ResetHigherLevel */
     orc_compute_particle_interaction(s);
-    orc_compute_density(s, 1);
+    /* the equation-of-state pressure written here is dead in the corrector (its first
+     * prediction zeroes the pressure); the warm start keeps the previous substep's instead */
+    orc_compute_density(s, mode != ORC_PCISPH_WARM);
     orc_compute_non_pressure_force(s);
     double delta = orc_compute_delta(s, dt);
     if (mode == ORC_PCISPH_AS_SHIPPED) { max_err_ratio = 0.01; max_it = 5; }
