@@ -4,16 +4,21 @@
 Workload: the 1,048,576-particle PCISPH dam break (128 x 64 x 128 cubic lattice at
 spacing 0.008, +-0.1 spacing jitter, 2 x 1 x 1.2 box), FP32 state, tolerance-mode
 corrector (max density error < 1 % of rho0, at most 20 iterations), substep dt at the
-CFL speed limit of scale 5.  A step is one substep: grid rebuild, density,
-non-pressure force, the corrector to tolerance, integration with colliders.
+CFL speed limit of scale 5, 1,000 substeps.  A step is one substep: grid rebuild,
+density, non-pressure force, the corrector to tolerance, integration with colliders.
+The first `--prep` (200) substeps run the plain corrector; the learned variant trains
+its warm-start MLP online on their (features, converged pressure) pairs.  After
+`--warmup` more substeps the timed window covers the remaining `--steps` substeps.
 
   value      particle-updates/s over the timed substeps, inputs resident in HBM, L2
              flushed (256 MB write) between steps, CUDA events on the launching stream
   e2e        the same metric through the C ABI with host buffers: upload positions and
-             velocities from pinned memory, one substep, download them, every step
+             velocities (and the carried pressure for warm starts) from pinned memory,
+             one substep, download them, every step
   roofline   dominant kernel: algorithmic bytes per launch / its average duration
   cpu_baseline  the CPU oracle (restatement of the reference's CPU path) on the box's
              host cores, on a bounded sample of the same workload
+  config.plain_same_window  the plain (zero-start) corrector timed on the same substeps
 
 `--impl reference` times the reference's CPU implementation of the path (the oracle
 port, all host threads) on the same workload and prints the same line with
@@ -199,12 +204,12 @@ def run_reference(args, scene, pos):
     # size the per-step sample so the whole run stays within ~150 s of CPU time
     probe = slab(pos, block, 8)
     rate, _, _, _ = cpu_oracle_rate(scene, probe, None, 0.0, threads, max_steps=1)
-    per_step_budget = 150.0 / max(1, args.steps + args.warmup)
+    per_step_budget = 150.0 / max(1, args.prep + args.steps + args.warmup)
     depth = int(np.clip((per_step_budget * rate) / (block[0] * block[1]) // 8 * 8, 8, block[2]))
     sample = slab(pos, block, depth)
     from oracle import oracle as O
     sim = O.OracleSim(scene, sample, None, variant="f32", threads=threads)
-    for _ in range(args.warmup):
+    for _ in range(args.prep + args.warmup):
         sim.pcisph_substep(scene["dt"], scene["max_density_error_ratio"], scene["max_iterations"],
                            O.PCISPH_TOLERANCE)
     t, iters = 0.0, 0
@@ -217,8 +222,8 @@ def run_reference(args, scene, pos):
     sim.close()
     value = len(sample) * args.steps / t
     desc = ("%d-layer slab (%d particles) of the dam-break block, one tolerance-mode substep "
-            "per step from t=0 (%d warm-up substeps), %.2f corrector iterations per substep"
-            % (depth, len(sample), args.warmup, iters / max(1, args.steps)))
+            "per step after %d preparation and %d warm-up substeps, %.2f corrector iterations "
+            "per substep" % (depth, len(sample), args.prep, args.warmup, iters / max(1, args.steps)))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
@@ -235,6 +240,37 @@ def run_reference(args, scene, pos):
     print(json.dumps(line), flush=True)
 
 
+def launches_per_substep(scene, variant, iters):
+    """Kernels one graph-launched PCISPH substep runs: 4 grid-rebuild kernels (hash and
+    count, scan, place, rank and gather; the scan is 3 launches), density, non-pressure,
+    3 per corrector iteration (predicted density, pressure force, loop control), plus the
+    warm start (start pressure, pressure force) and, learned, the feature pass; 2 more when
+    pseudo-viscosity is active."""
+    pv = 2 if scene.get("pseudo_viscosity", 10.0) * scene["dt"] > 0.1 else 0
+    extra = {"plain": 0, "warm": 2, "learned": 3}[variant]
+    return 8 + extra + 3 * iters + pv
+
+
+def timed_substeps(g, dt, steps, stream, flush, events=True):
+    """K substeps (graph replay), L2 flushed before each outside the events."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    iters, errs = [], []
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()
+        starts[k].record(stream)
+        g.advance_time_step(dt)
+        ends[k].record(stream)
+        st = g.stats()
+        iters.append(st["iterations"])
+        errs.append(st["max_density_error_ratio"])
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    return ms, iters, errs
+
+
 def run_ours(args, scene, pos):
     import torch
 
@@ -245,57 +281,67 @@ def run_ours(args, scene, pos):
     dist = init_dist(world, "nccl")
     n = len(pos)
     dt = scene["dt"]
+    variant = args.variant
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    warm = variant != "plain"
     with torch.cuda.stream(stream):
         g = bb.Solver(scene, pos=pos, device=local)
         g.set_stream(stream)
+        # the first `prep` substeps of the run: plain corrector; the learned variant trains
+        # its model on their (features, converged pressure) pairs
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.prep):
+            g.advance_time_step(dt)
+        torch.cuda.synchronize()
+        prep_s = time.perf_counter() - t0
+        mlp = g.mlp_status() if variant == "learned" else None
         for _ in range(args.warmup):
             g.advance_time_step(dt)
         torch.cuda.synchronize()
         # every region below replays the same K substeps from this state
-        warm = scene.get("pressure_init", "zero") != "zero"
         snap_p, snap_v = g.download()
         snap_pr = g.get(bb.FIELD_PRESSURE) if warm else None
         list_len = float(np.minimum(g.neighbor_counts() - 1, 64).mean())
 
-        def restore():
-            g.upload(snap_p, snap_v)
-            if warm:
-                g.set(bb.FIELD_PRESSURE, snap_pr)
+        def restore(solver, with_pressure):
+            solver.upload(snap_p, snap_v)
+            if with_pressure:
+                solver.set(bb.FIELD_PRESSURE, snap_pr)
             torch.cuda.synchronize()
         barrier(dist)
 
         sampler = ClockSampler(local)
         sampler.start()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        iters, max_err = [], []
-        torch.cuda.synchronize()
         barrier(dist)
         # timed region: every substep is one CUDA-graph launch
-        for k in range(args.steps):
-            flush.zero_()
-            starts[k].record(stream)
-            g.advance_time_step(dt)
-            ends[k].record(stream)
-            st = g.stats()
-            iters.append(st["iterations"])
-            max_err.append(st["max_density_error_ratio"])
-        torch.cuda.synchronize()
+        step_ms, iters, max_err = timed_substeps(g, dt, args.steps, stream, flush)
         barrier(dist)
-        step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         total_s = sum(step_ms) / 1e3
         value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
-        # kernels launched in the timed region: 6 grid + density + non-pressure + 3 per
-        # corrector iteration (+ 2 pseudo-viscosity when active)
-        pv = 2 if scene.get("pseudo_viscosity", 10.0) * dt > 0.1 else 0
-        launches_timed = int(sum(8 + 3 * it + pv for it in iters))
+        launches_timed = int(sum(launches_per_substep(scene, variant, it) for it in iters))
+
+        # the plain corrector on the same substeps, for the learned / warm comparison
+        plain = None
+        if warm and not args.no_plain:
+            gp = bb.Solver(dict(scene, pressure_init="zero"), pos=snap_p, vel=snap_v, device=local)
+            gp.set_stream(stream)
+            for _ in range(3):
+                gp.advance_time_step(dt)
+            restore(gp, False)
+            pms, pit, perr = timed_substeps(gp, dt, args.steps, stream, flush)
+            gp.close()
+            pv, _, _ = aggregate(dist, float(n * args.steps), sum(pms) / 1e3)
+            plain = {"value": pv, "ms_per_step": sum(pms) / args.steps,
+                     "corrector_iterations_mean": float(np.mean(pit)),
+                     "max_density_error_ratio_max": float(np.max(perr)),
+                     "speedup_of_this_variant": value / pv}
 
         # per-kernel breakdown: the same substeps launched directly with CUDA events
         # around every kernel on the launching stream
         g.use_cuda_graphs(False)
-        restore()
+        restore(g, warm)
         g.profiler_enable(True)
         torch.cuda.synchronize()
         for k in range(args.steps):
@@ -308,7 +354,7 @@ def run_ours(args, scene, pos):
         g.use_cuda_graphs(True)
 
         # end to end through the C ABI with pinned host buffers: every step uploads the
-        # particles, advances one substep and downloads them (warm variant: the pressure
+        # particles, advances one substep and downloads them (warm variants: the pressure
         # the next start needs travels with them)
         pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
         vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
@@ -382,26 +428,41 @@ def run_ours(args, scene, pos):
                                                       args.cpu_budget, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": ("%d substep(s) (%.1f s, %.2f corrector iterations each) of a %d-particle "
-                          "slab of the same dam-break state, FP32 oracle, %d threads"
+                          "slab of the same dam-break state, FP32 oracle, plain corrector, %d threads"
                           % (steps_c, t_c, iters_c / max(1, steps_c), len(sample_p), threads))}
 
     per_kernel = {k: {"ms_total": v[0], "launches": v[1], "avg_us": 1e3 * v[0] / max(1, v[1])}
                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    config = {"workload": scene["workload"], "variant": variant, "solver": "pcisph",
+              "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
+              "max_iterations": scene["max_iterations"],
+              "window": "substeps %d..%d of the run (%d preparation + %d warm-up substeps first)"
+                        % (args.prep + args.warmup, args.prep + args.warmup + args.steps - 1,
+                           args.prep, args.warmup),
+              "corrector_iterations_mean": float(np.mean(iters)),
+              "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
+              "max_density_error_ratio_max": float(np.max(max_err)),
+              "member_list_mean": list_len,
+              "preparation_s": prep_s,
+              "regions": "timed, per-kernel and e2e regions each replay the same substeps "
+                         "from one snapshot taken after warm-up",
+              "l2": "flushed between timed steps (256 MB write, outside the events)",
+              "parallelism": "replicas" if world > 1 else "single gpu"}
+    if variant == "warm":
+        config["warm_start"] = "previous substep's pressure x 0.5, monotone corrector update"
+    if variant == "learned":
+        config["warm_start"] = ("MLP 4-64-64-1 GELU, BF16 tensor-core inference; estimate x 0.9, "
+                                "monotone corrector update")
+        config["mlp"] = {"trained_substeps": mlp["trained_substeps"], "adam_steps": mlp["adam_steps"],
+                         "last_training_loss": mlp["last_loss"],
+                         "training": "online during the %d preparation substeps" % args.prep}
+    if plain is not None:
+        config["plain_same_window"] = plain
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene["workload"], "variant": args.variant, "solver": "pcisph",
-                   "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
-                   "max_iterations": scene["max_iterations"],
-                   "corrector_iterations_mean": float(np.mean(iters)),
-                   "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
-                   "member_list_mean": list_len,
-                   "regions": "timed, per-kernel and e2e regions each replay the same substeps "
-                              "from one snapshot taken after warm-up",
-                   "max_density_error_ratio_last": max_err[-1],
-                   "l2": "flushed between timed steps (256 MB write, outside the events)",
-                   "parallelism": "replicas" if world > 1 else "single gpu"},
+        "config": config,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (28 if warm else 24),
                 "d2h_bytes_per_step": n * (28 if warm else 24)},
         "roofline": roof,
@@ -417,24 +478,30 @@ def run_ours(args, scene, pos):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=795,
+                    help="timed substeps (default: the rest of the 1,000-substep run)")
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--prep", type=int, default=200,
+                    help="substeps run before warm-up (the learned variant trains during them)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="pcisph_1m")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--variant", default="plain", choices=["plain", "warm"],
-                    help="corrector start: plain = zero pressure (reference), warm = the "
-                         "previous substep's pressure")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
+    ap.add_argument("--variant", default="learned", choices=["plain", "warm", "learned"],
+                    help="corrector start: plain = zero pressure (reference), warm = the previous "
+                         "substep's pressure, learned = the MLP estimate")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     from bubbles_gb300 import scenes
     rank, _, _ = dist_env()
     scene, pos = scenes.config(args.config, seed=args.seed + rank)
-    scene["pressure_init"] = {"plain": "zero", "warm": "previous"}[args.variant]
+    scene["pressure_init"] = {"plain": "zero", "warm": "previous", "learned": "learned"}[args.variant]
+    if args.variant == "learned":
+        scene["mlp"] = {"train_substeps": args.prep}
     if args.impl == "reference":
         run_reference(args, scene, pos)
     else:

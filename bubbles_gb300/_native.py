@@ -15,6 +15,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device mem
 SOLVER_PCISPH, SOLVER_SPH = 0, 1
 PCISPH_AS_SHIPPED, PCISPH_TOLERANCE = 0, 1
 PRESSURE_INIT_ZERO, PRESSURE_INIT_PREVIOUS, PRESSURE_INIT_LEARNED = 0, 1, 2
+WARM_CLAMP_TOTAL, WARM_MONOTONE = 0, 1
 SHAPE_BOX, SHAPE_SPHERE = 1, 2
 MAX_COLLIDERS = 16
 
@@ -46,7 +47,23 @@ class SolverDesc(ctypes.Structure):
                 ("max_iterations", ctypes.c_int),
                 ("max_density_error_ratio", ctypes.c_double),
                 ("device", ctypes.c_int),
-                ("pressure_init", ctypes.c_int)]
+                ("pressure_init", ctypes.c_int),
+                ("warm_rule", ctypes.c_int),
+                ("warm_scale", ctypes.c_double)]
+
+
+MLP_PARAMS = 4545
+
+
+class MlpDesc(ctypes.Structure):
+    _fields_ = [("train_substeps", ctypes.c_int),
+                ("batch", ctypes.c_int),
+                ("steps_per_substep", ctypes.c_int),
+                ("learning_rate", ctypes.c_double),
+                ("beta1", ctypes.c_double),
+                ("beta2", ctypes.c_double),
+                ("epsilon", ctypes.c_double),
+                ("seed", ctypes.c_ulonglong)]
 
 
 class Shape(ctypes.Structure):
@@ -129,6 +146,15 @@ SIGNATURES = {
     "bbg_profiler_enable": [_P, _I],
     "bbg_use_cuda_graphs": [_P, _I],
     "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P],
+    "bbg_mlp_desc_default": [ctypes.POINTER(MlpDesc)],
+    "bbg_mlp_configure": [_P, ctypes.POINTER(MlpDesc)],
+    "bbg_mlp_get_params": [_P, _FP],
+    "bbg_mlp_set_params": [_P, _FP],
+    "bbg_mlp_set_trained": [_P, _I],
+    "bbg_mlp_status": [_P, _IP, _IP, _DP],
+    "bbg_mlp_infer": [_P, _FP, _I, _FP],
+    "bbg_mlp_train_batch": [_P, _FP, _FP, _I],
+    "bbg_mlp_get_features": [_P, _FP],
     "bbg_profiler_report": [_P, _I, ctypes.c_char_p, _DP, _IP, _IP,
                             ctypes.POINTER(ctypes.c_int64)],
 }

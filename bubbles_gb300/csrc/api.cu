@@ -4,11 +4,14 @@
 #include "../../include/bbg.h"
 #include "bbg_kernels.h"
 #include "host_math.h"
+#include "mlp.h"
 
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <random>
+#include <vector>
 
 using namespace bbg;
 
@@ -77,7 +80,7 @@ struct bbg_solver_s {
     struct SubstepGraph {
         bool valid = false;
         unsigned epoch = 0, dt_bits = 0, tol_bits = 0;
-        int state = -1, pid = -1, max_it = 0;
+        int state = -1, pid = -1, max_it = 0, variant = -1;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
     } graphs[4];
@@ -85,6 +88,12 @@ struct bbg_solver_s {
     unsigned epoch = 1;          // bumped whenever captured launch arguments may change
     bool use_graphs = true;
     cudaStream_t aux = nullptr;  // capture stream of the corrector loop body
+    // learned warm start
+    MlpBufs mlp;
+    bbg_mlp_desc mdesc;
+    bool mlp_alloc = false;
+    int mlp_trained = 0;         // substeps used for training so far
+    double mlp_loss_count = 1;   // samples behind the loss accumulator
 };
 
 namespace {
@@ -152,8 +161,11 @@ void drop_graphs(bbg_solver s) {
     }
 }
 
+void free_mlp(bbg_solver s);
+
 bbg_status free_all(bbg_solver s) {
     drop_graphs(s);
+    free_mlp(s);
     DevBufs &B = s->B;
     void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
                     B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
@@ -168,6 +180,75 @@ bbg_status free_all(bbg_solver s) {
     if (s->h_u) cudaFreeHost(s->h_u);
     s->h_st = nullptr;
     s->h_u = nullptr;
+    return BBG_OK;
+}
+
+void free_mlp(bbg_solver s) {
+    MlpBufs &M = s->mlp;
+    void *ptrs[] = {M.theta, M.grad, M.m1, M.m2, M.w1f, M.w2f, M.tail, M.step, M.loss, M.feat, M.divsum,
+                    M.bx, M.bt};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    M = MlpBufs();
+    s->mlp_alloc = false;
+}
+
+// Glorot-uniform weights, zero biases (FP32 master copy on the host, then uploaded).
+std::vector<float> mlp_initial_params(unsigned long long seed) {
+    std::vector<float> th(kParams, 0.f);
+    std::mt19937_64 rng(seed);
+    auto fill = [&](int off, int fan_in, int fan_out, int count) {
+        const float a = sqrtf(6.f / (float)(fan_in + fan_out));
+        std::uniform_real_distribution<float> u(-a, a);
+        for (int k = 0; k < count; k++) th[off + k] = u(rng);
+    };
+    fill(kOffW1, kIn, kHid, kIn * kHid);
+    fill(kOffW2, kHid, kHid, kHid * kHid);
+    fill(kOffW3, kHid, 1, kHid);
+    return th;
+}
+
+bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
+    if (d.batch < 1 || d.train_substeps < 0 || d.steps_per_substep < 0 || !(d.learning_rate > 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "invalid MLP training settings");
+    CK(cudaStreamSynchronize(s->stream));
+    if (!s->mlp_alloc || s->mlp.batch != d.batch) {
+        free_mlp(s);
+        MlpBufs &M = s->mlp;
+        const size_t n = (size_t)s->capacity;
+        bbg_status r = BBG_OK;
+#define ALLOC(ptr, cnt) if (!r) r = dalloc(&(ptr), (cnt))
+        ALLOC(M.theta, kParams); ALLOC(M.grad, kParams); ALLOC(M.m1, kParams); ALLOC(M.m2, kParams);
+        ALLOC(M.w1f, 8 * 32); ALLOC(M.w2f, 64 * 32); ALLOC(M.tail, kTail); ALLOC(M.step, 1);
+        ALLOC(M.loss, 1); ALLOC(M.feat, n); ALLOC(M.divsum, n); ALLOC(M.bx, (size_t)d.batch);
+        ALLOC(M.bt, (size_t)d.batch);
+#undef ALLOC
+        if (r) {
+            free_mlp(s);
+            return r;
+        }
+        CK(mlp_prepare());
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->desc.device));
+        M.infer_blocks = 2 * (sms > 0 ? sms : 1);
+        M.batch = d.batch;
+        s->mlp_alloc = true;
+    }
+    s->mdesc = d;
+    const std::vector<float> th = mlp_initial_params(d.seed);
+    MlpBufs &M = s->mlp;
+    CK(cudaMemcpyAsync(M.theta, th.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(M.grad, 0, sizeof(float) * kParams, s->stream));
+    CK(cudaMemsetAsync(M.m1, 0, sizeof(float) * kParams, s->stream));
+    CK(cudaMemsetAsync(M.m2, 0, sizeof(float) * kParams, s->stream));
+    CK(cudaMemsetAsync(M.step, 0, sizeof(unsigned), s->stream));
+    CK(cudaMemsetAsync(M.loss, 0, sizeof(double), s->stream));
+    CK(cudaMemsetAsync(M.feat, 0, sizeof(float4) * (size_t)s->capacity, s->stream));
+    launch_mlp_pack(M, s->stream);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->stream));
+    s->mlp_trained = 0;
+    s->epoch++;
     return BBG_OK;
 }
 
@@ -240,6 +321,61 @@ void add_substep_stats(bbg_solver s, float dt) {
     a.max_force = f;
 }
 
+// Learned warm start: 0 off, 1 a training substep (plain corrector, then training on its
+// pairs), 2 an inference substep (corrector started from the model's estimate).
+static int mlp_mode(bbg_solver s) {
+    if (s->desc.pressure_init != BBG_PRESSURE_INIT_LEARNED || s->desc.solver_kind != BBG_SOLVER_PCISPH)
+        return 0;
+    return s->mlp_trained < s->mdesc.train_substeps ? 1 : 2;
+}
+
+static bool warm_active(bbg_solver s) {
+    return s->desc.pressure_init == BBG_PRESSURE_INIT_PREVIOUS || mlp_mode(s) == 2;
+}
+
+// Warm-started correctors with the CLAMP_TOTAL rule let the pressure decrease.
+static int clamp_total(bbg_solver s) {
+    return warm_active(s) && s->desc.warm_rule == BBG_WARM_CLAMP_TOTAL;
+}
+
+// Start pressure = warm_scale * estimate; a scale <= 0 picks the measured defaults (the
+// monotone update cannot lower an overestimated start, so the estimate is damped: the
+// carried pressure by half, the learned one by a tenth).
+static float warm_scale(bbg_solver s) {
+    if (s->desc.warm_scale > 0) return (float)s->desc.warm_scale;
+    return s->desc.pressure_init == BBG_PRESSURE_INIT_LEARNED ? 0.9f : 0.5f;
+}
+
+// Pressure a corrector step assigns to a 1 % density error (the MLP's pressure unit).
+static float pressure_unit(bbg_solver s, float delta) { return delta * s->P.target_density * 0.01f; }
+
+// Launches of a substep between the density pass and the corrector loop.
+static void launch_prologue(bbg_solver s, int work, float dt, float delta, int max_it, cudaStream_t cs) {
+    const Params &P = s->P;
+    const DevBufs &B = s->B;
+    const int mm = mlp_mode(s);
+    const bool warm = warm_active(s);
+    launch_non_pressure(P, B, work, warm ? 0 : 1, dt, dt / s->mass, cs, mm ? s->mlp.divsum : nullptr);
+    if (mm) launch_mlp_features(P, B, s->mlp, work, dt, pressure_unit(s, delta), cs);
+    if (warm) {
+        if (mm == 2) launch_mlp_warm_start(P, B, s->mlp, work, pressure_unit(s, delta), warm_scale(s), cs);
+        else launch_warm_start(P, B, work, warm_scale(s), cs);
+        launch_pressure_force(P, B, work, 0, max_it, dt, dt / s->mass, cs, 2);
+    }
+}
+
+// After a training substep's corrector: Adam steps on pairs of the converged state.
+static void launch_training(bbg_solver s, float delta, cudaStream_t cs) {
+    const bbg_mlp_desc &d = s->mdesc;
+    cudaMemsetAsync(s->mlp.loss, 0, sizeof(double), cs);
+    s->mlp_loss_count = (double)s->mlp.batch * (double)(d.steps_per_substep > 0 ? d.steps_per_substep : 1);
+    for (int k = 0; k < d.steps_per_substep; k++) {
+        launch_mlp_collect(s->P, s->B, s->mlp, pressure_unit(s, delta), cs);
+        launch_mlp_train_step(s->mlp, s->mlp.bx, s->mlp.bt, s->mlp.batch, (float)d.learning_rate,
+                              (float)d.beta1, (float)d.beta2, (float)d.epsilon, cs);
+    }
+}
+
 // Corrector loop of ComputePressureForceAndIntegrate launched from the host: after each
 // iteration the host reads that iteration's max density error, as the reference's loop
 // does (pcisph_equations3.cpp:238-246), and stops once it is below tolerance.  The
@@ -252,8 +388,7 @@ bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
     s->last_max_it = max_it;
     s->last_tol = s->P.max_err_ratio;
     for (int k = 0; k < max_it; k++) {
-        launch_pred_density(s->P, s->B, s->state, k, delta, s->stream,
-                            s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO);
+        launch_pred_density(s->P, s->B, s->state, k, delta, s->stream, clamp_total(s));
         launch_pressure_force(s->P, s->B, s->state, k, max_it, dt, dt_over_m, s->stream);
         CK_LAUNCH();
         if (k == max_it - 1) break;
@@ -304,12 +439,7 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
         launch_sph_forces(P, B, work, dt, cs);
     } else {
         launch_density(P, B, work, 0, cs);
-        const bool warm = s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO;
-        launch_non_pressure(P, B, work, warm ? 0 : 1, dt, dt / s->mass, cs);
-        if (warm) {
-            launch_warm_start(P, B, work, cs);
-            launch_pressure_force(P, B, work, 0, max_it, dt, dt / s->mass, cs, 2);
-        }
+        launch_prologue(s, work, dt, delta, max_it, cs);
         cudaStreamCaptureStatus status;
         cudaGraph_t cg = nullptr;
         const cudaGraphNode_t *deps = nullptr;
@@ -329,8 +459,7 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
             e = cudaStreamBeginCaptureToGraph(s->aux, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                launch_pred_density(P, B, work, -1, delta, s->aux,
-                                    s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO);
+                launch_pred_density(P, B, work, -1, delta, s->aux, clamp_total(s));
                 launch_pressure_force(P, B, work, -1, max_it, dt, dt / s->mass, s->aux);
                 launch_corrector_control(P, B, max_it, handle, s->aux);
                 cudaError_t e2 = cudaStreamEndCapture(s->aux, &body);
@@ -339,6 +468,7 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
         }
         if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1,
                                                                       cudaStreamSetCaptureDependencies);
+        if (mlp_mode(s) == 1) launch_training(s, delta, cs);
     }
     const float pv = (float)s->desc.pseudo_viscosity * dt;
     if (pv > 0.1) {
@@ -392,7 +522,8 @@ bbg_status substep(bbg_solver s, float dt) {
         bbg_solver_s::SubstepGraph *hit = nullptr;
         for (auto &g : s->graphs)
             if (g.valid && g.epoch == s->epoch && g.dt_bits == fbits(dt) && g.state == s->state &&
-                g.pid == s->pid_cur && g.max_it == max_it && g.tol_bits == fbits(s->P.max_err_ratio))
+                g.pid == s->pid_cur && g.max_it == max_it && g.tol_bits == fbits(s->P.max_err_ratio) &&
+                g.variant == mlp_mode(s))
                 hit = &g;
         if (!hit) {
             hit = &s->graphs[s->graph_next];
@@ -405,8 +536,10 @@ bbg_status substep(bbg_solver s, float dt) {
             hit->pid = s->pid_cur;
             hit->max_it = max_it;
             hit->tol_bits = fbits(s->P.max_err_ratio);
+            hit->variant = mlp_mode(s);
         }
         CK(cudaGraphLaunch(hit->exec, s->stream));
+        if (mlp_mode(s) == 1) s->mlp_trained++;
         s->last_max_it = max_it;
         s->last_tol = s->P.max_err_ratio;
         after_substep(s, dt);
@@ -423,16 +556,16 @@ bbg_status substep(bbg_solver s, float dt) {
         return pseudo_viscosity(s, dt);
     }
     launch_density(s->P, s->B, s->state, 0, s->stream);
-    const bool warm = s->desc.pressure_init != BBG_PRESSURE_INIT_ZERO;
-    launch_non_pressure(s->P, s->B, s->state, warm ? 0 : 1, dt, dt / s->mass, s->stream);
-    if (warm) {
-        launch_warm_start(s->P, s->B, s->state, s->stream);
-        launch_pressure_force(s->P, s->B, s->state, 0, max_it, dt, dt / s->mass, s->stream, 2);
-    }
+    launch_prologue(s, s->state, dt, delta, max_it, s->stream);
     CK_LAUNCH();
     s->valid |= bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE);
     r = corrector(s, dt, delta, max_it);
     if (r) return r;
+    if (mlp_mode(s) == 1) {
+        launch_training(s, delta, s->stream);
+        CK_LAUNCH();
+        s->mlp_trained++;
+    }
     return pseudo_viscosity(s, dt);
 }
 
@@ -541,6 +674,9 @@ bbg_status bbg_solver_desc_default(bbg_solver_desc *d, int kind) {
     d->max_iterations = 5;
     d->max_density_error_ratio = 0.01;
     d->device = 0;
+    d->pressure_init = BBG_PRESSURE_INIT_ZERO;
+    d->warm_rule = BBG_WARM_MONOTONE;
+    d->warm_scale = 0.0;   // automatic: 0.5 for PREVIOUS, 0.9 for LEARNED
     return BBG_OK;
 }
 
@@ -634,7 +770,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.force, n); ALLOC(B.xstar, n); ALLOC(B.pforce, n); ALLOC(B.smoothed, n);
     ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
     ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
-    ALLOC(B.list, (size_t)kMaxList * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
+    ALLOC(B.list, (size_t)(kMaxList / 8) * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
     ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);
@@ -653,6 +789,17 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
         cudaStreamDestroy(s->own_stream);
         delete s;
         return r;
+    }
+    if (desc->pressure_init == BBG_PRESSURE_INIT_LEARNED) {
+        bbg_mlp_desc md;
+        bbg_mlp_desc_default(&md);
+        r = mlp_allocate(s, md);
+        if (r) {
+            free_all(s);
+            cudaStreamDestroy(s->own_stream);
+            delete s;
+            return r;
+        }
     }
     *out = s;
     return BBG_OK;
@@ -1145,3 +1292,121 @@ bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts) {
 }
 
 }  // extern "C"
+
+// ----------------------------------------------------------------------------
+// learned warm start
+// ----------------------------------------------------------------------------
+namespace {
+bbg_status require_mlp(bbg_solver s) {
+    if (!s->mlp_alloc) return fail(BBG_ERR_STATE, "the learned warm start is not configured");
+    return BBG_OK;
+}
+}  // namespace
+
+bbg_status bbg_mlp_desc_default(bbg_mlp_desc *d) {
+    if (!d) return fail(BBG_ERR_INVALID_ARGUMENT, "null desc");
+    memset(d, 0, sizeof(*d));
+    d->train_substeps = 200;
+    d->batch = 16384;
+    d->steps_per_substep = 4;
+    d->learning_rate = 1e-3;
+    d->beta1 = 0.9;
+    d->beta2 = 0.999;
+    d->epsilon = 1e-8;
+    d->seed = 20240601ull;
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_configure(bbg_solver s, const bbg_mlp_desc *d) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!d) return fail(BBG_ERR_INVALID_ARGUMENT, "null desc");
+    return mlp_allocate(s, *d);
+}
+
+bbg_status bbg_mlp_get_params(bbg_solver s, float *theta) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (!theta) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
+    CK(cudaMemcpyAsync(theta, s->mlp.theta, sizeof(float) * kParams, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_set_params(bbg_solver s, const float *theta) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (!theta) return fail(BBG_ERR_INVALID_ARGUMENT, "null input");
+    CK(cudaMemcpyAsync(s->mlp.theta, theta, sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
+    launch_mlp_pack(s->mlp, s->stream);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_set_trained(bbg_solver s, int trained) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (trained < 0) return fail(BBG_ERR_INVALID_ARGUMENT, "negative substep count");
+    s->mlp_trained = trained;
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_status(bbg_solver s, int *trained, int *adam_steps, double *last_loss) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    unsigned step = 0;
+    double loss = 0;
+    CK(cudaMemcpyAsync(s->h_u, s->mlp.step, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    memcpy(&step, s->h_u, sizeof(unsigned));
+    CK(cudaMemcpy(&loss, s->mlp.loss, sizeof(double), cudaMemcpyDeviceToHost));
+    if (trained) *trained = s->mlp_trained;
+    if (adam_steps) *adam_steps = (int)step;
+    if (last_loss) *last_loss = loss / s->mlp_loss_count;
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_infer(bbg_solver s, const float *features, int n, float *out) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (!features || !out || n <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 features");
+    if (n > s->capacity) return fail(BBG_ERR_CAPACITY, "%d rows exceed capacity %d", n, s->capacity);
+    float *df = s->B.stage, *dout = s->B.stage + 4 * (size_t)s->capacity;
+    CK(cudaMemcpyAsync(df, features, sizeof(float) * 4 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    launch_mlp_infer_raw(s->mlp, reinterpret_cast<const float4 *>(df), n, dout, s->stream);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_train_batch(bbg_solver s, const float *features, const float *targets, int batch) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (!features || !targets || batch <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "need a batch");
+    if (5 * (size_t)batch > 6 * (size_t)s->capacity)
+        return fail(BBG_ERR_CAPACITY, "batch of %d exceeds the staging of capacity %d", batch, s->capacity);
+    float *dx = s->B.stage, *dt = s->B.stage + 4 * (size_t)batch;
+    CK(cudaMemcpyAsync(dx, features, sizeof(float) * 4 * (size_t)batch, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dt, targets, sizeof(float) * (size_t)batch, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->mlp.loss, 0, sizeof(double), s->stream));
+    s->mlp_loss_count = (double)batch;
+    const bbg_mlp_desc &d = s->mdesc;
+    launch_mlp_train_step(s->mlp, reinterpret_cast<const float4 *>(dx), dt, batch, (float)d.learning_rate,
+                          (float)d.beta1, (float)d.beta2, (float)d.epsilon, s->stream);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_mlp_get_features(bbg_solver s, float *out) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (bbg_status r = require_mlp(s)) return r;
+    if (!out) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    launch_mlp_get_features(s->mlp, s->B.slot, s->B.stage, s->n, s->stream);
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(out, s->B.stage, sizeof(float) * 4 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}

@@ -166,60 +166,10 @@ __device__ __forceinline__ float dist2(float4 a, float4 b) {
     return dx * dx + dy * dy + dz * dz;
 }
 
-// Visit the 27 neighbour cells of cell c (reference neighbour list,
-// src/core/grid.h:555-593) as 9 contiguous slot ranges of the cell-sorted arrays.
-template <class F>
-__device__ __forceinline__ void for_each_candidate(const GridDev &g, const unsigned *__restrict__ start,
-                                                   unsigned c, F &&f) {
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const unsigned plane = (unsigned)nx * (unsigned)ny;
-    const int cz = (int)(c / plane);
-    const unsigned rem = c - (unsigned)cz * plane;
-    const int cy = (int)(rem / (unsigned)nx);
-    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
-    const int x0 = cx > 0 ? cx - 1 : 0;
-    const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
-    const int z0 = cz > 0 ? cz - 1 : 0, z1 = cz + 1 < nz ? cz + 1 : nz - 1;
-    const int y0 = cy > 0 ? cy - 1 : 0, y1 = cy + 1 < ny ? cy + 1 : ny - 1;
-    for (int z = z0; z <= z1; ++z) {
-        for (int y = y0; y <= y1; ++y) {
-            const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
-            const unsigned b = __ldg(&start[row + (unsigned)x0]);
-            const unsigned e = __ldg(&start[row + (unsigned)x1 + 1u]);
-            for (unsigned j = b; j < e; ++j) f(j);
-        }
-    }
-}
-
-// Neighbour sets recorded by the density pass: the slots of each particle's bucket
-// members other than itself, member-major (list[q * n + i], q < kMaxList) so a warp reads
-// entry q of 32 particles in one coalesced load.  A particle with more than kMaxList
-// members has kWide set in its cell word and is re-tested exactly on every pass instead.
+// A particle whose neighbour set does not fit the compact list (tile.cuh) has kWide set
+// in its cell word and is re-tested exactly on every pass instead.
 constexpr unsigned kWide = 0x80000000u;
 constexpr int kMaxList = 64;
-
-// f(j) for every member j != i of particle i's step-start neighbour set.
-template <class F>
-__device__ __forceinline__ void for_each_member(const Params &P, const unsigned *__restrict__ start,
-                                                const unsigned *__restrict__ list,
-                                                const int *__restrict__ nbr,
-                                                const float4 *__restrict__ pos, unsigned cellw,
-                                                int i, F &&f) {
-    if (cellw & kWide) {
-        const float4 pi = pos[i];
-        for_each_candidate(P.g, start, cellw & ~kWide, [&](unsigned j) {
-            if (j == (unsigned)i) return;
-            const float4 pj = __ldg(&pos[j]);
-            if (std_member(P, pi, pj, dist2(pi, pj))) f(j);
-        });
-        return;
-    }
-    const int cnt = __ldg(&nbr[i]) - 1;   // members other than i
-    const unsigned n = (unsigned)P.n;
-    const unsigned *l = list + i;
-#pragma unroll 4
-    for (int q = 0; q < cnt; ++q) f(__ldg(&l[(unsigned)q * n]));
-}
 
 // ----------------------------------------------------------------------------
 // colliders: exact FP32 restatement of CollisionHandle / ColliderSet3::ResolveCollision

@@ -21,7 +21,8 @@ struct DevBufs {
     unsigned *partials;        // scan partials
     uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
     int *nbr;                  // neighbour count of each sorted slot
-    unsigned *list;            // kMaxList member slots per particle (member-major)
+    uint4 *list;               // member lists: kMaxList / 8 chunks of 8 16-bit entries
+                               // per particle, chunk-major (list[c * n + i]; tile.cuh)
     float *inv_rho;            // 1 / density
     float *pprev;              // pressure of the previous substep, in the current order
     StepState *st;
@@ -60,8 +61,9 @@ void launch_max_force(const float4 *force, int n, unsigned *out_bits, cudaStream
 // sph.cu
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure,
                     cudaStream_t s);
+// divsum != null: also the velocity-divergence sum of each particle (learned warm start)
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
-                         float dt_over_m, cudaStream_t s);
+                         float dt_over_m, cudaStream_t s, float *divsum = nullptr);
 void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_first, float dt,
                           float dt_over_m, cudaStream_t s);
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
@@ -72,7 +74,8 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
 // 1: pressure force only; 2: pressure force and prediction, never integration.
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it,
                            float dt, float dt_over_m, cudaStream_t s, int mode = 0);
-void launch_warm_start(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
+// p = scale * previous pressure, rho* = rho, pos.w = p / rho^2
+void launch_warm_start(const Params &P, const DevBufs &B, int buf, float scale, cudaStream_t s);
 void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
                               cudaGraphConditionalHandle handle, cudaStream_t s);
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);

@@ -15,14 +15,14 @@ namespace bbg {
 enum KernelId {
     KID_HASH_COUNT = 0, KID_SCAN, KID_PLACE, KID_RANK_GATHER, KID_DENSITY, KID_NON_PRESSURE,
     KID_PREDICT_FIRST, KID_PRED_DENSITY, KID_PRESSURE_FORCE, KID_SPH_FORCES, KID_INTEGRATE,
-    KID_PSEUDO_VISCOSITY, KID_LAYOUT, KID_MAX_FORCE, KID_COUNT
+    KID_PSEUDO_VISCOSITY, KID_LAYOUT, KID_MAX_FORCE, KID_MLP, KID_MLP_TRAIN, KID_COUNT
 };
 
 inline const char *kernel_name(int id) {
     static const char *names[KID_COUNT] = {
         "k_hash_count", "k_scan", "k_place", "k_rank_gather", "k_density", "k_non_pressure",
         "k_predict_first", "k_pred_density", "k_pressure_force", "k_sph_forces", "k_integrate",
-        "k_pseudo_viscosity", "k_layout", "k_max_force"};
+        "k_pseudo_viscosity", "k_layout", "k_max_force", "k_mlp_warm_start", "k_mlp_train"};
     return (id >= 0 && id < KID_COUNT) ? names[id] : "?";
 }
 

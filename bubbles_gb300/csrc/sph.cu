@@ -3,11 +3,12 @@
 //
 // Neighbour sets follow the reference buckets: j is a neighbour of i when
 // IsWithinStd(|x_i - x_j|, h) holds at the positions of the last grid update
-// (src/core/grid.h:423-447).  Instead of materialising a 100-slot bucket per particle
-// (400 B) the kernels re-test the 27 neighbour cells (9 contiguous slot ranges) at
-// every pass with the exact FP32 membership test; the predicted-density pass tests
-// membership at step-start positions and sums at predicted positions, which is what
-// the reference does with its stale bucket (src/equations/pcisph_equations3.cpp:58-89).
+// (src/core/grid.h:423-447).  The density pass tests every candidate of the 27 cells
+// (9 contiguous slot ranges) once per substep with the exact FP32 membership test and
+// records the members in a compact list (tile.cuh); later passes walk that list.  The
+// predicted-density pass uses the step-start membership with values at predicted
+// positions, which is what the reference does with its stale bucket
+// (src/equations/pcisph_equations3.cpp:58-89).
 //
 // Fusions (per PCISPH substep: density, non-pressure, 2 per corrector iteration):
 //   - non-pressure force + the k = 0 prediction (PredictVelocityAndPositionFor);
@@ -18,10 +19,11 @@
 // the host launches max_iterations x 2 kernels without synchronising; kernels of
 // iterations after convergence return immediately.
 #include "bbg_kernels.h"
+#include "tile.cuh"
 
 namespace bbg {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = kTile;
 
 static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
@@ -37,33 +39,34 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
 
 // ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
 // Tests every candidate of the 27 cells exactly once per substep and records the
-// neighbour set (the reference bucket, grid.h:423-447) as a member list.
+// neighbour set (the reference bucket, grid.h:423-447) as a compact member list.
 __global__ void __launch_bounds__(kThreads)
 k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
-          float *__restrict__ press, int *__restrict__ nbr, unsigned *__restrict__ list,
+          float *__restrict__ press, int *__restrict__ nbr, uint4 *__restrict__ list,
           int compute_pressure, StepState *st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
-    const unsigned n = (unsigned)P.n;
+    const size_t n = (size_t)P.n;
     float sum = 0.f;
     int cnt = 0;      // bucket members, i included
-    int listed = 0;   // members other than i written to the list
-    for_each_candidate(P.g, start, cw & ~kWide, [&](unsigned j) {
+    bool fits = true;
+    ChunkWriter w;    // members other than i
+    tile_candidates_coded(P.g, start, T, cw & ~kWide, &fits, [&](unsigned j, unsigned base) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
         if (std_member(P, pi, pj, r2)) {
             const float x = 1.f - r2 * P.inv_h2;
             sum += x * x * x;
             cnt++;
-            if (j != (unsigned)i) {
-                if (listed < kMaxList) list[(unsigned)listed * n + (unsigned)i] = j;
-                listed++;
-            }
+            if (j != (unsigned)i) w.push(list, n, (unsigned)i, j + base);
         }
     });
+    w.finish(list, n, (unsigned)i);
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
@@ -76,37 +79,51 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     inv_rho[i] = ir;
     reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
     nbr[i] = cnt;
-    if (listed > kMaxList) cell[i] = cw | kWide;
+    if (w.count > kMaxList || !fits) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
 // ComputeNonPressureForceFor (sph_equations3.cpp:80-110), optionally followed by the
-// k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).
+// k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).  With DIV it also
+// accumulates sum_j (1/rho_j) (1 - d/h)^2 / d (v_j - v_i).(x_j - x_i), the velocity
+// divergence up to m * 45 / (pi h^4), a feature of the learned warm start.
+template <bool DIV>
 __global__ void __launch_bounds__(kThreads)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
-               const unsigned *__restrict__ start, const unsigned *__restrict__ list, const int *__restrict__ nbr,
+               const unsigned *__restrict__ start, const uint4 *__restrict__ list, const int *__restrict__ nbr,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
-               float *__restrict__ press, int predict, float dt, float dt_over_m) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+               float *__restrict__ press, float *__restrict__ divsum, int predict, float dt, float dt_over_m) {
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const float4 vi = vel[i];
     float fx = P.mass * P.gx - P.drag * vi.x;
     float fy = P.mass * P.gy - P.drag * vi.y;
     float fz = P.mass * P.gz - P.drag * vi.z;
+    float dv = 0.f;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
-    for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
+    tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
-        const float d = r2 * rsqrtf(r2);
+        const float inv_d = rsqrtf(r2);
+        const float d = r2 * inv_d;
         const float4 vj = __ldg(&vel[j]);   // vj.w = 1 / rho_j
-        const float w = kv * (1.f - d * P.inv_h) * vj.w;
+        const float x = 1.f - d * P.inv_h;
+        const float w = kv * x * vj.w;
         fx += (vj.x - vi.x) * w;
         fy += (vj.y - vi.y) * w;
         fz += (vj.z - vi.z) * w;
+        if (DIV && r2 > 0.f) {
+            const float dot = (vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) +
+                              (vj.z - vi.z) * (pj.z - pi.z);
+            dv += vj.w * x * x * inv_d * dot;
+        }
     });
     force[i] = make_float4(fx, fy, fz, 0.f);
+    if (DIV) divsum[i] = dv;
     if (predict) {
         press[i] = 0.f;
         pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -137,15 +154,16 @@ k_predict_first(Params P, const float4 *__restrict__ pos, const float4 *__restri
     xstar[i] = F4(xs);
 }
 
-// Warm start of the corrector: p = the previous substep's pressure, rho* = rho, and
-// pos.w = p / rho^2 for the pressure-force pass that predicts x* from F + Fp(p).
+// Warm start of the corrector: p = scale * the start estimate (the previous substep's
+// pressure), rho* = rho, and pos.w = p / rho^2 for the pressure-force pass that predicts
+// x* from F + Fp(p).
 __global__ void k_warm_start(int n, float4 *pos, const float *__restrict__ rho,
                              const float *__restrict__ pinit, float *__restrict__ press,
-                             float *__restrict__ rhostar, float *__restrict__ derr) {
+                             float *__restrict__ rhostar, float *__restrict__ derr, float scale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float d = rho[i];
-    const float p = pinit[i];
+    const float p = scale * pinit[i];
     press[i] = p;
     rhostar[i] = d;
     derr[i] = 0.f;
@@ -168,19 +186,21 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
 __global__ void __launch_bounds__(kThreads)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
+               const uint4 *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
                float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
                float delta, int clamp_total) {
     // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
     // unconverged iterations); k >= 0: host-launched sequence, skip after convergence.
     if (k < 0) k = st->iter;
     else if (converged_before(P, st, k)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     float aerr = 0.f;
     if (i < P.n) {
         const float4 xi = xstar[i];
         float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
-        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
+        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 xj = __ldg(&xstar[j]);
             const float r2 = dist2(xi, xj);
             if (r2 < P.h2mz) {
@@ -233,7 +253,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
 __global__ void __launch_bounds__(kThreads)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+                 const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
@@ -242,14 +262,16 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
     else if (converged_before(P, st, k)) return;
     const bool last = mode == 0 && ((k == max_it - 1) ||
                       fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
         const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
-        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
+        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 pj = __ldg(&pos[j]);   // pj.w = p_j / rho*_j^2
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
@@ -305,9 +327,11 @@ __global__ void k_corrector_control(Params P, StepState *st, int max_it,
 __global__ void __launch_bounds__(kThreads)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-             const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+             const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
@@ -319,7 +343,7 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
         const float kv = P.visc_m2 * P.spiky_d2w_c;
-        for_each_member(P, start, list, nbr, pos, cell[i], i, [&](unsigned j) {
+        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
             const float4 pj = __ldg(&pos[j]);
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
@@ -386,15 +410,17 @@ __global__ void __launch_bounds__(kThreads)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
                const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+               const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * kTile + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     // the particle itself (distance 0): W_spiky(0) m / rho_i
     const float w0 = P.mass * __ldg(&inv_rho[i]) * P.spiky_w_c;
     const float4 v0 = vel[i];
     float ws = w0, sx = w0 * v0.x, sy = w0 * v0.y, sz = w0 * v0.z;
-    for_each_member(P, start, list, nbr, pos_old, cell[i], i, [&](unsigned j) {
+    tile_members(P, start, T, list, nbr, pos_old, cell[i], i, [&](unsigned j) {
         const float4 pj = __ldg(&pos[j]);
         const float d = sqrtf(dist2(pi, pj));
         if (d - P.h <= -P.iz) {
@@ -433,11 +459,16 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
 }
 
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
-                         float dt_over_m, cudaStream_t s) {
+                         float dt_over_m, cudaStream_t s, float *divsum) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
-    k_non_pressure<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
-        predict, dt, dt_over_m);
+    if (divsum)
+        k_non_pressure<true><<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+            P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
+            divsum, predict, dt, dt_over_m);
+    else
+        k_non_pressure<false><<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+            P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
+            nullptr, predict, dt, dt_over_m);
     BBG_PEND(B, s);
 }
 
@@ -459,9 +490,9 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
     BBG_PEND(B, s);
 }
 
-void launch_warm_start(const Params &P, const DevBufs &B, int buf, cudaStream_t s) {
+void launch_warm_start(const Params &P, const DevBufs &B, int buf, float scale, cudaStream_t s) {
     k_warm_start<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.rho, B.pprev,
-                                                                B.press, B.rhostar, B.derr);
+                                                                B.press, B.rhostar, B.derr, scale);
 }
 
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s) {

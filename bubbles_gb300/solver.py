@@ -40,6 +40,8 @@ def desc_from_scene(scene, device=0):
     d.max_iterations = int(scene.get("max_iterations", 20 if mode == "tolerance" else 5))
     d.device = int(device)
     d.pressure_init = {"zero": 0, "previous": 1, "learned": 2}[scene.get("pressure_init", "zero")]
+    d.warm_rule = {"clamp_total": 0, "monotone": 1}[scene.get("warm_rule", "monotone")]
+    d.warm_scale = float(scene.get("warm_scale", 0.0))
     return d
 
 
@@ -75,6 +77,8 @@ class Solver:
         shapes, count = shapes_from_scene(scene)
         N.call("bbg_set_colliders", self.h, shapes, count)
         self.n = 0
+        if scene.get("pressure_init") == "learned" and scene.get("mlp"):
+            self.mlp_configure(**scene["mlp"])
         if pos is not None:
             self.upload(pos, vel)
             if setup:
@@ -267,6 +271,48 @@ class Solver:
             name = names.raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
             out[name] = (ms[i], cnt[i])
         return out, total.value
+
+    # --- learned warm start ----------------------------------------------------
+    def mlp_configure(self, **settings):
+        """(Re)initialise the warm-start MLP; settings override bbg_mlp_desc_default."""
+        d = N.MlpDesc()
+        N.call("bbg_mlp_desc_default", ctypes.byref(d))
+        for k, v in settings.items():
+            setattr(d, k, v)
+        N.call("bbg_mlp_configure", self.h, ctypes.byref(d))
+
+    def mlp_params(self):
+        out = np.zeros(N.MLP_PARAMS, np.float32)
+        N.call("bbg_mlp_get_params", self.h, _fptr(out))
+        return out
+
+    def mlp_set_params(self, theta):
+        a = np.ascontiguousarray(theta, dtype=np.float32).reshape(N.MLP_PARAMS)
+        N.call("bbg_mlp_set_params", self.h, _fptr(a))
+
+    def mlp_set_trained(self, substeps):
+        N.call("bbg_mlp_set_trained", self.h, int(substeps))
+
+    def mlp_status(self):
+        t, s, l = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        N.call("bbg_mlp_status", self.h, ctypes.byref(t), ctypes.byref(s), ctypes.byref(l))
+        return {"trained_substeps": t.value, "adam_steps": s.value, "last_loss": l.value}
+
+    def mlp_infer(self, features):
+        f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 4)
+        out = np.zeros(len(f), np.float32)
+        N.call("bbg_mlp_infer", self.h, _fptr(f), len(f), _fptr(out))
+        return out
+
+    def mlp_train_batch(self, features, targets):
+        f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 4)
+        t = np.ascontiguousarray(targets, dtype=np.float32).reshape(len(f))
+        N.call("bbg_mlp_train_batch", self.h, _fptr(f), _fptr(t), len(f))
+
+    def mlp_features(self):
+        out = np.zeros((self.n, 4), np.float32)
+        N.call("bbg_mlp_get_features", self.h, _fptr(out))
+        return out
 
     def neighbor_counts(self):
         out = np.zeros(self.n, np.int32)

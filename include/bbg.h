@@ -58,6 +58,15 @@ typedef int bbg_status;
 #define BBG_PRESSURE_INIT_PREVIOUS 1
 #define BBG_PRESSURE_INIT_LEARNED 2
 
+/* Pressure update of a warm-started corrector.  MONOTONE (default): the reference update
+ * (negative increments scaled by the negative-pressure scale) from the warm start, which
+ * therefore has to underestimate: warm_scale damps it (0.5 for PREVIOUS and 0.9 for
+ * LEARNED when warm_scale <= 0).  CLAMP_TOTAL: p += delta * err with either sign and the
+ * total clamped like a negative pressure, so an overestimated start can come down; over
+ * long runs it saves few iterations and with LEARNED starts it has diverged. */
+#define BBG_WARM_CLAMP_TOTAL 0
+#define BBG_WARM_MONOTONE 1
+
 #define BBG_SHAPE_BOX 1
 #define BBG_SHAPE_SPHERE 2
 #define BBG_MAX_COLLIDERS 16
@@ -102,6 +111,8 @@ typedef struct {
     double max_density_error_ratio;  /* corrector tolerance (reference: 0.01) */
     int device;                      /* CUDA device ordinal */
     int pressure_init;               /* BBG_PRESSURE_INIT_* (reference: ZERO) */
+    int warm_rule;                   /* BBG_WARM_* for a non-zero pressure_init */
+    double warm_scale;               /* start pressure = warm_scale * estimate; <= 0: default */
 } bbg_solver_desc;
 
 /* Analytic collider shape with a translation-only ObjectToWorld (MakeBox,
@@ -126,6 +137,23 @@ typedef struct {
     int out_of_grid;                  /* particles hashed outside the grid (clamped) */
     double max_force;                 /* max |F| after the last substep (CFL input) */
 } bbg_step_stats;
+
+/* Learned warm start (pressure_init = BBG_PRESSURE_INIT_LEARNED): a per-particle MLP
+ * 4 -> 64 -> 64 -> 1 (GELU, BF16 tensor-core inference with FP32 accumulation) maps
+ * (100 (rho - rho0) / rho0, -100 dt div v, (neighbours - 1) / 32, p_prev / p_unit) to
+ * p / p_unit, p_unit = delta rho0 / 100.  The first train_substeps substeps run the plain
+ * corrector and train the model online (FP32 forward / backward, Adam) on their
+ * (features, converged pressure) pairs; later substeps start the unchanged corrector from
+ * the model's estimate.  No reference counterpart. */
+#define BBG_MLP_PARAMS 4545   /* W1[4][64], b1[64], W2[64][64], b2[64], w3[64], b3 */
+typedef struct {
+    int train_substeps;        /* plain substeps that train the model before it is used (200) */
+    int batch;                 /* training pairs per Adam step (16384) */
+    int steps_per_substep;     /* Adam steps after each training substep (4) */
+    double learning_rate;      /* 1e-3 */
+    double beta1, beta2, epsilon;   /* 0.9, 0.999, 1e-8 */
+    unsigned long long seed;   /* weight initialisation */
+} bbg_mlp_desc;
 
 /* ----- library ----------------------------------------------------------- */
 const char *bbg_version(void);
@@ -180,6 +208,25 @@ bbg_status bbg_advance_time_step(bbg_solver s, double dt, bbg_step_stats *stats)
 bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable);
 /* Read the statistics of the last substep (synchronises). */
 bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
+
+/* ----- learned warm start ---------------------------------------------------- */
+bbg_status bbg_mlp_desc_default(bbg_mlp_desc *desc);
+/* (Re)initialise the model and its training schedule (allocates on first use). */
+bbg_status bbg_mlp_configure(bbg_solver s, const bbg_mlp_desc *desc);
+/* FP32 master parameters, BBG_MLP_PARAMS floats in the layout above. */
+bbg_status bbg_mlp_get_params(bbg_solver s, float *theta);
+bbg_status bbg_mlp_set_params(bbg_solver s, const float *theta);
+/* Substeps already used for training; setting it to train_substeps or more switches a
+ * model loaded with bbg_mlp_set_params straight to inference. */
+bbg_status bbg_mlp_set_trained(bbg_solver s, int trained_substeps);
+bbg_status bbg_mlp_status(bbg_solver s, int *trained_substeps, int *adam_steps, double *last_loss);
+/* Raw network outputs (p / p_unit before the clamp at 0) for n host feature rows
+ * (n x 4 floats), through the tensor-core inference kernel. */
+bbg_status bbg_mlp_infer(bbg_solver s, const float *features, int n, float *out);
+/* One forward / backward / Adam step on a host batch (batch x 4 features, batch targets). */
+bbg_status bbg_mlp_train_batch(bbg_solver s, const float *features, const float *targets, int batch);
+/* Features of the last substep in the caller's particle order (n x 4 floats). */
+bbg_status bbg_mlp_get_features(bbg_solver s, float *out);
 
 /* ----- individual passes (sph_solver.h:124-196, pcisph_solver.h:85-99) ------- */
 bbg_status bbg_update_grid_distribution(bbg_solver s);          /* UpdateGridDistributionGPU */

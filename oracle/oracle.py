@@ -23,7 +23,8 @@ VECTOR_FIELDS = {POSITION, VELOCITY, FORCE, INTERACTION, PRED_POSITION, PRED_VEL
 
 PCISPH_AS_SHIPPED = 0
 PCISPH_TOLERANCE = 1
-PCISPH_WARM = 2
+PCISPH_WARM = 2            # warm start, total pressure clamped
+PCISPH_WARM_MONOTONE = 3   # warm start, reference (non-negative increment) update
 BUCKET = 100
 
 

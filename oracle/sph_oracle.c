@@ -1073,15 +1073,16 @@ int orc_pressure_force_and_integrate(orc_sim *s, double dt_in, double max_err_ra
     Float densityErrorRatio = 0;
     int it = 0;
     s->tol_mode = (mode != ORC_PCISPH_AS_SHIPPED);
+    const int warm = (mode == ORC_PCISPH_WARM || mode == ORC_PCISPH_WARM_MONOTONE);
     s->clamp_total = (mode == ORC_PCISPH_WARM);
-    if (mode == ORC_PCISPH_WARM) {
+    if (warm) {
         /* warm start: keep each particle's pressure from the previous substep, rho* = rho,
          * and predict the first positions from F + Fp(p) instead of F alone */
         for (int i = 0; i < s->n; i++) { s->dpred[i] = s->density[i]; s->derr[i] = 0; }
         parallel_for(s->n, k_pred_force, s);
     }
     for (int k = 0; k < max_it; k++) {
-        pass_ctx pp = {s, k == 0 && mode != ORC_PCISPH_WARM, dt};
+        pass_ctx pp = {s, k == 0 && !warm, dt};
         parallel_for(s->n, k_predict, &pp);
         pass_ctx pr = {s, 0, delta};
         parallel_for(s->n, k_pred_pressure, &pr);
@@ -1179,7 +1180,7 @@ int orc_pcisph_substep(orc_sim *s, double dt, double max_err_ratio, int max_it, 
     orc_compute_particle_interaction(s);
     /* the equation-of-state pressure written here is dead in the corrector (its first
      * prediction zeroes the pressure); the warm start keeps the previous substep's instead */
-    orc_compute_density(s, mode != ORC_PCISPH_WARM);
+    orc_compute_density(s, mode != ORC_PCISPH_WARM && mode != ORC_PCISPH_WARM_MONOTONE);
     orc_compute_non_pressure_force(s);
     double delta = orc_compute_delta(s, dt);
     if (mode == ORC_PCISPH_AS_SHIPPED) { max_err_ratio = 0.01; max_it = 5; }

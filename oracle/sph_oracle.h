@@ -84,8 +84,10 @@ enum {
 };
 
 /* PCISPH corrector modes */
-/* WARM: tolerance mode started from the pressure left by the previous substep. */
-enum { ORC_PCISPH_AS_SHIPPED = 0, ORC_PCISPH_TOLERANCE = 1, ORC_PCISPH_WARM = 2 };
+/* WARM / WARM_MONOTONE: tolerance mode started from the pressure the particles hold
+ * (the previous substep's, or any start set with orc_set_field); WARM lets the pressure
+ * decrease and clamps the total, WARM_MONOTONE keeps the reference update. */
+enum { ORC_PCISPH_AS_SHIPPED = 0, ORC_PCISPH_TOLERANCE = 1, ORC_PCISPH_WARM = 2, ORC_PCISPH_WARM_MONOTONE = 3 };
 
 int      orc_float_bytes(void);
 void     orc_set_threads(int n);

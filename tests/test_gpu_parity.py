@@ -57,22 +57,6 @@ def rel_close(a, b, rtol=RTOL):
     return worst <= rtol, worst
 
 
-@pytest.fixture(scope="module")
-def small():
-    return scenes.small_pcisph()
-
-
-@pytest.fixture(scope="module")
-def moved(gpu, small):
-    """A state after 30 GPU substeps of the small dam break (particles in motion)."""
-    sc, pos = small
-    with bb.Solver(sc, pos=pos) as g:
-        for _ in range(30):
-            g.advance_time_step(sc["dt"])
-        p, v = g.download()
-    return sc, p, v
-
-
 def test_grid_bit_exact_initial(gpu, small):
     sc, pos = small
     g, o = pair(sc, pos)
@@ -290,12 +274,15 @@ def test_full_substep(gpu, moved, mode):
     g.close()
 
 
-def test_warm_started_substeps_match_oracle(gpu, moved):
-    """Corrector started from the previous substep's pressure: each substep, from the
-    GPU's own state (positions, velocities and the carried pressure), matches the oracle
-    run the same way; the warm start never needs more iterations than the zero start."""
+@pytest.mark.parametrize("rule,scale,mode", [("clamp_total", 1.0, O.PCISPH_WARM),
+                                              ("monotone", 0.5, O.PCISPH_WARM_MONOTONE)])
+def test_warm_started_substeps_match_oracle(gpu, moved, rule, scale, mode):
+    """Corrector started from (a multiple of) the previous substep's pressure: each
+    substep, from the GPU's own state (positions, velocities and the carried pressure),
+    matches the oracle run the same way; the warm start never needs more iterations than
+    the zero start."""
     sc, p, v = moved
-    scw = dict(sc, pressure_init="previous")
+    scw = dict(sc, pressure_init="previous", warm_rule=rule, warm_scale=scale)
     g = bb.Solver(scw, pos=p, vel=v)
     gz = bb.Solver(sc, pos=p, vel=v)
     its_w, its_z = [], []
@@ -303,9 +290,9 @@ def test_warm_started_substeps_match_oracle(gpu, moved):
         pg, vg = g.download()
         o = O.OracleSim(scw, pg, vg, variant="f32")
         if its_w:
-            o.set(O.PRESSURE, g.get(bb.FIELD_PRESSURE))
+            o.set(O.PRESSURE, np.float32(scale) * g.get(bb.FIELD_PRESSURE))
         st = g.advance_time_step(sc["dt"], stats=True)
-        it_o, _ = o.pcisph_substep(sc["dt"], 0.01, sc["max_iterations"], O.PCISPH_WARM)
+        it_o, _ = o.pcisph_substep(sc["dt"], 0.01, sc["max_iterations"], mode)
         assert st["iterations"] == it_o
         assert st["max_density_error_ratio"] < 0.01
         pg2, _ = g.download()
