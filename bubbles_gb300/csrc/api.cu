@@ -230,7 +230,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
         CK(mlp_prepare());
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->desc.device));
-        M.infer_blocks = 2 * (sms > 0 ? sms : 1);
+        M.infer_blocks = 4 * (sms > 0 ? sms : 1);   // 4 blocks of 128 threads fit an SM
         M.batch = d.batch;
         s->mlp_alloc = true;
     }
@@ -244,6 +244,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
     CK(cudaMemsetAsync(M.step, 0, sizeof(unsigned), s->stream));
     CK(cudaMemsetAsync(M.loss, 0, sizeof(double), s->stream));
     CK(cudaMemsetAsync(M.feat, 0, sizeof(float4) * (size_t)s->capacity, s->stream));
+    CK(cudaMemsetAsync(M.tail, 0, sizeof(float) * kTail, s->stream));
     launch_mlp_pack(M, s->stream);
     CK_LAUNCH();
     CK(cudaStreamSynchronize(s->stream));
@@ -770,7 +771,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.force, n); ALLOC(B.xstar, n); ALLOC(B.pforce, n); ALLOC(B.smoothed, n);
     ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
     ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
-    ALLOC(B.list, (size_t)(kMaxList / 8) * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
+    ALLOC(B.list, (size_t)kMaxList * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
     ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);

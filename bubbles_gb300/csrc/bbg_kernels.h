@@ -21,8 +21,8 @@ struct DevBufs {
     unsigned *partials;        // scan partials
     uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
     int *nbr;                  // neighbour count of each sorted slot
-    uint4 *list;               // member lists: kMaxList / 8 chunks of 8 16-bit entries
-                               // per particle, chunk-major (list[c * n + i]; tile.cuh)
+    unsigned short *list;      // member lists: kMaxList 16-bit entries per particle,
+                               // member-major (list[q * n + i]; tile.cuh)
     float *inv_rho;            // 1 / density
     float *pprev;              // pressure of the previous substep, in the current order
     StepState *st;

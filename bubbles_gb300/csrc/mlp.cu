@@ -54,6 +54,23 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
+__device__ __forceinline__ __nv_bfloat162 as_bf2(uint32_t v) { return *reinterpret_cast<__nv_bfloat162 *>(&v); }
+__device__ __forceinline__ uint32_t as_u32(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
+
+// GELU (tanh form) of two BF16 values in BF16 arithmetic: 7 paired operations, one of
+// them on the MUFU pipe (tanh.approx.bf16x2).
+__device__ __forceinline__ uint32_t gelu_bf16x2(uint32_t xv) {
+    const __nv_bfloat162 x = as_bf2(xv);
+    const __nv_bfloat162 a = __float2bfloat162_rn(kGeluA), c = __float2bfloat162_rn(kGeluC);
+    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
+    const __nv_bfloat162 ax2 = __hmul2(a, __hmul2(x, x));
+    const __nv_bfloat162 u = __hmul2(c, __hfma2(ax2, x, x));
+    uint32_t t;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(as_u32(u)));
+    const __nv_bfloat162 hx = __hmul2(half, x);
+    return as_u32(__hfma2(hx, as_bf2(t), hx));
+}
+
 __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1) {
     asm volatile(
@@ -90,19 +107,24 @@ __global__ void k_mlp_features(int n, const float4 *__restrict__ vel, const floa
 }
 
 // Tensor-core inference fused with the warm start of the corrector: p = scale * p_unit *
-// max(0, MLP(features)), rho* = rho, err = 0, pos.w = p / rho^2.
+// clamp(MLP(features), 0, largest training target), rho* = rho, err = 0, pos.w = p / rho^2.
+// Layer-2 B fragments live in shared memory (8 KB per block), the layer-1 fragments,
+// bias and w3 in registers; GELU runs in BF16x2 arithmetic.
 __global__ void __launch_bounds__(128)
 k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restrict__ w1f,
                  const uint32_t *__restrict__ w2f, const float *__restrict__ tail, float p_unit, float scale,
                  float4 *__restrict__ pos, const float *__restrict__ rho, float *__restrict__ press,
                  float *__restrict__ rhostar, float *__restrict__ derr, float *__restrict__ raw) {
+    __shared__ uint2 sW2[32 * 32];   // [fragment pair q / 2][lane]
     const int lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
-    uint32_t b1f[8], b2f[64];
+    for (int k = threadIdx.x; k < 32 * 32; k += blockDim.x) {
+        const int qp = k >> 5, l = k & 31;
+        sW2[k] = make_uint2(__ldg(&w2f[(2 * qp) * 32 + l]), __ldg(&w2f[(2 * qp + 1) * 32 + l]));
+    }
+    uint32_t b1f[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) b1f[q] = __ldg(&w1f[q * 32 + lane]);
-#pragma unroll
-    for (int q = 0; q < 64; q++) b2f[q] = __ldg(&w2f[q * 32 + lane]);
     float bias2[16], w3[16];
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {
@@ -112,6 +134,8 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
         w3[2 * nt + 1] = __ldg(&tail[kTailW3 + 8 * nt + 2 * t + 1]);
     }
     const float b3 = __ldg(&tail[kTailB3]);
+    const float ymax = __ldg(&tail[kTailYmax]);
+    __syncthreads();
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16; base < n; base += warps * 16) {
         const int pa = base + g, pb = base + g + 8;
@@ -126,8 +150,8 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
             float c[4] = {0.f, 0.f, 0.f, 0.f};
             mma_bf16(c, a0, a1, 0u, 0u, b1f[nt], 0u);
             const int kc = nt >> 1, hi = nt & 1;
-            h1[kc * 4 + hi * 2 + 0] = pack_bf16(gelu_fast(c[0]), gelu_fast(c[1]));
-            h1[kc * 4 + hi * 2 + 1] = pack_bf16(gelu_fast(c[2]), gelu_fast(c[3]));
+            h1[kc * 4 + hi * 2 + 0] = gelu_bf16x2(pack_bf16(c[0], c[1]));
+            h1[kc * 4 + hi * 2 + 1] = gelu_bf16x2(pack_bf16(c[2], c[3]));
         }
         // layer 2: 16 x 64 times 64 x 64, accumulators start at the bias
         float acc[8][4];
@@ -141,18 +165,21 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
 #pragma unroll
         for (int kc = 0; kc < 4; kc++) {
 #pragma unroll
-            for (int nt = 0; nt < 8; nt++)
-                mma_bf16(acc[nt], h1[kc * 4 + 0], h1[kc * 4 + 1], h1[kc * 4 + 2], h1[kc * 4 + 3],
-                         b2f[(kc * 8 + nt) * 2], b2f[(kc * 8 + nt) * 2 + 1]);
+            for (int nt = 0; nt < 8; nt++) {
+                const uint2 bf = sW2[(kc * 8 + nt) * 32 + lane];
+                mma_bf16(acc[nt], h1[kc * 4 + 0], h1[kc * 4 + 1], h1[kc * 4 + 2], h1[kc * 4 + 3], bf.x, bf.y);
+            }
         }
         // layer 3 on the FP32 pipes: rows g (c0, c1) and g + 8 (c2, c3)
         float ya = 0.f, yb = 0.f;
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
-            ya = fmaf(gelu_fast(acc[nt][0]), w3[2 * nt], ya);
-            ya = fmaf(gelu_fast(acc[nt][1]), w3[2 * nt + 1], ya);
-            yb = fmaf(gelu_fast(acc[nt][2]), w3[2 * nt], yb);
-            yb = fmaf(gelu_fast(acc[nt][3]), w3[2 * nt + 1], yb);
+            const float2 ha = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][0], acc[nt][1]))));
+            const float2 hb = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][2], acc[nt][3]))));
+            ya = fmaf(ha.x, w3[2 * nt], ya);
+            ya = fmaf(ha.y, w3[2 * nt + 1], ya);
+            yb = fmaf(hb.x, w3[2 * nt], yb);
+            yb = fmaf(hb.y, w3[2 * nt + 1], yb);
         }
         ya += __shfl_xor_sync(0xffffffffu, ya, 1);
         ya += __shfl_xor_sync(0xffffffffu, ya, 2);
@@ -163,7 +190,9 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
         if (t < 2 && p_out < n) {
             if (raw) raw[p_out] = y;
             if (press) {
-                const float p = scale * p_unit * fmaxf(y, 0.f);
+                float e = fmaxf(y, 0.f);
+                if (ymax > 0.f) e = fminf(e, ymax);
+                const float p = scale * p_unit * e;
                 const float d = rho[p_out];
                 press[p_out] = p;
                 rhostar[p_out] = d;
@@ -176,10 +205,11 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
 
 // Training pairs of the substep that just converged: features at its start and the
 // converged pressure / p_unit, B particles spread evenly over the slots from a per-step
-// offset.
+// offset; the largest target seen bounds the estimates of inference.
 __global__ void k_mlp_collect(int n, int batch, const unsigned *__restrict__ step,
                               const float4 *__restrict__ feat, const float *__restrict__ press,
-                              float inv_p_unit, float4 *__restrict__ bx, float *__restrict__ bt) {
+                              float inv_p_unit, float4 *__restrict__ bx, float *__restrict__ bt,
+                              float *ymax) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= batch) return;
     const unsigned s = *step;
@@ -187,7 +217,9 @@ __global__ void k_mlp_collect(int n, int batch, const unsigned *__restrict__ ste
     const int i = (int)((off + (unsigned long long)b * (unsigned long long)n / (unsigned long long)batch) %
                         (unsigned long long)n);
     bx[b] = feat[i];
-    bt[b] = press[i] * inv_p_unit;
+    const float y = press[i] * inv_p_unit;
+    bt[b] = y;
+    if (y > 0.f) atomicMax(reinterpret_cast<unsigned *>(ymax), __float_as_uint(y));
 }
 
 // Forward + backward of one 128-sample block; weight gradients reduced in shared memory
@@ -432,7 +464,7 @@ void launch_mlp_train_step(const MlpBufs &M, const float4 *bx, const float *bt, 
 
 void launch_mlp_collect(const Params &P, const DevBufs &B, const MlpBufs &M, float p_unit, cudaStream_t s) {
     k_mlp_collect<<<blocks_for(M.batch, 256), 256, 0, s>>>(P.n, M.batch, M.step, M.feat, B.press,
-                                                           1.f / p_unit, M.bx, M.bt);
+                                                           1.f / p_unit, M.bx, M.bt, M.tail + kTailYmax);
 }
 
 __global__ void k_mlp_get_features(const float4 *__restrict__ feat, const int *__restrict__ slot, float *out,

@@ -16,8 +16,10 @@ constexpr int kOffB2 = kOffW2 + kHid * kHid;
 constexpr int kOffW3 = kOffB2 + kHid;
 constexpr int kOffB3 = kOffW3 + kHid;
 constexpr int kParams = kOffB3 + 1;
-// FP32 tail used by inference: b2 [64], w3 [64] (rounded to BF16), b3
-constexpr int kTailB2 = 0, kTailW3 = kHid, kTailB3 = 2 * kHid, kTail = 2 * kHid + 1;
+// FP32 tail used by inference: b2 [64], w3 [64] (rounded to BF16), b3, and the largest
+// training target (estimates are clamped to it; 0 = no bound)
+constexpr int kTailB2 = 0, kTailW3 = kHid, kTailB3 = 2 * kHid, kTailYmax = 2 * kHid + 1;
+constexpr int kTail = 2 * kHid + 2;
 
 struct MlpBufs {
     float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;   // kParams each

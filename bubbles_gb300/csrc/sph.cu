@@ -25,6 +25,11 @@ namespace bbg {
 
 constexpr int kThreads = kTile;
 
+// a neighbour's position and velocity records
+struct PosVel {
+    float4 p, v;
+};
+
 static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // True when some corrector iteration before k already met the tolerance
@@ -40,10 +45,10 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
 // ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
 // Tests every candidate of the 27 cells exactly once per substep and records the
 // neighbour set (the reference bucket, grid.h:423-447) as a compact member list.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 12)
 k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
-          float *__restrict__ press, int *__restrict__ nbr, uint4 *__restrict__ list,
+          float *__restrict__ press, int *__restrict__ nbr, unsigned short *__restrict__ list,
           int compute_pressure, StepState *st) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
@@ -54,8 +59,8 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     const size_t n = (size_t)P.n;
     float sum = 0.f;
     int cnt = 0;      // bucket members, i included
+    int listed = 0;   // members other than i
     bool fits = true;
-    ChunkWriter w;    // members other than i
     tile_candidates_coded(P.g, start, T, cw & ~kWide, &fits, [&](unsigned j, unsigned base) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
@@ -63,10 +68,12 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
             const float x = 1.f - r2 * P.inv_h2;
             sum += x * x * x;
             cnt++;
-            if (j != (unsigned)i) w.push(list, n, (unsigned)i, j + base);
+            if (j != (unsigned)i) {
+                if (listed < kMaxList) list[(size_t)listed * n + (size_t)i] = (unsigned short)(j + base);
+                listed++;
+            }
         }
     });
-    w.finish(list, n, (unsigned)i);
     const float di = sum * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
@@ -79,7 +86,7 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     inv_rho[i] = ir;
     reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
     nbr[i] = cnt;
-    if (w.count > kMaxList || !fits) cell[i] = cw | kWide;
+    if (listed > kMaxList || !fits) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
@@ -91,7 +98,7 @@ template <bool DIV>
 __global__ void __launch_bounds__(kThreads)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
-               const unsigned *__restrict__ start, const uint4 *__restrict__ list, const int *__restrict__ nbr,
+               const unsigned *__restrict__ start, const unsigned short *__restrict__ list, const int *__restrict__ nbr,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
                float *__restrict__ press, float *__restrict__ divsum, int predict, float dt, float dt_over_m) {
     __shared__ TileMap T;
@@ -105,23 +112,25 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     float fz = P.mass * P.gz - P.drag * vi.z;
     float dv = 0.f;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
-    tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
-        const float4 pj = __ldg(&pos[j]);
-        const float r2 = dist2(pi, pj);
-        const float inv_d = rsqrtf(r2);
-        const float d = r2 * inv_d;
-        const float4 vj = __ldg(&vel[j]);   // vj.w = 1 / rho_j
-        const float x = 1.f - d * P.inv_h;
-        const float w = kv * x * vj.w;
-        fx += (vj.x - vi.x) * w;
-        fy += (vj.y - vi.y) * w;
-        fz += (vj.z - vi.z) * w;
-        if (DIV && r2 > 0.f) {
-            const float dot = (vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) +
-                              (vj.z - vi.z) * (pj.z - pi.z);
-            dv += vj.w * x * x * inv_d * dot;
-        }
-    });
+    tile_members<(kGatherBatch < 4 ? kGatherBatch : 4)>(
+        P, start, T, list, nbr, pos, cell[i], i,
+        [&](unsigned j) { return PosVel{__ldg(&pos[j]), __ldg(&vel[j])}; },
+        [&](const PosVel &nb) {
+            const float4 pj = nb.p, vj = nb.v;   // vj.w = 1 / rho_j
+            const float r2 = dist2(pi, pj);
+            const float inv_d = rsqrtf(r2);
+            const float d = r2 * inv_d;
+            const float x = 1.f - d * P.inv_h;
+            const float w = kv * x * vj.w;
+            fx += (vj.x - vi.x) * w;
+            fy += (vj.y - vi.y) * w;
+            fz += (vj.z - vi.z) * w;
+            if (DIV && r2 > 0.f) {
+                const float dot = (vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) +
+                                  (vj.z - vi.z) * (pj.z - pi.z);
+                dv += vj.w * x * x * inv_d * dot;
+            }
+        });
     force[i] = make_float4(fx, fy, fz, 0.f);
     if (DIV) divsum[i] = dv;
     if (predict) {
@@ -186,7 +195,7 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
 __global__ void __launch_bounds__(kThreads)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const uint4 *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
+               const unsigned short *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
                float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
                float delta, int clamp_total) {
     // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
@@ -200,14 +209,15 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     if (i < P.n) {
         const float4 xi = xstar[i];
         float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
-        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
-            const float4 xj = __ldg(&xstar[j]);
-            const float r2 = dist2(xi, xj);
-            if (r2 < P.h2mz) {
-                const float x = 1.f - r2 * P.inv_h2;
-                sum += x * x * x;
-            }
-        });
+        tile_members(
+            P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&xstar[j]); },
+            [&](const float4 xj) {
+                const float r2 = dist2(xi, xj);
+                if (r2 < P.h2mz) {
+                    const float x = 1.f - r2 * P.inv_h2;
+                    sum += x * x * x;
+                }
+            });
         const float density = sum * P.std_c * P.mass;
         float err = density - P.target_density;
         float pr = delta * err;
@@ -253,7 +263,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
 __global__ void __launch_bounds__(kThreads)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+                 const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
@@ -271,20 +281,21 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
         const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
-        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
-            const float4 pj = __ldg(&pos[j]);   // pj.w = p_j / rho*_j^2
-            const float r2 = dist2(pi, pj);
-            const float inv_d = rsqrtf(r2);
-            const float d = r2 * inv_d;
-            // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
-            if (d - P.h <= -P.iz && d >= P.iz) {
-                const float x = 1.f - d * P.inv_h;
-                const float c = kg * (ai + pj.w) * x * x * inv_d;
-                tx += (pj.x - pi.x) * c;
-                ty += (pj.y - pi.y) * c;
-                tz += (pj.z - pi.z) * c;
-            }
-        });
+        tile_members(
+            P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&pos[j]); },
+            [&](const float4 pj) {   // pj.w = p_j / rho*_j^2
+                const float r2 = dist2(pi, pj);
+                const float inv_d = rsqrtf(r2);
+                const float d = r2 * inv_d;
+                // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
+                if (d - P.h <= -P.iz && d >= P.iz) {
+                    const float x = 1.f - d * P.inv_h;
+                    const float c = kg * (ai + pj.w) * x * x * inv_d;
+                    tx += (pj.x - pi.x) * c;
+                    ty += (pj.y - pi.y) * c;
+                    tz += (pj.z - pi.z) * c;
+                }
+            });
         const v3 fp = V(-tx, -ty, -tz);
         pforce[i] = F4(fp);
         const v3 f = V(force[i]);
@@ -327,7 +338,7 @@ __global__ void k_corrector_control(Params P, StepState *st, int max_it,
 __global__ void __launch_bounds__(kThreads)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-             const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+             const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
@@ -343,26 +354,28 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
         const float kv = P.visc_m2 * P.spiky_d2w_c;
-        tile_members(P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) {
-            const float4 pj = __ldg(&pos[j]);
-            const float r2 = dist2(pi, pj);
-            const float inv_d = rsqrtf(r2);
-            const float d = r2 * inv_d;
-            if (d - P.h <= -P.iz) {
-                const float x = 1.f - d * P.inv_h;
-                if (d >= P.iz) {
-                    const float c = kg * (ai + pj.w) * x * x * inv_d;
-                    tx += (pj.x - pi.x) * c;
-                    ty += (pj.y - pi.y) * c;
-                    tz += (pj.z - pi.z) * c;
+        tile_members<(kGatherBatch < 4 ? kGatherBatch : 4)>(
+            P, start, T, list, nbr, pos, cell[i], i,
+            [&](unsigned j) { return PosVel{__ldg(&pos[j]), __ldg(&vel[j])}; },
+            [&](const PosVel &nb) {
+                const float4 pj = nb.p, vj = nb.v;   // vj.w = 1 / rho_j
+                const float r2 = dist2(pi, pj);
+                const float inv_d = rsqrtf(r2);
+                const float d = r2 * inv_d;
+                if (d - P.h <= -P.iz) {
+                    const float x = 1.f - d * P.inv_h;
+                    if (d >= P.iz) {
+                        const float c = kg * (ai + pj.w) * x * x * inv_d;
+                        tx += (pj.x - pi.x) * c;
+                        ty += (pj.y - pi.y) * c;
+                        tz += (pj.z - pi.z) * c;
+                    }
+                    const float w = kv * x * vj.w;
+                    fx += (vj.x - vi.x) * w;
+                    fy += (vj.y - vi.y) * w;
+                    fz += (vj.z - vi.z) * w;
                 }
-                const float4 vj = __ldg(&vel[j]);   // vj.w = 1 / rho_j
-                const float w = kv * x * vj.w;
-                fx += (vj.x - vi.x) * w;
-                fy += (vj.y - vi.y) * w;
-                fz += (vj.z - vi.z) * w;
-            }
-        });
+            });
         const v3 f = V(fx - tx, fy - ty, fz - tz);
         force[i] = F4(f);
         v3 x = V(pi), v = V(vi);
@@ -410,7 +423,7 @@ __global__ void __launch_bounds__(kThreads)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
                const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const uint4 *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
+               const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * kTile + threadIdx.x;
@@ -420,19 +433,21 @@ k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__res
     const float w0 = P.mass * __ldg(&inv_rho[i]) * P.spiky_w_c;
     const float4 v0 = vel[i];
     float ws = w0, sx = w0 * v0.x, sy = w0 * v0.y, sz = w0 * v0.z;
-    tile_members(P, start, T, list, nbr, pos_old, cell[i], i, [&](unsigned j) {
-        const float4 pj = __ldg(&pos[j]);
-        const float d = sqrtf(dist2(pi, pj));
-        if (d - P.h <= -P.iz) {
-            const float x = 1.f - d * P.inv_h;
-            const float wj = P.mass * __ldg(&inv_rho[j]) * (P.spiky_w_c * x * x * x);
-            const float4 vj = __ldg(&vel[j]);
-            ws += wj;
-            sx += wj * vj.x;
-            sy += wj * vj.y;
-            sz += wj * vj.z;
-        }
-    });
+    tile_members(
+        P, start, T, list, nbr, pos_old, cell[i], i, [&](unsigned j) { return j; },
+        [&](unsigned j) {
+            const float4 pj = __ldg(&pos[j]);
+            const float d = sqrtf(dist2(pi, pj));
+            if (d - P.h <= -P.iz) {
+                const float x = 1.f - d * P.inv_h;
+                const float wj = P.mass * __ldg(&inv_rho[j]) * (P.spiky_w_c * x * x * x);
+                const float4 vj = __ldg(&vel[j]);
+                ws += wj;
+                sx += wj * vj.x;
+                sy += wj * vj.y;
+                sz += wj * vj.z;
+            }
+        });
     if (ws > 0.f) {
         const float inv = 1.f / ws;
         sx *= inv; sy *= inv; sz *= inv;

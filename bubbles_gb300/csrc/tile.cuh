@@ -8,12 +8,12 @@
 // as (r << 12) | (j - lo[r]); every pass rebuilds the tile's 9 range starts from the
 // grid (two loads per range) and decodes j = lo[r] + offset.
 //
-// Lists are chunk-major, 8 entries per 16-byte chunk: entry q of particle i is half-word
-// q % 8 of list[(q / 8) * n + i], so a warp reads chunk c of 32 particles in one
-// coalesced 512-byte load and a particle's usual 2-4 chunks are all requested before
-// any neighbour is gathered.  A particle with more than kMaxList members, or with a
-// member more than 4,095 slots into its range, is "wide" (kWide in its cell word) and
-// re-tests its 27 cells exactly on every pass instead.
+// Lists are member-major, one 16-bit entry per member: entry q of particle i is
+// list[q * n + i], so the density pass writes entry q of 32 particles with one
+// coalesced 64-byte store and the later passes read them the same way, eight entries
+// requested before any neighbour is gathered.  A particle with more than kMaxList
+// members, or with a member more than 4,095 slots into its range, is "wide" (kWide in its
+// cell word) and re-tests its 27 cells exactly on every pass instead.
 #pragma once
 
 #include "bbg_internal.cuh"
@@ -21,6 +21,11 @@
 namespace bbg {
 
 constexpr int kTile = 128;          // slots per tile = threads per block of a neighbour pass
+#ifndef BBG_GATHER_BATCH
+#define BBG_GATHER_BATCH 4
+#endif
+// members whose neighbour records are requested together (build-time tuning knob)
+constexpr int kGatherBatch = BBG_GATHER_BATCH;
 constexpr int kOffBits = 12;
 constexpr int kOffLimit = 1 << kOffBits;
 
@@ -70,8 +75,8 @@ __device__ __forceinline__ void tile_candidates(const GridDev &g, const unsigned
     }
 }
 
-// Same visit order, for the density pass: f(j, base) with the list entry of j equal to
-// j + base; *fits turns false when a range reaches past the 12-bit offset limit.
+// Same visit order, for the density pass: f(j, base) with the list entry of slot j equal
+// to j + base; *fits turns false when a range reaches past the 12-bit offset limit.
 template <class F>
 __device__ __forceinline__ void tile_candidates_coded(const GridDev &g, const unsigned *__restrict__ start,
                                                       const TileMap &T, unsigned c, bool *fits, F &&f) {
@@ -103,71 +108,40 @@ __device__ __forceinline__ unsigned list_slot(const TileMap &T, unsigned e) {
     return (unsigned)T.lo[e >> kOffBits] + (e & (kOffLimit - 1));
 }
 
-// Builds a particle's list in registers and stores each full chunk with one 16-byte
-// store (a warp writes 512 contiguous bytes per chunk).
-struct ChunkWriter {
-    unsigned long long a = 0ull, b = 0ull;   // entries 0-3 and 4-7 of the open chunk
-    int count = 0;                           // entries pushed (stores stop at kMaxList)
-    __device__ __forceinline__ void store(uint4 *list, size_t n, unsigned i, int chunk) {
-        list[(size_t)chunk * n + i] = make_uint4((unsigned)a, (unsigned)(a >> 32), (unsigned)b,
-                                                 (unsigned)(b >> 32));
-        a = b = 0ull;
-    }
-    __device__ __forceinline__ void push(uint4 *list, size_t n, unsigned i, unsigned e) {
-        const int p = count & 7;
-        const unsigned long long v = (unsigned long long)e << ((p & 3) * 16);
-        if (p < 4) a |= v;
-        else b |= v;
-        if (p == 7 && count < kMaxList) store(list, n, i, count >> 3);
-        count++;
-    }
-    __device__ __forceinline__ void finish(uint4 *list, size_t n, unsigned i) {
-        if ((count & 7) != 0 && count < kMaxList) store(list, n, i, count >> 3);
-    }
-};
-
-template <class F>
-__device__ __forceinline__ void list_chunk(const TileMap &T, uint4 w, int m, F &f) {
-    f(list_slot(T, w.x & 0xffffu));
-    if (m > 1) f(list_slot(T, w.x >> 16));
-    if (m > 2) f(list_slot(T, w.y & 0xffffu));
-    if (m > 3) f(list_slot(T, w.y >> 16));
-    if (m > 4) f(list_slot(T, w.z & 0xffffu));
-    if (m > 5) f(list_slot(T, w.z >> 16));
-    if (m > 6) f(list_slot(T, w.w & 0xffffu));
-    if (m > 7) f(list_slot(T, w.w >> 16));
-}
-
-// f(j) for every member j != i of particle i's step-start neighbour set; wide particles
-// re-test their candidates with the exact membership test at the step-start positions.
-template <class F>
+// For every member j != i of particle i's step-start neighbour set: use(fetch(j)).
+// Members are processed NB at a time: the NB list entries and then the NB neighbour
+// records are requested before any is used (entries past the end fetch particle i
+// itself and are not used).  Wide particles re-test their candidates with the
+// exact membership test at the step-start positions pos0.
+template <int NB = kGatherBatch, class Fetch, class Use>
 __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__restrict__ start,
-                                             const TileMap &T, const uint4 *__restrict__ list,
+                                             const TileMap &T, const unsigned short *__restrict__ list,
                                              const int *__restrict__ nbr, const float4 *__restrict__ pos0,
-                                             unsigned cellw, int i, F &&f) {
+                                             unsigned cellw, int i, Fetch &&fetch, Use &&use) {
     if (cellw & kWide) {
         const float4 pi = __ldg(&pos0[i]);
         tile_candidates(P.g, start, cellw & ~kWide, [&](unsigned j, int) {
             if (j == (unsigned)i) return;
             const float4 pj = __ldg(&pos0[j]);
-            if (std_member(P, pi, pj, dist2(pi, pj))) f(j);
+            if (std_member(P, pi, pj, dist2(pi, pj))) use(fetch(j));
         });
         return;
     }
     const int cnt = __ldg(&nbr[i]) - 1;   // members other than i
     const size_t n = (size_t)P.n;
-    const uint4 *l = list + i;
-    // request the first four chunks (32 members) before gathering any neighbour
-    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-    const uint4 w0 = cnt > 0 ? __ldg(l) : z;
-    const uint4 w1 = cnt > 8 ? __ldg(l + n) : z;
-    const uint4 w2 = cnt > 16 ? __ldg(l + 2 * n) : z;
-    const uint4 w3 = cnt > 24 ? __ldg(l + 3 * n) : z;
-    if (cnt > 0) list_chunk(T, w0, cnt, f);
-    if (cnt > 8) list_chunk(T, w1, cnt - 8, f);
-    if (cnt > 16) list_chunk(T, w2, cnt - 16, f);
-    if (cnt > 24) list_chunk(T, w3, cnt - 24, f);
-    for (int q = 32; q < cnt; q += 8) list_chunk(T, __ldg(l + (size_t)(q >> 3) * n), cnt - q, f);
+    const unsigned short *l = list + i;
+    for (int q = 0; q < cnt; q += NB) {
+        unsigned j[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++)
+            j[k] = q + k < cnt ? list_slot(T, __ldg(&l[(size_t)(q + k) * n])) : (unsigned)i;
+        decltype(fetch(0u)) d[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) d[k] = fetch(j[k]);
+#pragma unroll
+        for (int k = 0; k < NB; k++)
+            if (q + k < cnt) use(d[k]);
+    }
 }
 
 }  // namespace bbg

@@ -32,15 +32,27 @@ def bf16(x):
     return r.astype(np.uint32).view(np.float32)
 
 
+def gelu_bf16(x):
+    """GELU of BF16 values in BF16 arithmetic, rounding after every operation as the
+    inference kernel's paired BF16 instructions do (the fused multiply-add rounds once)."""
+    a, c, half = bf16(np.float32(GELU_A)), bf16(np.float32(GELU_C)), np.float32(0.5)
+    x = bf16(x)
+    ax2 = bf16(a * bf16(x * x))
+    u = bf16(c * bf16(ax2.astype(np.float64) * x + x))
+    t = bf16(np.tanh(u.astype(np.float64)).astype(np.float32))
+    hx = bf16(half * x)
+    return bf16((hx.astype(np.float64) * t + hx).astype(np.float32))
+
+
 def forward_bf16(theta, x):
-    """What the inference kernel computes: BF16 inputs, weights and first-layer
-    activations, FP32 accumulation, FP32 second-layer activations, BF16 w3."""
+    """What the inference kernel computes: BF16 inputs and weights, FP32 accumulation,
+    BF16 GELU of both hidden layers, BF16 w3 and an FP32 output dot product."""
     w1, b1, w2, b2, w3, b3 = unpack(theta)
     x = bf16(np.asarray(x, np.float32)).astype(np.float64)
-    z1 = x @ bf16(w1).astype(np.float64) + bf16(b1).astype(np.float64)
-    h1 = bf16(gelu(z1).astype(np.float32)).astype(np.float64)
-    z2 = h1 @ bf16(w2).astype(np.float64) + b2.astype(np.float64)
-    h2 = gelu(z2)
+    z1 = (x @ bf16(w1).astype(np.float64) + bf16(b1).astype(np.float64)).astype(np.float32)
+    h1 = gelu_bf16(z1).astype(np.float64)
+    z2 = (h1 @ bf16(w2).astype(np.float64) + b2.astype(np.float64)).astype(np.float32)
+    h2 = gelu_bf16(z2).astype(np.float64)
     return (h2 @ bf16(w3).astype(np.float64) + float(b3)).astype(np.float32)
 
 
