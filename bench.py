@@ -200,13 +200,19 @@ def run_reference(args, scene, pos):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    block = scene["block"]
-    # size the per-step sample so the whole run stays within ~150 s of CPU time
-    probe = slab(pos, block, 8)
-    rate, _, _, _ = cpu_oracle_rate(scene, probe, None, 0.0, threads, max_steps=1)
-    per_step_budget = 150.0 / max(1, args.prep + args.steps + args.warmup)
-    depth = int(np.clip((per_step_budget * rate) / (block[0] * block[1]) // 8 * 8, 8, block[2]))
-    sample = slab(pos, block, depth)
+    if scene.get("batch"):
+        # the reference has no batching: it would run the scenes one after the other; the
+        # sample is the median-size scene
+        scene, sample, _, what = cpu_sample(scene, pos, None, 0)
+    else:
+        block = scene["block"]
+        # size the per-step sample so the whole run stays within ~150 s of CPU time
+        probe = slab(pos, block, 8)
+        rate, _, _, _ = cpu_oracle_rate(scene, probe, None, 0.0, threads, max_steps=1)
+        per_step_budget = 150.0 / max(1, args.prep + args.steps + args.warmup)
+        depth = int(np.clip((per_step_budget * rate) / (block[0] * block[1]) // 8 * 8, 8, block[2]))
+        sample = slab(pos, block, depth)
+        what = "%d-layer slab of the dam-break block" % depth
     from oracle import oracle as O
     sim = O.OracleSim(scene, sample, None, variant="f32", threads=threads)
     for _ in range(args.prep + args.warmup):
@@ -221,9 +227,9 @@ def run_reference(args, scene, pos):
         iters += it
     sim.close()
     value = len(sample) * args.steps / t
-    desc = ("%d-layer slab (%d particles) of the dam-break block, one tolerance-mode substep "
-            "per step after %d preparation and %d warm-up substeps, %.2f corrector iterations "
-            "per substep" % (depth, len(sample), args.prep, args.warmup, iters / max(1, args.steps)))
+    desc = ("%s (%d particles), one tolerance-mode substep per step after %d preparation and "
+            "%d warm-up substeps, %.2f corrector iterations per substep"
+            % (what, len(sample), args.prep, args.warmup, iters / max(1, args.steps)))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
@@ -238,6 +244,39 @@ def run_reference(args, scene, pos):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def make_solver(bb, scene, pos, device):
+    """The solver of a configuration: one scene, or a batch of scenes (`pos` a list)."""
+    if scene.get("batch"):
+        return bb.BatchSolver(scene, scene["boxes"], pos, device=device)
+    return bb.Solver(scene, pos=pos, device=device)
+
+
+def one_scene(scene, pos, index):
+    """Scene `index` of a batch as a single-scene configuration (its own container)."""
+    lo, hi = scene["boxes"][index]
+    ext = tuple(float(b - a) for a, b in zip(lo, hi))
+    center = tuple(float(a + b) / 2 for a, b in zip(lo, hi))
+    sc = dict(scene, domain_min=tuple(lo), domain_max=tuple(hi), batch=False,
+              colliders=[{"type": "box", "size": ext, "center": center, "reverse": True}])
+    return sc, pos[index]
+
+
+def cpu_sample(scene, pos, vel, depth):
+    """Bounded CPU sample: the first `depth` z-layers of the lattice block, or for a batch
+    the scene whose size is the median of the batch."""
+    if scene.get("batch"):
+        sizes = [len(p) for p in pos]
+        k = int(np.argsort(sizes)[len(sizes) // 2])
+        sc, p = one_scene(scene, pos, k)
+        v = vel[k] if vel is not None else None
+        return sc, p, v, "scene %d of the batch (%d particles)" % (k, len(p))
+    block = scene["block"]
+    if depth >= block[2]:
+        return scene, pos, vel, "the whole block"
+    return (scene, slab(pos, block, depth), slab(vel, block, depth) if vel is not None else None,
+            "a %d-layer slab of the block" % depth)
 
 
 def launches_per_substep(scene, variant, iters):
@@ -279,14 +318,14 @@ def run_ours(args, scene, pos):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dist = init_dist(world, "nccl")
-    n = len(pos)
+    n = sum(len(p) for p in pos) if scene.get("batch") else len(pos)
     dt = scene["dt"]
     variant = args.variant
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     warm = variant != "plain"
     with torch.cuda.stream(stream):
-        g = bb.Solver(scene, pos=pos, device=local)
+        g = make_solver(bb, scene, pos, local)
         g.set_stream(stream)
         # the first `prep` substeps of the run: plain corrector; the learned variant trains
         # its model on their (features, converged pressure) pairs
@@ -325,8 +364,9 @@ def run_ours(args, scene, pos):
         # the plain corrector on the same substeps, for the learned / warm comparison
         plain = None
         if warm and not args.no_plain:
-            gp = bb.Solver(dict(scene, pressure_init="zero"), pos=snap_p, vel=snap_v, device=local)
+            gp = make_solver(bb, dict(scene, pressure_init="zero"), pos, local)
             gp.set_stream(stream)
+            restore(gp, False)
             for _ in range(3):
                 gp.advance_time_step(dt)
             restore(gp, False)
@@ -388,6 +428,7 @@ def run_ours(args, scene, pos):
         e2e_value, _, _ = aggregate(dist, float(n * args.steps), e2e_s)
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
+        batch_offsets = g.layout() if scene.get("batch") else None
         g.close()
 
     if rank != 0:
@@ -419,17 +460,21 @@ def run_ours(args, scene, pos):
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        block = scene["block"]
-        depth = args.cpu_slab
-        sample_p = slab(final_pos, block, depth) if depth < block[2] else final_pos
-        sample_v = slab(final_vel, block, depth) if depth < block[2] else final_vel
-        rate, steps_c, iters_c, t_c = cpu_oracle_rate(scene, sample_p.astype(np.float64),
-                                                      sample_v.astype(np.float64),
+        if scene.get("batch"):
+            cuts = np.cumsum([len(p) for p in pos])[:-1]
+            fp, fv = np.split(final_pos, cuts), np.split(final_vel, cuts)
+            # the e2e buffers hold packed coordinates: take each scene back out
+            fp = [a - batch_offsets[i].astype(np.float32) for i, a in enumerate(fp)]
+        else:
+            fp, fv = final_pos, final_vel
+        sc_c, sample_p, sample_v, what = cpu_sample(scene, fp, fv, args.cpu_slab)
+        rate, steps_c, iters_c, t_c = cpu_oracle_rate(sc_c, np.asarray(sample_p, np.float64),
+                                                      np.asarray(sample_v, np.float64),
                                                       args.cpu_budget, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": ("%d substep(s) (%.1f s, %.2f corrector iterations each) of a %d-particle "
-                          "slab of the same dam-break state, FP32 oracle, plain corrector, %d threads"
-                          % (steps_c, t_c, iters_c / max(1, steps_c), len(sample_p), threads))}
+               "sample": ("%d substep(s) (%.1f s, %.2f corrector iterations each) of %s "
+                          "(%d particles) from the same state, FP32 oracle, plain corrector, %d threads"
+                          % (steps_c, t_c, iters_c / max(1, steps_c), what, len(sample_p), threads))}
 
     per_kernel = {k: {"ms_total": v[0], "launches": v[1], "avg_us": 1e3 * v[0] / max(1, v[1])}
                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}

@@ -66,6 +66,12 @@ class MlpDesc(ctypes.Structure):
                 ("seed", ctypes.c_ulonglong)]
 
 
+class SceneDesc(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int),
+                ("box_min", ctypes.c_double * 3),
+                ("box_max", ctypes.c_double * 3)]
+
+
 class Shape(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("reverse", ctypes.c_int),
                 ("center", ctypes.c_double * 3), ("size", ctypes.c_double * 3),
@@ -146,6 +152,12 @@ SIGNATURES = {
     "bbg_profiler_enable": [_P, _I],
     "bbg_use_cuda_graphs": [_P, _I],
     "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P],
+    "bbg_batch_create": [ctypes.POINTER(SolverDesc), ctypes.POINTER(SceneDesc), _I, ctypes.POINTER(_P)],
+    "bbg_batch_scene_count": [_P, _IP],
+    "bbg_batch_layout": [_P, _DP],
+    "bbg_batch_upload": [_P, _FP, _FP],
+    "bbg_batch_download": [_P, _FP, _FP],
+    "bbg_batch_scene_stats": [_P, _IP, _DP],
     "bbg_mlp_desc_default": [ctypes.POINTER(MlpDesc)],
     "bbg_mlp_configure": [_P, ctypes.POINTER(MlpDesc)],
     "bbg_mlp_get_params": [_P, _FP],

@@ -37,6 +37,12 @@ struct ShapeDev {
     float friction;
 };
 
+// Corrector state of one scene of a batch.
+struct SceneState {
+    unsigned err_bits[kMaxIterations];   // max |density error| of each iteration
+    double err_sum[kMaxIterations];      // sum |density error| of each iteration (FP64)
+};
+
 // Scalars every pass needs; passed by value as a kernel parameter.
 struct Params {
     GridDev g;
@@ -61,6 +67,12 @@ struct Params {
     float rest_c1_int;   // (float)(-1.0 - 0.6): integrate restitution term
     float rest_int;      // (float)0.6
     float max_err_ratio; // corrector tolerance (float, as the reference compares)
+    // batch of independent scenes stacked along z (nscenes = 0: one scene)
+    int nscenes;
+    const float *scene_zb;          // nscenes region starts along z (scene_zb[0] = -FLT_MAX)
+    const ShapeDev *scene_box;      // container box of each scene
+    SceneState *scene_st;           // per-scene corrector state (reset each substep)
+    unsigned short *scene;          // scene of each sorted slot (density pass)
 };
 
 // Per-substep device scalars (reset each substep).
@@ -302,22 +314,22 @@ __device__ __forceinline__ bool clearly_clear(const ShapeDev &s, v3 p, float r) 
 // point and IsInside (two more distance evaluations); Shape::ClosestDistance equals the
 // closest-point query's signed distance bit for bit for boxes and spheres, so one query
 // per shape gives the same answer.
-__device__ __forceinline__ void resolve_collision(const Params &P, float r, float rc1, v3 *pos,
-                                                  v3 *vel) {
-    if (P.nshapes <= 0) return;
+__device__ __forceinline__ void resolve_against(const Params &P, const ShapeDev *shapes, int nshapes, float r,
+                                                float rc1, v3 *pos, v3 *vel) {
+    if (nshapes <= 0) return;
     bool all_clear = true;
-    for (int i = 0; i < P.nshapes; i++) all_clear = all_clear && clearly_clear(P.shapes[i], *pos, P.radius);
+    for (int i = 0; i < nshapes; i++) all_clear = all_clear && clearly_clear(shapes[i], *pos, P.radius);
     if (all_clear) return;
     int target = -1;
     float minD = 3.402823466e+38f;   // Infinity = FLT_MAX
     Cpq q;
-    for (int i = 0; i < P.nshapes; i++) {
-        const Cpq qi = shape_closest_point(P.shapes[i], *pos, P.iz, P.iz6);
+    for (int i = 0; i < nshapes; i++) {
+        const Cpq qi = shape_closest_point(shapes[i], *pos, P.iz, P.iz6);
         const float d = fabsf(qi.sd);
         if (d < minD) { target = i; minD = d; q = qi; }
     }
     if (target < 0) return;
-    const ShapeDev &s = P.shapes[target];
+    const ShapeDev &s = shapes[target];
     const bool inside = (s.reverse != 0) == !(q.sd < 0.f);
     if (!(inside || minD < P.radius)) return;
     v3 n = q.normal;
@@ -341,6 +353,28 @@ __device__ __forceinline__ void resolve_collision(const Params &P, float r, floa
 }
 
 // TimeIntegrationFor, src/equations/sph_equations3.cpp:283-339 (extended = 0).
+// Scene of a batch whose region along z holds z (binary search over the region starts).
+__device__ __forceinline__ int scene_of(const Params &P, float z) {
+    int lo = 0, hi = P.nscenes;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&P.scene_zb[mid]) <= z) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ColliderSet3::ResolveCollision over the scene's colliders: the global shapes of a
+// single scene, or the container box of the particle's scene in a batch.
+__device__ __forceinline__ void resolve_collision(const Params &P, float r, float rc1, v3 *pos, v3 *vel) {
+    if (P.nscenes > 0) {
+        const ShapeDev box = P.scene_box[scene_of(P, pos->z)];
+        resolve_against(P, &box, 1, r, rc1, pos, vel);
+        return;
+    }
+    resolve_against(P, P.shapes, P.nshapes, r, rc1, pos, vel);
+}
+
 __device__ __forceinline__ void integrate_particle(const Params &P, float dt, v3 f, v3 *pos, v3 *vel) {
     v3 aFi = vdiv(f, P.mass);
     v3 at = vadd(V(0.f, 0.f, 0.f), aFi);

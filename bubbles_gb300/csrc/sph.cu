@@ -42,6 +42,17 @@ __device__ __forceinline__ bool converged_before(const Params &P, const StepStat
     return false;
 }
 
+// Batch: true when scene s met the tolerance at an iteration before k (its particles
+// are integrated and skip the rest of the corrector).
+__device__ __forceinline__ bool scene_converged_before(const Params &P, int s, int k) {
+    const SceneState &ss = P.scene_st[s];
+    for (int q = 0; q < k; q++) {
+        float e = __uint_as_float(ss.err_bits[q]);
+        if (fdv(e, P.target_density) < P.max_err_ratio) return true;
+    }
+    return false;
+}
+
 // ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
 // Tests every candidate of the 27 cells exactly once per substep and records the
 // neighbour set (the reference bucket, grid.h:423-447) as a compact member list.
@@ -86,6 +97,7 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     inv_rho[i] = ir;
     reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
     nbr[i] = cnt;
+    if (P.nscenes > 0) P.scene[i] = (unsigned short)scene_of(P, pi.z);
     if (listed > kMaxList || !fits) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
@@ -206,7 +218,12 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * kTile + threadIdx.x;
     float aerr = 0.f;
-    if (i < P.n) {
+    int sc = -1;   // batch: scene of particle i while its corrector still runs
+    if (i < P.n && P.nscenes > 0) {
+        sc = P.scene[i];
+        if (scene_converged_before(P, sc, k)) sc = -2;
+    }
+    if (i < P.n && sc != -2) {
         const float4 xi = xstar[i];
         float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
         tile_members(
@@ -256,6 +273,20 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
         if (bm) atomicMax(&st->err_bits[k], bm);
         atomicAdd(&st->err_sum[k], bs);
     }
+    if (P.nscenes > 0) {
+        // per-scene maxima: lanes grouped by scene (one group per warp except at the
+        // boundaries between scenes)
+        const unsigned grp = __match_any_sync(0xffffffffu, sc);
+        const unsigned gm = __reduce_max_sync(grp, __float_as_uint(aerr));
+        if (sc >= 0) {
+            if ((__ffs(grp) - 1) == lane && gm) atomicMax(&P.scene_st[sc].err_bits[k], gm);
+            if (grp == 0xffffffffu) {
+                if (lane == 0) atomicAdd(&P.scene_st[sc].err_sum[k], s);
+            } else {
+                atomicAdd(&P.scene_st[sc].err_sum[k], (double)aerr);
+            }
+        }
+    }
 }
 
 // PredictPressureForceFor (pcisph_equations3.cpp:114-155) at the current positions,
@@ -270,13 +301,21 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
                  float dt_over_m, int mode) {
     if (k < 0) k = st->iter;
     else if (converged_before(P, st, k)) return;
-    const bool last = mode == 0 && ((k == max_it - 1) ||
-                      fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
+    bool last = mode == 0 && ((k == max_it - 1) ||
+                fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * kTile + threadIdx.x;
     unsigned fbits = 0;
-    if (i < P.n) {
+    bool active = i < P.n;
+    if (active && P.nscenes > 0) {
+        // batch: each scene stops at its own convergence
+        const int sc = P.scene[i];
+        active = !scene_converged_before(P, sc, k);
+        last = mode == 0 && ((k == max_it - 1) ||
+                             fdv(__uint_as_float(P.scene_st[sc].err_bits[k]), P.target_density) < P.max_err_ratio);
+    }
+    if (active) {
         const float4 pi = pos[i];
         const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
@@ -313,10 +352,8 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
             xstar[i] = F4(xs);
         }
     }
-    if (last) {
-        fbits = warp_max_u(fbits);
-        if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
-    }
+    fbits = warp_max_u(fbits);
+    if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
 }
 
 // End of one corrector iteration in the graph-driven loop: stop when the density error

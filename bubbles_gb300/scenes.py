@@ -144,11 +144,51 @@ def small_pcisph(n_side=(12, 10, 12), spacing=0.02, box=(0.6, 0.5, 0.6), seed=0,
     return sc, dam_block(sc, n_side, seed)
 
 
+def batch_scenes(count, spacing, nmin, nmax, seed=0, positions=True):
+    """Independent dam breaks for a batch: particle counts log-uniform in [nmin, nmax],
+    block aspect ratios uniform in [0.3, 1] per axis; each container is centred at the
+    origin and holds its block in the (-x, -y, -z) corner with room to collapse (twice
+    the block along x, 1.5 times along y, plus one spacing of margin on every side)."""
+    rng = np.random.default_rng(seed)
+    boxes, pos = [], []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        a = rng.uniform(0.3, 1.0, 3)
+        k = (n / float(np.prod(a))) ** (1.0 / 3.0)
+        dims = np.maximum(2, np.round(a * k)).astype(int)
+        block = dims * spacing
+        ext = np.array([2.0 * block[0], 1.5 * block[1], block[2]]) + 2.0 * spacing
+        lo, hi = -ext / 2, ext / 2
+        boxes.append((tuple(lo), tuple(hi)))
+        if positions:
+            sc = {"spacing": spacing, "domain_min": tuple(lo)}
+            pos.append(dam_block(sc, tuple(int(d) for d in dims), int(rng.integers(1 << 31))))
+        else:
+            rng.integers(1 << 31)
+            pos.append(np.zeros((int(np.prod(dims)), 3)))
+    return boxes, pos
+
+
+def batched_64(seed=0, positions=True):
+    """64 independent PCISPH dam breaks at spacing 0.01 in one solver: counts
+    log-uniform in [8,192, 131,072], aspect ratios uniform in [0.3, 1]."""
+    sc = base_scene("pcisph", 0.01, (1.0, 1.0, 1.0))
+    dt = 0.4 * (2 * 0.01) / 100.0 * 5.0   # CFL speed limit at scale 5 (particle.h:598)
+    boxes, pos = batch_scenes(64, 0.01, 8192, 131072, seed=seed, positions=positions)
+    total = sum(len(p) for p in pos)
+    sc.update(dt=dt, steps=500, max_iterations=20, max_density_error_ratio=0.01, batch=True,
+              boxes=boxes,
+              workload="Batched PCISPH: 64 dam breaks, %d particles (counts log-uniform in "
+                       "[8192, 131072], spacing 0.01)" % total)
+    return sc, pos
+
+
 CONFIGS = {
     "sph_16k": sph_16k,
     "pcisph_262k": pcisph_262k,
     "pcisph_1m": pcisph_1m,
     "pcisph_4m": pcisph_4m,
+    "batched_64": batched_64,
 }
 
 

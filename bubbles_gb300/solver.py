@@ -320,6 +320,66 @@ class Solver:
         return out
 
 
+class BatchSolver(Solver):
+    """Independent scenes advanced together (bbg_batch_create): `scene` holds the shared
+    parameters (spacing, density, corrector controls, pressure start, MLP settings),
+    `boxes` each scene's container (box_min, box_max) and `positions` its particles."""
+
+    def __init__(self, scene, boxes, positions, velocities=None, device=0, setup=True):
+        self.scene = dict(scene)
+        self.desc = desc_from_scene(dict(scene, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0)),
+                                    device)
+        if len(boxes) != len(positions) or not boxes:
+            raise ValueError("one container per scene")
+        arr = (N.SceneDesc * len(boxes))()
+        for i, ((lo, hi), p) in enumerate(zip(boxes, positions)):
+            arr[i].count = len(p)
+            for k in range(3):
+                arr[i].box_min[k] = float(lo[k])
+                arr[i].box_max[k] = float(hi[k])
+        h = ctypes.c_void_p()
+        N.call("bbg_batch_create", ctypes.byref(self.desc), arr, len(boxes), ctypes.byref(h))
+        self.h = h
+        self.counts = [len(p) for p in positions]
+        self.n = 0
+        if scene.get("pressure_init") == "learned" and scene.get("mlp"):
+            self.mlp_configure(**scene["mlp"])
+        self.upload_scenes(positions, velocities)
+        if setup:
+            self.setup()
+
+    @property
+    def scene_count(self):
+        return len(self.counts)
+
+    def layout(self):
+        out = np.zeros((self.scene_count, 3))
+        N.call("bbg_batch_layout", self.h, out.ctypes.data_as(N._DP))
+        return out
+
+    def upload_scenes(self, positions, velocities=None):
+        p = np.ascontiguousarray(np.concatenate(positions), dtype=np.float32).reshape(-1, 3)
+        v = None
+        if velocities is not None:
+            v = np.ascontiguousarray(np.concatenate(velocities), dtype=np.float32).reshape(-1, 3)
+        N.call("bbg_batch_upload", self.h, _fptr(p), _fptr(v) if v is not None else None)
+        self.n = int(p.shape[0])
+
+    def download_scenes(self):
+        """Per-scene positions and velocities in scene coordinates."""
+        p = np.zeros((self.n, 3), np.float32)
+        v = np.zeros((self.n, 3), np.float32)
+        N.call("bbg_batch_download", self.h, _fptr(p), _fptr(v))
+        cuts = np.cumsum(self.counts)[:-1]
+        return np.split(p, cuts), np.split(v, cuts)
+
+    def scene_stats(self):
+        it = np.zeros(self.scene_count, np.int32)
+        err = np.zeros(self.scene_count)
+        N.call("bbg_batch_scene_stats", self.h, it.ctypes.data_as(N._IP), err.ctypes.data_as(N._DP))
+        return it, err
+
+
 class PciSphSolver3(Solver):
     """Reference-named facade of PciSphSolver3 (src/core/pcisph_solver.h:56-83)."""
 

@@ -209,6 +209,29 @@ bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable);
 /* Read the statistics of the last substep (synchronises). */
 bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
 
+/* ----- batches of independent scenes ------------------------------------------ */
+/* Many small scenes advanced together by one solver: every pass is one launch over all
+ * of them.  The scenes share the solver description (spacing, density, corrector
+ * controls, dt) and each has its own container, a reverse box collider (global colliders
+ * of bbg_set_colliders are not used in a batch).  Containers are stacked along z with
+ * two empty grid cells between them, so no particle has a neighbour in another scene;
+ * each scene's corrector stops at its own convergence.  No reference counterpart. */
+typedef struct {
+    int count;                /* particles of the scene */
+    double box_min[3];        /* its container in scene coordinates */
+    double box_max[3];
+} bbg_scene_desc;
+bbg_status bbg_batch_create(const bbg_solver_desc *desc, const bbg_scene_desc *scenes, int count,
+                            bbg_solver *out);
+bbg_status bbg_batch_scene_count(bbg_solver s, int *count);
+/* Translation of each scene into the packed domain (count x 3: packed = scene + offset). */
+bbg_status bbg_batch_layout(bbg_solver s, double *offsets);
+/* All particles, scene after scene, in scene coordinates (n x 3 each; vel may be NULL). */
+bbg_status bbg_batch_upload(bbg_solver s, const float *pos, const float *vel);
+bbg_status bbg_batch_download(bbg_solver s, float *pos, float *vel);
+/* Corrector iterations and final max|err|/rho0 of each scene in the last substep. */
+bbg_status bbg_batch_scene_stats(bbg_solver s, int *iterations, double *max_err);
+
 /* ----- learned warm start ---------------------------------------------------- */
 bbg_status bbg_mlp_desc_default(bbg_mlp_desc *desc);
 /* (Re)initialise the model and its training schedule (allocates on first use). */
