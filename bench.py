@@ -325,7 +325,15 @@ def run_ours(args, scene, pos):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     warm = variant != "plain"
     with torch.cuda.stream(stream):
+        tuned = None
+        if not args.no_tuning:
+            from bubbles_gb300 import autotune
+            tuned = autotune.load(args.config)
+            if tuned is not None and scene.get("batch"):
+                scene = dict(scene, grid_spacing_scale=tuned["grid_spacing_scale"])
         g = make_solver(bb, scene, pos, local)
+        if tuned is not None:
+            g.set_tuning(**tuned["tuning"])
         g.set_stream(stream)
         # the first `prep` substeps of the run: plain corrector; the learned variant trains
         # its model on their (features, converged pressure) pairs
@@ -365,6 +373,8 @@ def run_ours(args, scene, pos):
         plain = None
         if warm and not args.no_plain:
             gp = make_solver(bb, dict(scene, pressure_init="zero"), pos, local)
+            if tuned is not None:
+                gp.set_tuning(**tuned["tuning"])
             gp.set_stream(stream)
             restore(gp, False)
             for _ in range(3):
@@ -407,7 +417,7 @@ def run_ours(args, scene, pos):
             g.advance_time_step(dt)
             g.download(pos_h, vel_h)
             if warm:
-                pr_h[:] = g.get(bb.FIELD_PRESSURE)
+                g.get(bb.FIELD_PRESSURE, out=pr_h)
 
         def e2e_reset():
             pos_h[:] = snap_p
@@ -492,6 +502,9 @@ def run_ours(args, scene, pos):
               "regions": "timed, per-kernel and e2e regions each replay the same substeps "
                          "from one snapshot taken after warm-up",
               "l2": "flushed between timed steps (256 MB write, outside the events)",
+              "tuning": ({"source": "bubbles_gb300/tuned/%s.json" % args.config,
+                          "grid_spacing_scale": scene.get("grid_spacing_scale", 2.0),
+                          **tuned["tuning"]} if tuned is not None else "defaults"),
               "parallelism": "replicas" if world > 1 else "single gpu"}
     if variant == "warm":
         config["warm_start"] = "previous substep's pressure x 0.5, monotone corrector update"
@@ -535,6 +548,8 @@ def main():
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
+    ap.add_argument("--no-tuning", action="store_true",
+                    help="ignore bubbles_gb300/tuned/<config>.json (autotuner output)")
     ap.add_argument("--variant", default="learned", choices=["plain", "warm", "learned"],
                     help="corrector start: plain = zero pressure (reference), warm = the previous "
                          "substep's pressure, learned = the MLP estimate")

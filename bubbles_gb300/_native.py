@@ -72,6 +72,11 @@ class SceneDesc(ctypes.Structure):
                 ("box_max", ctypes.c_double * 3)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("block_size", ctypes.c_int), ("batch_np", ctypes.c_int),
+                ("batch_pd", ctypes.c_int), ("batch_pf", ctypes.c_int)]
+
+
 class Shape(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("reverse", ctypes.c_int),
                 ("center", ctypes.c_double * 3), ("size", ctypes.c_double * 3),
@@ -152,6 +157,8 @@ SIGNATURES = {
     "bbg_profiler_enable": [_P, _I],
     "bbg_use_cuda_graphs": [_P, _I],
     "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P],
+    "bbg_get_tuning": [_P, ctypes.POINTER(Tuning)],
+    "bbg_set_tuning": [_P, ctypes.POINTER(Tuning)],
     "bbg_batch_create": [ctypes.POINTER(SolverDesc), ctypes.POINTER(SceneDesc), _I, ctypes.POINTER(_P)],
     "bbg_batch_scene_count": [_P, _IP],
     "bbg_batch_layout": [_P, _DP],

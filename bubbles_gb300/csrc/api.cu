@@ -189,8 +189,10 @@ bbg_status free_all(bbg_solver s) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     Prof *keep = B.prof;
-    memset(&B, 0, sizeof(B));
+    const Tuning tune = B.tune;
+    B = DevBufs();
     B.prof = keep;
+    B.tune = tune;
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_u) cudaFreeHost(s->h_u);
     s->h_st = nullptr;
@@ -764,7 +766,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
 
     bbg_solver s = new (std::nothrow) bbg_solver_s();
     if (!s) return fail(BBG_ERR_OUT_OF_MEMORY, "host allocation failed");
-    memset(&s->B, 0, sizeof(s->B));
+    s->B = DevBufs();
     memset(&s->P, 0, sizeof(s->P));
     memset(&s->acc, 0, sizeof(s->acc));
     s->desc = *desc;
@@ -1598,5 +1600,34 @@ bbg_status bbg_batch_scene_stats(bbg_solver s, int *iterations, double *max_err)
         if (iterations) iterations[i] = it;
         if (max_err) max_err[i] = err;
     }
+    return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// launch tuning
+// ----------------------------------------------------------------------------
+bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!t) return fail(BBG_ERR_INVALID_ARGUMENT, "null tuning");
+    t->block_size = s->B.tune.block;
+    t->batch_np = s->B.tune.batch_np;
+    t->batch_pd = s->B.tune.batch_pd;
+    t->batch_pf = s->B.tune.batch_pf;
+    return BBG_OK;
+}
+
+bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!t) return fail(BBG_ERR_INVALID_ARGUMENT, "null tuning");
+    if (t->block_size != 64 && t->block_size != 128 && t->block_size != 256)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "block size must be 64, 128 or 256");
+    for (int b : {t->batch_np, t->batch_pd, t->batch_pf})
+        if (b != 2 && b != 4 && b != 8) return fail(BBG_ERR_INVALID_ARGUMENT, "gather batches must be 2, 4 or 8");
+    CK(cudaStreamSynchronize(s->stream));
+    s->B.tune.block = t->block_size;
+    s->B.tune.batch_np = t->batch_np;
+    s->B.tune.batch_pd = t->batch_pd;
+    s->B.tune.batch_pf = t->batch_pf;
+    s->epoch++;   // captured graphs hold the old launch shapes
     return BBG_OK;
 }

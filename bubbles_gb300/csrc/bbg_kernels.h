@@ -6,6 +6,15 @@
 
 namespace bbg {
 
+// Launch tuning of the neighbour passes (bbg_set_tuning): block size (= tile) and how
+// many members' records each thread requests together, per pass.
+struct Tuning {
+    int block = 128;       // 64, 128 or 256
+    int batch_np = 4;      // non-pressure pass (two records per member)
+    int batch_pd = 4;      // predicted-density pass
+    int batch_pf = 4;      // pressure-force pass
+};
+
 // Device buffers of one solver (all sized for `capacity` particles / grid cells).
 struct DevBufs {
     float4 *pos[2], *vel[2];   // ping-pong particle state
@@ -29,6 +38,7 @@ struct DevBufs {
     float *stage;              // n * 3 floats of staging for host copies
     unsigned *red;             // reduction scratch (max |F|)
     Prof *prof;                // host-side launch profiler (may be null)
+    Tuning tune;
 };
 
 #define BBG_PBEGIN(B, id, s, it) do { if ((B).prof) (B).prof->begin((id), (s), (it)); } while (0)

@@ -25,6 +25,20 @@ namespace bbg {
 
 constexpr int kThreads = kTile;
 
+#ifndef BBG_NBR_MIN_BLOCKS
+#define BBG_NBR_MIN_BLOCKS 8
+#endif
+#ifndef BBG_PF_MIN_BLOCKS
+#define BBG_PF_MIN_BLOCKS 12
+#endif
+// resident 128-thread blocks per SM the member-walking passes are compiled for (register
+// budget; build-time tuning knobs, measured: 12 for the pressure-force pass, which trades
+// a few spilled registers for occupancy, 8 for the others).  Kernels are compiled for
+// blocks of up to kMaxTile threads with the same register budget.
+constexpr int kNbrMinBlocks = BBG_NBR_MIN_BLOCKS * kTile / kMaxTile;
+constexpr int kPfMinBlocks = BBG_PF_MIN_BLOCKS * kTile / kMaxTile;
+constexpr int kDensityMinBlocks = 12 * kTile / kMaxTile;
+
 // a neighbour's position and velocity records
 struct PosVel {
     float4 p, v;
@@ -56,14 +70,14 @@ __device__ __forceinline__ bool scene_converged_before(const Params &P, int s, i
 // ComputeDensityFor + ComputePressureValue, src/equations/sph_equations3.cpp:7-58.
 // Tests every candidate of the 27 cells exactly once per substep and records the
 // neighbour set (the reference bucket, grid.h:423-447) as a compact member list.
-__global__ void __launch_bounds__(kThreads, 12)
+__global__ void __launch_bounds__(kMaxTile, kDensityMinBlocks)
 k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
           float *__restrict__ press, int *__restrict__ nbr, unsigned short *__restrict__ list,
           int compute_pressure, StepState *st) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
@@ -106,8 +120,8 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
 // k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).  With DIV it also
 // accumulates sum_j (1/rho_j) (1 - d/h)^2 / d (v_j - v_i).(x_j - x_i), the velocity
 // divergence up to m * 45 / (pi h^4), a feature of the learned warm start.
-template <bool DIV>
-__global__ void __launch_bounds__(kThreads)
+template <bool DIV, int NB>
+__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
                const unsigned *__restrict__ start, const unsigned short *__restrict__ list, const int *__restrict__ nbr,
@@ -115,7 +129,7 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
                float *__restrict__ press, float *__restrict__ divsum, int predict, float dt, float dt_over_m) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const float4 vi = vel[i];
@@ -124,7 +138,7 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     float fz = P.mass * P.gz - P.drag * vi.z;
     float dv = 0.f;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
-    tile_members<(kGatherBatch < 4 ? kGatherBatch : 4)>(
+    tile_members<NB>(
         P, start, T, list, nbr, pos, cell[i], i,
         [&](unsigned j) { return PosVel{__ldg(&pos[j]), __ldg(&vel[j])}; },
         [&](const PosVel &nb) {
@@ -204,7 +218,8 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
 // PredictPressureFor (pcisph_equations3.cpp:60-90) over the step-start neighbour set at
 // predicted positions, with the density error stored (tolerance mode) and reduced to
 // max |err| and sum |err| for iteration k; also p / rho*^2 for the pressure force.
-__global__ void __launch_bounds__(kThreads)
+template <int NB>
+__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                const unsigned short *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
@@ -216,7 +231,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     else if (converged_before(P, st, k)) return;
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float aerr = 0.f;
     int sc = -1;   // batch: scene of particle i while its corrector still runs
     if (i < P.n && P.nscenes > 0) {
@@ -226,7 +241,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     if (i < P.n && sc != -2) {
         const float4 xi = xstar[i];
         float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
-        tile_members(
+        tile_members<NB>(
             P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&xstar[j]); },
             [&](const float4 xj) {
                 const float r2 = dist2(xi, xj);
@@ -259,8 +274,8 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
         aerr = fabsf(err);
     }
     // block reduction: max |err| (exact as bits of non-negative floats), sum |err| in FP64
-    __shared__ unsigned smax[kThreads / 32];
-    __shared__ double ssum[kThreads / 32];
+    __shared__ unsigned smax[kMaxTile / 32];
+    __shared__ double ssum[kMaxTile / 32];
     const unsigned m = warp_max_u(__float_as_uint(aerr));
     const double s = warp_sum_d((double)aerr);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -269,7 +284,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     if (threadIdx.x == 0) {
         unsigned bm = 0;
         double bs = 0.0;
-        for (int w = 0; w < kThreads / 32; w++) { bm = max(bm, smax[w]); bs += ssum[w]; }
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { bm = max(bm, smax[w]); bs += ssum[w]; }
         if (bm) atomicMax(&st->err_bits[k], bm);
         atomicAdd(&st->err_sum[k], bs);
     }
@@ -291,7 +306,8 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
 
 // PredictPressureForceFor (pcisph_equations3.cpp:114-155) at the current positions,
 // then either the next prediction or AccumulateForcesFor + TimeIntegrationFor.
-__global__ void __launch_bounds__(kThreads)
+template <int NB>
+__global__ void __launch_bounds__(kMaxTile, kPfMinBlocks)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                  const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
@@ -305,7 +321,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
                 fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
     bool active = i < P.n;
     if (active && P.nscenes > 0) {
@@ -320,7 +336,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
         const float ai = pi.w;   // p_i / rho*_i^2
         float tx = 0.f, ty = 0.f, tz = 0.f;
         const float kg = P.m2 * P.spiky_dw_c;
-        tile_members(
+        tile_members<NB>(
             P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&pos[j]); },
             [&](const float4 pj) {   // pj.w = p_j / rho*_j^2
                 const float r2 = dist2(pi, pj);
@@ -372,14 +388,14 @@ __global__ void k_corrector_control(Params P, StepState *st, int max_it,
 // reference integrates each particle inside the force loop (:277), racing with its
 // neighbours' reads; here all forces read the step-start state and the integrated
 // state goes to the other buffer.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kMaxTile)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
              const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
     if (i < P.n) {
         const float4 pi = pos[i];
@@ -456,14 +472,14 @@ k_integrate(Params P, const float4 *__restrict__ pos, const float4 *__restrict__
 
 // ComputePseudoViscosityAggregationKernelFor (sph_equations3.cpp:341-371): membership
 // from the step-start positions (the bucket), values at the integrated state.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kMaxTile)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
                const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * kTile + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     // the particle itself (distance 0): W_spiky(0) m / rho_i
@@ -504,23 +520,33 @@ __global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *
 
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
-    k_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell,
-                                                             B.start, B.rho, B.inv_rho, B.press,
-                                                             B.nbr, B.list, compute_pressure, B.st);
+    const int t = B.tune.block;
+    k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
+                                               B.press, B.nbr, B.list, compute_pressure, B.st);
     BBG_PEND(B, s);
+}
+
+template <bool DIV>
+static void non_pressure_nb(const Params &P, const DevBufs &B, int buf, int predict, float dt,
+                            float dt_over_m, cudaStream_t s, float *divsum) {
+    const int t = B.tune.block;
+#define NP_LAUNCH(NB)                                                                                   \
+    k_non_pressure<DIV, NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, \
+                                                            B.list, B.nbr, B.force, B.xstar, B.pforce,  \
+                                                            B.press, divsum, predict, dt, dt_over_m)
+    switch (B.tune.batch_np) {
+        case 2: NP_LAUNCH(2); break;
+        case 8: NP_LAUNCH(8); break;
+        default: NP_LAUNCH(4); break;
+    }
+#undef NP_LAUNCH
 }
 
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
                          float dt_over_m, cudaStream_t s, float *divsum) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
-    if (divsum)
-        k_non_pressure<true><<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-            P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
-            divsum, predict, dt, dt_over_m);
-    else
-        k_non_pressure<false><<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-            P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, B.press,
-            nullptr, predict, dt, dt_over_m);
+    if (divsum) non_pressure_nb<true>(P, B, buf, predict, dt, dt_over_m, s, divsum);
+    else non_pressure_nb<false>(P, B, buf, predict, dt, dt_over_m, s, nullptr);
     BBG_PEND(B, s);
 }
 
@@ -536,9 +562,17 @@ void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_fir
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
                          cudaStream_t s, int clamp_total) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
-    k_pred_density<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.xstar, B.cell, B.start, B.list, B.nbr, B.press, B.rhostar, B.derr, B.st, k,
-        delta, clamp_total);
+    const int t = B.tune.block;
+#define PD_LAUNCH(NB)                                                                                  \
+    k_pred_density<NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.xstar, B.cell, B.start, B.list, \
+                                                        B.nbr, B.press, B.rhostar, B.derr, B.st, k, delta, \
+                                                        clamp_total)
+    switch (B.tune.batch_pd) {
+        case 2: PD_LAUNCH(2); break;
+        case 8: PD_LAUNCH(8); break;
+        default: PD_LAUNCH(4); break;
+    }
+#undef PD_LAUNCH
     BBG_PEND(B, s);
 }
 
@@ -554,9 +588,18 @@ void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t 
 void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, int max_it, float dt,
                            float dt_over_m, cudaStream_t s, int mode) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
-    k_pressure_force<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,
-        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, mode);
+    const int t = B.tune.block;
+#define PF_LAUNCH(NB)                                                                                \
+    k_pressure_force<NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start,  \
+                                                          B.list, B.nbr, B.force, B.pforce, B.xstar,   \
+                                                          B.pos[1 - buf], B.vel[1 - buf], B.st, k,     \
+                                                          max_it, dt, dt_over_m, mode)
+    switch (B.tune.batch_pf) {
+        case 2: PF_LAUNCH(2); break;
+        case 8: PF_LAUNCH(8); break;
+        default: PF_LAUNCH(4); break;
+    }
+#undef PF_LAUNCH
     BBG_PEND(B, s);
 }
 
@@ -567,7 +610,7 @@ void launch_corrector_control(const Params &P, const DevBufs &B, int max_it,
 
 void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s) {
     BBG_PBEGIN(B, KID_SPH_FORCES, s, -1);
-    k_sph_forces<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+    k_sph_forces<<<blocks_for(P.n, B.tune.block), B.tune.block, 0, s>>>(
         P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pos[1 - buf],
         B.vel[1 - buf], B.st, dt);
     BBG_PEND(B, s);
@@ -591,7 +634,7 @@ void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cuda
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
                              cudaStream_t s) {
     BBG_PBEGIN(B, KID_PSEUDO_VISCOSITY, s, -1);
-    k_pv_aggregate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(
+    k_pv_aggregate<<<blocks_for(P.n, B.tune.block), B.tune.block, 0, s>>>(
         P, B.pos[1 - new_buf], B.pos[new_buf], B.vel[new_buf], B.inv_rho, B.cell, B.start, B.list, B.nbr,
         B.smoothed);
     k_pv_interpolate<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.vel[new_buf], B.smoothed,

@@ -1,7 +1,7 @@
 // tile.cuh -- tiles of the neighbour passes and the compact neighbour lists.
 //
-// Every neighbour pass runs one thread per particle in blocks of kTile consecutive slots
-// of the cell-sorted arrays (a "tile").  The 27 neighbour cells of any particle in a tile
+// Every neighbour pass runs one thread per particle in blocks of consecutive slots of the
+// cell-sorted arrays (a "tile": the block size, 64 to 256, a tuning parameter).  The 27 neighbour cells of any particle in a tile
 // lie, for each of the 9 (dy, dz) row offsets r, inside one contiguous range of linear
 // cell ids, [first cell - 1 + off_r, last cell + 1 + off_r], i.e. one contiguous slot
 // range starting at lo[r].  A neighbour j of a particle is therefore stored in 16 bits
@@ -20,7 +20,8 @@
 
 namespace bbg {
 
-constexpr int kTile = 128;          // slots per tile = threads per block of a neighbour pass
+constexpr int kTile = 128;          // default tile: slots per tile = threads per block
+constexpr int kMaxTile = 256;       // largest block size a neighbour pass is launched with
 #ifndef BBG_GATHER_BATCH
 #define BBG_GATHER_BATCH 4
 #endif
@@ -37,7 +38,7 @@ struct TileMap {
 __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
                                            const unsigned *__restrict__ start, int n, TileMap &T) {
     if (threadIdx.x < 9) {
-        const int s0 = blockIdx.x * kTile;
+        const int s0 = blockIdx.x * blockDim.x;
         const int r = threadIdx.x;
         const long long plane = (long long)g.nx * g.ny;
         const long long off = (long long)(r % 3 - 1) * g.nx + (long long)(r / 3 - 1) * plane;

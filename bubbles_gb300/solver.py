@@ -203,9 +203,12 @@ class Solver:
         return c.value
 
     # state ---------------------------------------------------------------------
-    def get(self, field):
+    def get(self, field, out=None):
         shape = (self.n, 3) if field in N.VECTOR_FIELDS else (self.n,)
-        out = np.zeros(shape, np.float32)
+        if out is None:
+            out = np.zeros(shape, np.float32)
+        elif out.dtype != np.float32 or not out.flags.c_contiguous or out.size != int(np.prod(shape)):
+            raise ValueError("field buffer must be contiguous float32 of shape %s" % (shape,))
         N.call("bbg_get_field", self.h, int(field), _fptr(out))
         return out
 
@@ -271,6 +274,19 @@ class Solver:
             name = names.raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
             out[name] = (ms[i], cnt[i])
         return out, total.value
+
+    # --- launch tuning ----------------------------------------------------------
+    def tuning(self):
+        t = N.Tuning()
+        N.call("bbg_get_tuning", self.h, ctypes.byref(t))
+        return {name: getattr(t, name) for name, _ in t._fields_}
+
+    def set_tuning(self, **values):
+        t = N.Tuning()
+        N.call("bbg_get_tuning", self.h, ctypes.byref(t))
+        for k, v in values.items():
+            setattr(t, k, int(v))
+        N.call("bbg_set_tuning", self.h, ctypes.byref(t))
 
     # --- learned warm start ----------------------------------------------------
     def mlp_configure(self, **settings):

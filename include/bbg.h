@@ -209,6 +209,20 @@ bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable);
 /* Read the statistics of the last substep (synchronises). */
 bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
 
+/* ----- launch tuning ------------------------------------------------------------ */
+/* Block size of the neighbour passes (each block walks one tile of consecutive cell-
+ * sorted particles) and how many members' records a thread requests together in the
+ * non-pressure, predicted-density and pressure-force passes.  Results do not depend on
+ * them; bubbles_gb300.autotune measures and picks them. */
+typedef struct {
+    int block_size;      /* 64, 128 (default) or 256 */
+    int batch_np;        /* 2, 4 (default) or 8 */
+    int batch_pd;
+    int batch_pf;
+} bbg_tuning;
+bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t);
+bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t);
+
 /* ----- batches of independent scenes ------------------------------------------ */
 /* Many small scenes advanced together by one solver: every pass is one launch over all
  * of them.  The scenes share the solver description (spacing, density, corrector

@@ -506,3 +506,26 @@ def test_gpu_against_reference_fixtures(gpu):
         g.accumulate_and_integrate(dt)
         p, v = g.download()
         assert np.max(np.abs(p - g32["corr_pos"])) <= RTOL * h0
+
+
+@pytest.mark.parametrize("tuning", [dict(block_size=64, batch_np=2, batch_pd=8, batch_pf=2),
+                                    dict(block_size=256, batch_np=8, batch_pd=2, batch_pf=8)])
+def test_launch_tuning_does_not_change_results(gpu, moved, tuning):
+    """Block size and gather batches change the launch shape, not the arithmetic: the
+    substeps are bitwise identical to the default tuning."""
+    sc, p, v = moved
+    ga = bb.Solver(sc, pos=p, vel=v)
+    gb = bb.Solver(sc, pos=p, vel=v)
+    gb.set_tuning(**tuning)
+    assert gb.tuning() == tuning
+    for _ in range(3):
+        sa = ga.advance_time_step(sc["dt"], stats=True)
+        sb = gb.advance_time_step(sc["dt"], stats=True)
+        assert sa["iterations"] == sb["iterations"]
+    pa, va = ga.download()
+    pb, vb = gb.download()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    with pytest.raises(bb.BbgError):
+        gb.set_tuning(block_size=96)
+    ga.close()
+    gb.close()
