@@ -296,6 +296,7 @@ def timed_substeps(g, dt, steps, stream, flush, events=True):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     iters, errs = [], []
+    flags = {"out_of_grid": 0, "crowded": 0, "not_converged": 0}
     torch.cuda.synchronize()
     for k in range(steps):
         flush.zero_()
@@ -305,8 +306,12 @@ def timed_substeps(g, dt, steps, stream, flush, events=True):
         st = g.stats()
         iters.append(st["iterations"])
         errs.append(st["max_density_error_ratio"])
+        flags["out_of_grid"] = max(flags["out_of_grid"], st["out_of_grid"])
+        flags["crowded"] = max(flags["crowded"], st["crowded"])
+        flags["not_converged"] += st["not_converged"]
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    timed_substeps.flags = flags
     return ms, iters, errs
 
 
@@ -364,6 +369,7 @@ def run_ours(args, scene, pos):
         barrier(dist)
         # timed region: every substep is one CUDA-graph launch
         step_ms, iters, max_err = timed_substeps(g, dt, args.steps, stream, flush)
+        timed_flags = dict(timed_substeps.flags)
         barrier(dist)
         total_s = sum(step_ms) / 1e3
         value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
@@ -497,6 +503,9 @@ def run_ours(args, scene, pos):
               "corrector_iterations_mean": float(np.mean(iters)),
               "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
               "max_density_error_ratio_max": float(np.max(max_err)),
+              "substeps_at_max_iterations_above_tolerance": timed_flags["not_converged"],
+              "state_checks": {"out_of_grid_max": timed_flags["out_of_grid"],
+                               "crowded_max": timed_flags["crowded"]},
               "member_list_mean": list_len,
               "preparation_s": prep_s,
               "regions": "timed, per-kernel and e2e regions each replay the same substeps "

@@ -63,7 +63,8 @@ class MlpDesc(ctypes.Structure):
                 ("beta1", ctypes.c_double),
                 ("beta2", ctypes.c_double),
                 ("epsilon", ctypes.c_double),
-                ("seed", ctypes.c_ulonglong)]
+                ("seed", ctypes.c_ulonglong),
+                ("expectile", ctypes.c_double)]
 
 
 class SceneDesc(ctypes.Structure):
@@ -93,7 +94,8 @@ class StepStats(ctypes.Structure):
                 ("mean_density_error_ratio", ctypes.c_double),
                 ("neighbor_overflow", ctypes.c_int),
                 ("out_of_grid", ctypes.c_int),
-                ("max_force", ctypes.c_double)]
+                ("max_force", ctypes.c_double),
+                ("crowded", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -226,7 +226,8 @@ std::vector<float> mlp_initial_params(unsigned long long seed) {
 }
 
 bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
-    if (d.batch < 1 || d.train_substeps < 0 || d.steps_per_substep < 0 || !(d.learning_rate > 0))
+    if (d.batch < 1 || d.train_substeps < 0 || d.steps_per_substep < 0 || !(d.learning_rate > 0) ||
+        !(d.expectile > 0 && d.expectile < 1))
         return fail(BBG_ERR_INVALID_ARGUMENT, "invalid MLP training settings");
     CK(cudaStreamSynchronize(s->stream));
     if (!s->mlp_alloc || s->mlp.batch != d.batch) {
@@ -351,6 +352,7 @@ void add_substep_stats(bbg_solver s, float dt) {
     }
     a.neighbor_overflow = (int)st->nbr_overflow;
     a.out_of_grid = (int)st->out_of_grid;
+    a.crowded = (int)st->crowded;
     float f;
     memcpy(&f, &st->max_force_bits, 4);
     a.max_force = f;
@@ -407,7 +409,7 @@ static void launch_training(bbg_solver s, float delta, cudaStream_t cs) {
     for (int k = 0; k < d.steps_per_substep; k++) {
         launch_mlp_collect(s->P, s->B, s->mlp, pressure_unit(s, delta), cs);
         launch_mlp_train_step(s->mlp, s->mlp.bx, s->mlp.bt, s->mlp.batch, (float)d.learning_rate,
-                              (float)d.beta1, (float)d.beta2, (float)d.epsilon, cs);
+                              (float)d.beta1, (float)d.beta2, (float)d.epsilon, (float)d.expectile, cs);
     }
 }
 
@@ -1343,6 +1345,7 @@ bbg_status bbg_mlp_desc_default(bbg_mlp_desc *d) {
     d->beta2 = 0.999;
     d->epsilon = 1e-8;
     d->seed = 20240601ull;
+    d->expectile = 0.5;
     return BBG_OK;
 }
 
@@ -1422,7 +1425,7 @@ bbg_status bbg_mlp_train_batch(bbg_solver s, const float *features, const float 
     s->mlp_loss_count = (double)batch;
     const bbg_mlp_desc &d = s->mdesc;
     launch_mlp_train_step(s->mlp, reinterpret_cast<const float4 *>(dx), dt, batch, (float)d.learning_rate,
-                          (float)d.beta1, (float)d.beta2, (float)d.epsilon, s->stream);
+                          (float)d.beta1, (float)d.beta2, (float)d.epsilon, (float)d.expectile, s->stream);
     CK_LAUNCH();
     CK(cudaStreamSynchronize(s->stream));
     return BBG_OK;

@@ -83,8 +83,18 @@ struct StepState {
     unsigned out_of_grid;
     unsigned nbr_overflow;
     unsigned nonfinite;
+    unsigned crowded;                    // cells / particles past the work caps (see below)
     int iter;                            // corrector iteration (graph-driven loop)
 };
+
+// Work caps that keep a degenerate state (e.g. a blown-up simulation that piles particles
+// into a few cells) from turning the per-cell rank and the candidate search quadratic:
+// a cell with more than kRankCap particles keeps its arrival order instead of the order
+// by id, and a particle with more than kMaxCandidates candidates in its 27 cells gets no
+// neighbours.  Both are counted in StepState::crowded; normal states are far below them
+// (about 8 particles per cell, 216 candidates).
+constexpr unsigned kRankCap = 512;
+constexpr unsigned kMaxCandidates = 1024;
 
 // ----------------------------------------------------------------------------
 // explicitly rounded FP32 helpers (no contraction)

@@ -141,15 +141,20 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
               const float4 *__restrict__ vel_in, float4 *__restrict__ pos_out,
               float4 *__restrict__ vel_out, int *__restrict__ pid_out, int *__restrict__ slot,
               unsigned *__restrict__ cell, const float *__restrict__ press_in,
-              float *__restrict__ pprev) {
+              float *__restrict__ pprev, StepState *st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const uint2 e = tmp[t];
     const unsigned c = cell_old[e.y];
     const unsigned a = start[c], b = start[c + 1];
-    unsigned rank = 0;
-    for (unsigned q = a; q < b; ++q) rank += (tmp[q].x < e.x) ? 1u : 0u;
-    const unsigned dst = a + rank;
+    unsigned dst = (unsigned)t;   // arrival order: only for cells past the cap
+    if (b - a <= kRankCap) {
+        unsigned rank = 0;
+        for (unsigned q = a; q < b; ++q) rank += (tmp[q].x < e.x) ? 1u : 0u;
+        dst = a + rank;
+    } else if ((unsigned)t == a) {
+        atomicAdd(&st->crowded, 1u);
+    }
     pos_out[dst] = pos_in[e.y];
     vel_out[dst] = vel_in[e.y];
     pid_out[dst] = (int)e.x;
@@ -189,7 +194,7 @@ void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src,
     BBG_PBEGIN(B, KID_RANK_GATHER, s, -1);
     k_rank_gather<<<blocks_for(n, kThreads), kThreads, 0, s>>>(
         n, B.tmp, B.cell_old, B.start, B.pos[src], B.vel[src], B.pos[1 - src], B.vel[1 - src],
-        B.pid[1 - pid_src], B.slot, B.cell, B.press, B.pprev);
+        B.pid[1 - pid_src], B.slot, B.cell, B.press, B.pprev, B.st);
     BBG_PEND(B, s);
 }
 

@@ -223,10 +223,11 @@ __global__ void k_mlp_collect(int n, int batch, const unsigned *__restrict__ ste
 }
 
 // Forward + backward of one 128-sample block; weight gradients reduced in shared memory
-// and added to grad (FP32 atomics); sum of squared errors added to *loss.
+// and added to grad (FP32 atomics); sum of (weighted) squared errors added to *loss.
 __global__ void __launch_bounds__(128)
 k_mlp_train(int batch, const float4 *__restrict__ bx, const float *__restrict__ bt,
-            const float *__restrict__ theta, float *__restrict__ grad, double *__restrict__ loss) {
+            const float *__restrict__ theta, float *__restrict__ grad, double *__restrict__ loss,
+            float expectile) {
     extern __shared__ float smem[];
     float *sW2 = smem;                    // [64][64]
     float *sW1 = sW2 + kHid * kHid;       // [4][64]
@@ -288,7 +289,10 @@ k_mlp_train(int batch, const float4 *__restrict__ bx, const float *__restrict__ 
         z2[k] = d;   // keep GELU'(z2)
     }
     const float err = valid ? y - target : 0.f;
-    const float dy = 2.f * err / (float)batch;
+    // asymmetric squared error (expectile tau): over-estimates weigh (1 - tau) / 0.5,
+    // under-estimates tau / 0.5; tau = 0.5 is the mean squared error
+    const float wgt = (err > 0.f ? 1.f - expectile : expectile) * 2.f;
+    const float dy = 2.f * wgt * err / (float)batch;
     sDY[t] = dy;
     // backward through layer 3 and GELU 2
 #pragma unroll
@@ -304,7 +308,7 @@ k_mlp_train(int batch, const float4 *__restrict__ bx, const float *__restrict__ 
         sD1[a * 128 + t] *= acc;   // dz1
     }
     // squared error of the block
-    double l = (double)err * (double)err;
+    double l = (double)wgt * (double)err * (double)err;
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
     if ((t & 31) == 0) sLoss[t >> 5] = l;
     __syncthreads();
@@ -455,8 +459,9 @@ cudaError_t mlp_prepare() {
 }
 
 void launch_mlp_train_step(const MlpBufs &M, const float4 *bx, const float *bt, int batch, float lr,
-                           float beta1, float beta2, float eps, cudaStream_t s) {
-    k_mlp_train<<<blocks_for(batch, 128), 128, mlp_train_smem(), s>>>(batch, bx, bt, M.theta, M.grad, M.loss);
+                           float beta1, float beta2, float eps, float expectile, cudaStream_t s) {
+    k_mlp_train<<<blocks_for(batch, 128), 128, mlp_train_smem(), s>>>(batch, bx, bt, M.theta, M.grad, M.loss,
+                                                                      expectile);
     k_mlp_adam<<<blocks_for(kParams, 256), 256, 0, s>>>(M.theta, M.grad, M.m1, M.m2, M.step, lr, beta1,
                                                          beta2, eps);
     k_mlp_pack<<<1, 256, 0, s>>>(M.theta, M.w1f, M.w2f, M.tail, M.step, 1);

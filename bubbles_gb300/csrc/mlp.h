@@ -45,7 +45,7 @@ void launch_mlp_warm_start(const Params &P, const DevBufs &B, const MlpBufs &M, 
 void launch_mlp_infer_raw(const MlpBufs &M, const float4 *feat, int n, float *out, cudaStream_t s);
 // one forward / backward / Adam step on a batch, then the BF16 fragments are rebuilt
 void launch_mlp_train_step(const MlpBufs &M, const float4 *bx, const float *bt, int batch, float lr,
-                           float beta1, float beta2, float eps, cudaStream_t s);
+                           float beta1, float beta2, float eps, float expectile, cudaStream_t s);
 void launch_mlp_collect(const Params &P, const DevBufs &B, const MlpBufs &M, float p_unit, cudaStream_t s);
 void launch_mlp_pack(const MlpBufs &M, cudaStream_t s);
 // features in caller order (n x 4 floats) through the id -> slot map

@@ -75,9 +75,13 @@ k_na_rank(int n, const uint2 *__restrict__ pairs, const unsigned *__restrict__ s
     if (t >= n) return;
     const uint2 e = pairs[t];   // (particle index, cell)
     const unsigned a = start[e.y], b = start[e.y + 1];
-    unsigned rank = 0;
-    for (unsigned q = a; q < b; ++q) rank += (pairs[q].x < e.x) ? 1u : 0u;
-    sorted_ids[a + rank] = e.x;
+    unsigned dst = (unsigned)t;   // arrival order in a cell past the rank cap, as the solver
+    if (b - a <= kRankCap) {
+        unsigned rank = 0;
+        for (unsigned q = a; q < b; ++q) rank += (pairs[q].x < e.x) ? 1u : 0u;
+        dst = a + rank;
+    }
+    sorted_ids[dst] = e.x;
     cell_of[e.x] = e.y;
 }
 

@@ -86,7 +86,13 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     int cnt = 0;      // bucket members, i included
     int listed = 0;   // members other than i
     bool fits = true;
-    tile_candidates_coded(P.g, start, T, cw & ~kWide, &fits, [&](unsigned j, unsigned base) {
+    const bool crowded = candidate_count(P.g, start, cw & ~kWide) > kMaxCandidates;
+    if (crowded) {
+        // past the work cap: the particle itself only (counted, see kMaxCandidates)
+        sum = 1.f;
+        cnt = 1;
+        atomicAdd(&st->crowded, 1u);
+    } else tile_candidates_coded(P.g, start, T, cw & ~kWide, &fits, [&](unsigned j, unsigned base) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);
         if (std_member(P, pi, pj, r2)) {
@@ -145,7 +151,7 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
             const float4 pj = nb.p, vj = nb.v;   // vj.w = 1 / rho_j
             const float r2 = dist2(pi, pj);
             const float inv_d = rsqrtf(r2);
-            const float d = r2 * inv_d;
+            const float d = r2 > 0.f ? r2 * inv_d : 0.f;   // coincident particles: distance 0
             const float x = 1.f - d * P.inv_h;
             const float w = kv * x * vj.w;
             fx += (vj.x - vi.x) * w;
@@ -341,7 +347,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
             [&](const float4 pj) {   // pj.w = p_j / rho*_j^2
                 const float r2 = dist2(pi, pj);
                 const float inv_d = rsqrtf(r2);
-                const float d = r2 * inv_d;
+                const float d = r2 > 0.f ? r2 * inv_d : 0.f;   // coincident particles: distance 0
                 // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
                 if (d - P.h <= -P.iz && d >= P.iz) {
                     const float x = 1.f - d * P.inv_h;
@@ -414,7 +420,7 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
                 const float4 pj = nb.p, vj = nb.v;   // vj.w = 1 / rho_j
                 const float r2 = dist2(pi, pj);
                 const float inv_d = rsqrtf(r2);
-                const float d = r2 * inv_d;
+                const float d = r2 > 0.f ? r2 * inv_d : 0.f;   // coincident particles: distance 0
                 if (d - P.h <= -P.iz) {
                     const float x = 1.f - d * P.inv_h;
                     if (d >= P.iz) {

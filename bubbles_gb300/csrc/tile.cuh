@@ -50,6 +50,30 @@ __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__r
     __syncthreads();
 }
 
+// The 9 row ranges of the 27 neighbour cells of cell c in z, y, x order: f(r, b, e) for
+// range r = slots [b, e).
+template <class F>
+__device__ __forceinline__ void tile_rows(const GridDev &g, const unsigned *__restrict__ start, unsigned c,
+                                          F &&f) {
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
+    const int cz = (int)(c / plane);
+    const unsigned rem = c - (unsigned)cz * plane;
+    const int cy = (int)(rem / (unsigned)nx);
+    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
+    const int x0 = cx > 0 ? cx - 1 : 0;
+    const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+    const int z0 = cz > 0 ? cz - 1 : 0, z1 = cz + 1 < nz ? cz + 1 : nz - 1;
+    const int y0 = cy > 0 ? cy - 1 : 0, y1 = cy + 1 < ny ? cy + 1 : ny - 1;
+    for (int z = z0; z <= z1; ++z) {
+        for (int y = y0; y <= y1; ++y) {
+            const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
+            f((z - cz + 1) * 3 + (y - cy + 1), __ldg(&start[row + (unsigned)x0]),
+              __ldg(&start[row + (unsigned)x1 + 1u]));
+        }
+    }
+}
+
 // The 9 row ranges of the 27 neighbour cells of cell c (reference neighbour list,
 // src/core/grid.h:555-593) in z, y, x order: f(j, r) for every candidate slot j of range r.
 template <class F>
@@ -74,6 +98,14 @@ __device__ __forceinline__ void tile_candidates(const GridDev &g, const unsigned
             for (unsigned j = b; j < e; ++j) f(j, r);
         }
     }
+}
+
+// Number of candidates in the 27 cells of cell c.
+__device__ __forceinline__ unsigned candidate_count(const GridDev &g, const unsigned *__restrict__ start,
+                                                    unsigned c) {
+    unsigned total = 0;
+    tile_rows(g, start, c, [&](int, unsigned b, unsigned e) { total += e - b; });
+    return total;
 }
 
 // Same visit order, for the density pass: f(j, base) with the list entry of slot j equal
@@ -120,6 +152,7 @@ __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__
                                              const int *__restrict__ nbr, const float4 *__restrict__ pos0,
                                              unsigned cellw, int i, Fetch &&fetch, Use &&use) {
     if (cellw & kWide) {
+        if (candidate_count(P.g, start, cellw & ~kWide) > kMaxCandidates) return;
         const float4 pi = __ldg(&pos0[i]);
         tile_candidates(P.g, start, cellw & ~kWide, [&](unsigned j, int) {
             if (j == (unsigned)i) return;

@@ -106,7 +106,8 @@ def pcisph_262k(seed=0, positions=True):
     """Plain PCISPH dam break: 64^3 at 0.01 in a 2 x 1.5 x 1 box, sphere r 0.15 at the centre."""
     sc = base_scene("pcisph", 0.01, (2.0, 1.5, 1.0))
     sc["colliders"].append({"type": "sphere", "center": (0.0, 0.0, 0.0), "radius": 0.15})
-    sc.update(dt=5e-4, steps=500, max_iterations=20, max_density_error_ratio=0.01,
+    # Advance(5e-4) splits into 2 CFL substeps (speed limit 4e-4 at scale 5)
+    sc.update(dt=2.5e-4, advance_dt=5e-4, steps=500, max_iterations=20, max_density_error_ratio=0.01,
               workload="PCISPH dam break 262,144 particles (64^3 @ 0.01, 2x1.5x1 box, sphere r0.15)")
     sc["block"] = (64, 64, 64)
     return sc, (dam_block(sc, (64, 64, 64), seed) if positions else None)
@@ -129,7 +130,8 @@ def pcisph_4m(seed=0, positions=True):
     lo = np.asarray(sc["domain_min"]) + 0.005
     block_hi = lo + np.array([256, 64, 256]) * 0.005
     sc["colliders"] += place_spheres(rng, 8, 0.1, 0.3, (4.0, 1.0, 2.0), block_hi, 0.02)
-    sc.update(dt=2.5e-4, steps=2000, max_iterations=20, max_density_error_ratio=0.01,
+    # Advance(2.5e-4) splits into 2 CFL substeps (speed limit 2e-4 at scale 5)
+    sc.update(dt=1.25e-4, advance_dt=2.5e-4, steps=2000, max_iterations=20, max_density_error_ratio=0.01,
               workload="PCISPH dam break 4,194,304 particles (256x64x256 @ 0.005, 4x1x2 box, 8 spheres)")
     sc["block"] = (256, 64, 256)
     return sc, (dam_block(sc, (256, 64, 256), seed) if positions else None)

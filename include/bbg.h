@@ -136,6 +136,8 @@ typedef struct {
     int neighbor_overflow;            /* particles with > 100 neighbours (reference bucket cap) */
     int out_of_grid;                  /* particles hashed outside the grid (clamped) */
     double max_force;                 /* max |F| after the last substep (CFL input) */
+    int crowded;                      /* cells / particles past the work caps of a degenerate
+                                         state (a cell of > 512 particles, > 1,024 candidates) */
 } bbg_step_stats;
 
 /* Learned warm start (pressure_init = BBG_PRESSURE_INIT_LEARNED): a per-particle MLP
@@ -153,6 +155,9 @@ typedef struct {
     double learning_rate;      /* 1e-3 */
     double beta1, beta2, epsilon;   /* 0.9, 0.999, 1e-8 */
     unsigned long long seed;   /* weight initialisation */
+    double expectile;          /* training loss: squared error weighted (1 - tau) above and
+                                  tau below the target (0.5: mean squared error); tau < 0.5
+                                  biases estimates low, which suits the monotone update */
 } bbg_mlp_desc;
 
 /* ----- library ----------------------------------------------------------- */
@@ -320,7 +325,9 @@ bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts);
  * bbg_update_grid_distribution + bbg_dump_grid on caller-owned device buffers:
  *   d_pos          n xyz float triples (caller order)
  *   d_cell_of      n cell ids (caller order)
- *   d_sorted_ids   n particle indices sorted by (cell id, index)
+ *   d_sorted_ids   n particle indices sorted by (cell id, index); a cell of more than
+ *                  512 particles (a degenerate state) keeps the arrival order instead,
+ *                  as the solver's grid does
  *   d_cell_start   cells + 1 offsets of each cell's range in d_sorted_ids
  * with the grid of UtilBuildGridForDomain(domain, spacing, spacing_scale).  It never
  * allocates: its scratch is one fixed __device__ array of BBG_NOALLOC_SCRATCH_BYTES

@@ -56,8 +56,9 @@ def forward_bf16(theta, x):
     return (h2 @ bf16(w3).astype(np.float64) + float(b3)).astype(np.float32)
 
 
-def loss_and_grad(theta, x, t):
-    """Mean squared error and its gradient in FP32 (torch autograd, CPU)."""
+def loss_and_grad(theta, x, t, expectile=0.5):
+    """Mean (expectile-weighted) squared error and its gradient in FP32 (torch autograd,
+    CPU): errors above the target weigh 2 (1 - tau), below 2 tau."""
     import torch
     th = torch.tensor(np.asarray(theta, np.float32), requires_grad=True)
     w1 = th[OFF_W1:OFF_B1].reshape(N_IN, N_HID)
@@ -72,6 +73,8 @@ def loss_and_grad(theta, x, t):
 
     xt = torch.tensor(np.asarray(x, np.float32))
     y = g(g(xt @ w1 + b1) @ w2 + b2) @ w3 + b3
-    loss = ((y - torch.tensor(np.asarray(t, np.float32))) ** 2).mean()
+    err = y - torch.tensor(np.asarray(t, np.float32))
+    w = torch.where(err > 0, 2.0 * (1.0 - expectile), 2.0 * expectile)
+    loss = (w.detach() * err ** 2).mean()
     loss.backward()
-    return float(loss), th.grad.numpy().copy()
+    return float(loss.detach()), th.grad.numpy().copy()

@@ -54,11 +54,12 @@ def test_mlp_params_round_trip(gpu, small):
     g.close()
 
 
-def test_mlp_gradient_matches_autograd(gpu, small):
+@pytest.mark.parametrize("expectile", [0.5, 0.3])
+def test_mlp_gradient_matches_autograd(gpu, small, expectile):
     """With Adam's epsilon far above |g| one step moves theta by -lr * g / eps, which
-    exposes the gradient of the training kernel."""
+    exposes the gradient of the training kernel (plain and expectile-weighted loss)."""
     sc, p = small
-    g = learned_solver(sc, p, learning_rate=1.0, epsilon=1e3, beta1=0.0, beta2=0.0)
+    g = learned_solver(sc, p, learning_rate=1.0, epsilon=1e3, beta1=0.0, beta2=0.0, expectile=expectile)
     th = random_params(3, 0.5)
     g.mlp_set_params(th)
     rng = np.random.default_rng(2)
@@ -66,7 +67,7 @@ def test_mlp_gradient_matches_autograd(gpu, small):
     t = rng.normal(0.0, 1.0, 1000).astype(np.float32)
     g.mlp_train_batch(x, t)
     moved = (th.astype(np.float64) - g.mlp_params()) * 1e3   # = g / (1 + |g| / eps)
-    loss, grad = loss_and_grad(th, x, t)
+    loss, grad = loss_and_grad(th, x, t, expectile)
     want = grad / (1.0 + np.abs(grad) / 1e3)
     assert np.max(np.abs(moved - want)) <= 1e-4 * max(1.0, np.abs(want).max())
     st = g.mlp_status()

@@ -529,3 +529,19 @@ def test_launch_tuning_does_not_change_results(gpu, moved, tuning):
         gb.set_tuning(block_size=96)
     ga.close()
     gb.close()
+
+
+def test_degenerate_pileup_is_bounded_and_reported(gpu, small):
+    """Particles piled into one point (a blown-up state): the per-cell rank and the
+    candidate search stay within their work caps, the substep ends and reports it."""
+    import time
+    sc, _ = small
+    pos = np.tile(np.array([[0.0, -0.1, 0.0]]), (3000, 1))
+    g = bb.Solver(sc, pos=pos)
+    t0 = time.time()
+    st = g.advance_time_step(sc["dt"], stats=True)
+    assert time.time() - t0 < 60
+    assert st["crowded"] > 0
+    p, _ = g.download()
+    assert np.all(np.isfinite(p))
+    g.close()
