@@ -3,6 +3,7 @@
 
 #include "bbg_internal.cuh"
 #include "prof.h"
+#include "tile.cuh"
 
 namespace bbg {
 
@@ -30,7 +31,7 @@ struct DevBufs {
     unsigned *partials;        // scan partials
     uint2 *tmp;                // scratch: (original id, pre-sort slot) placed by cell
     int *nbr;                  // neighbour count of each sorted slot
-    unsigned short *list;      // member lists: kMaxList 16-bit entries per particle,
+    ListEntry *list;           // member lists: kMaxList entries per particle,
                                // member-major (list[q * n + i]; tile.cuh)
     float *inv_rho;            // 1 / density
     float *pprev;              // pressure of the previous substep, in the current order

@@ -73,7 +73,7 @@ __device__ __forceinline__ bool scene_converged_before(const Params &P, int s, i
 __global__ void __launch_bounds__(kMaxTile, kDensityMinBlocks)
 k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
           const unsigned *__restrict__ start, float *__restrict__ rho, float *__restrict__ inv_rho,
-          float *__restrict__ press, int *__restrict__ nbr, unsigned short *__restrict__ list,
+          float *__restrict__ press, int *__restrict__ nbr, ListEntry *__restrict__ list,
           int compute_pressure, StepState *st) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
@@ -100,7 +100,7 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
             sum += x * x * x;
             cnt++;
             if (j != (unsigned)i) {
-                if (listed < kMaxList) list[(size_t)listed * n + (size_t)i] = (unsigned short)(j + base);
+                if (listed < kMaxList) list[(size_t)listed * n + (size_t)i] = list_code(j, base);
                 listed++;
             }
         }
@@ -130,7 +130,7 @@ template <bool DIV, int NB>
 __global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
-               const unsigned *__restrict__ start, const unsigned short *__restrict__ list, const int *__restrict__ nbr,
+               const unsigned *__restrict__ start, const ListEntry *__restrict__ list, const int *__restrict__ nbr,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
                float *__restrict__ press, float *__restrict__ divsum, int predict, float dt, float dt_over_m) {
     __shared__ TileMap T;
@@ -228,7 +228,7 @@ template <int NB>
 __global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned short *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
+               const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
                float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
                float delta, int clamp_total) {
     // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
@@ -316,7 +316,7 @@ template <int NB>
 __global__ void __launch_bounds__(kMaxTile, kPfMinBlocks)
 k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+                 const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
                  float4 *__restrict__ pforce,
                  float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
                  float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
@@ -397,7 +397,7 @@ __global__ void k_corrector_control(Params P, StepState *st, int max_it,
 __global__ void __launch_bounds__(kMaxTile)
 k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
              const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-             const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+             const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, StepState *st, float dt) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kMaxTile)
 k_pv_aggregate(Params P, const float4 *__restrict__ pos_old, const float4 *__restrict__ pos,
                const float4 *__restrict__ vel, const float *__restrict__ inv_rho,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const unsigned short *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
+               const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ smoothed) {
     __shared__ TileMap T;
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

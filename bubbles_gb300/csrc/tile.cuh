@@ -34,6 +34,26 @@ struct TileMap {
     int lo[9];      // first slot of range r
 };
 
+#ifndef BBG_LIST_BITS
+#define BBG_LIST_BITS 16
+#endif
+#if BBG_LIST_BITS == 32
+// build-time alternative: absolute slot indices (4 bytes per member, no decoding)
+using ListEntry = unsigned;
+__device__ __forceinline__ unsigned list_slot(const TileMap &, unsigned e) { return e; }
+__device__ __forceinline__ unsigned list_code(unsigned j, unsigned) { return j; }
+constexpr bool kListRelative = false;
+#else
+using ListEntry = unsigned short;
+__device__ __forceinline__ unsigned list_slot(const TileMap &T, unsigned e) {
+    return (unsigned)T.lo[e >> kOffBits] + (e & (kOffLimit - 1));
+}
+__device__ __forceinline__ unsigned short list_code(unsigned j, unsigned base) {
+    return (unsigned short)(j + base);
+}
+constexpr bool kListRelative = true;
+#endif
+
 // The tile's 9 range starts from the grid (all threads of the block must call it).
 __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
                                            const unsigned *__restrict__ start, int n, TileMap &T) {
@@ -131,15 +151,13 @@ __device__ __forceinline__ void tile_candidates_coded(const GridDev &g, const un
             const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
             const unsigned b = __ldg(&start[row + (unsigned)x0]);
             const unsigned e = __ldg(&start[row + (unsigned)x1 + 1u]);
-            if (e - lo > (unsigned)kOffLimit) *fits = false;
+            if (kListRelative && e - lo > (unsigned)kOffLimit) *fits = false;
             for (unsigned j = b; j < e; ++j) f(j, base);
         }
     }
 }
 
-__device__ __forceinline__ unsigned list_slot(const TileMap &T, unsigned e) {
-    return (unsigned)T.lo[e >> kOffBits] + (e & (kOffLimit - 1));
-}
+
 
 // For every member j != i of particle i's step-start neighbour set: use(fetch(j)).
 // Members are processed NB at a time: the NB list entries and then the NB neighbour
@@ -148,7 +166,7 @@ __device__ __forceinline__ unsigned list_slot(const TileMap &T, unsigned e) {
 // exact membership test at the step-start positions pos0.
 template <int NB = kGatherBatch, class Fetch, class Use>
 __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__restrict__ start,
-                                             const TileMap &T, const unsigned short *__restrict__ list,
+                                             const TileMap &T, const ListEntry *__restrict__ list,
                                              const int *__restrict__ nbr, const float4 *__restrict__ pos0,
                                              unsigned cellw, int i, Fetch &&fetch, Use &&use) {
     if (cellw & kWide) {
@@ -163,7 +181,7 @@ __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__
     }
     const int cnt = __ldg(&nbr[i]) - 1;   // members other than i
     const size_t n = (size_t)P.n;
-    const unsigned short *l = list + i;
+    const ListEntry *l = list + i;
     for (int q = 0; q < cnt; q += NB) {
         unsigned j[NB];
 #pragma unroll
