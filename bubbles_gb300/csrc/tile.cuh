@@ -1,19 +1,21 @@
-// tile.cuh -- tiles of the neighbour passes and the compact neighbour lists.
+// tile.cuh -- tiles of the neighbour passes and the neighbour lists.
 //
 // Every neighbour pass runs one thread per particle in blocks of consecutive slots of the
-// cell-sorted arrays (a "tile": the block size, 64 to 256, a tuning parameter).  The 27 neighbour cells of any particle in a tile
-// lie, for each of the 9 (dy, dz) row offsets r, inside one contiguous range of linear
-// cell ids, [first cell - 1 + off_r, last cell + 1 + off_r], i.e. one contiguous slot
-// range starting at lo[r].  A neighbour j of a particle is therefore stored in 16 bits
-// as (r << 12) | (j - lo[r]); every pass rebuilds the tile's 9 range starts from the
-// grid (two loads per range) and decodes j = lo[r] + offset.
+// cell-sorted arrays (a "tile": the block size, 64 to 256, a tuning parameter).
 //
-// Lists are member-major, one 16-bit entry per member: entry q of particle i is
-// list[q * n + i], so the density pass writes entry q of 32 particles with one
-// coalesced 64-byte store and the later passes read them the same way, eight entries
-// requested before any neighbour is gathered.  A particle with more than kMaxList
-// members, or with a member more than 4,095 slots into its range, is "wide" (kWide in its
-// cell word) and re-tests its 27 cells exactly on every pass instead.
+// The density pass records each particle's neighbour set (the reference bucket) as a
+// list, member-major: entry q of particle i is list[q * n + i], so entry q of 32
+// particles is written and read with one coalesced access.  Later passes request several
+// entries and then the neighbours' records before using any (tile_members).  A particle
+// with more than kMaxList members is "wide" (kWide in its cell word) and re-tests its 27
+// cells exactly on every pass instead.
+//
+// Entries are absolute slot indices (32 bit).  A build-time alternative
+// (BBG_LIST_BITS=16) halves the list: the 27 neighbour cells of any particle in a tile
+// lie, for each of the 9 (dy, dz) row offsets r, inside one contiguous slot range starting
+// at lo[r] ([first cell - 1 + off_r, last cell + 1 + off_r] in linear cell ids), so j is
+// stored as (r << 12) | (j - lo[r]) and every pass rebuilds the tile's 9 starts; on GB300
+// the decoding cost more issue slots than the smaller list saved (13-16 % slower steps).
 #pragma once
 
 #include "bbg_internal.cuh"
@@ -35,10 +37,11 @@ struct TileMap {
 };
 
 #ifndef BBG_LIST_BITS
-#define BBG_LIST_BITS 16
+#define BBG_LIST_BITS 32
 #endif
 #if BBG_LIST_BITS == 32
-// build-time alternative: absolute slot indices (4 bytes per member, no decoding)
+// absolute slot indices (4 bytes per member, no decoding): measured faster on GB300 than
+// the 16-bit tile-relative entries, whose decoding costs issue slots in every pass
 using ListEntry = unsigned;
 __device__ __forceinline__ unsigned list_slot(const TileMap &, unsigned e) { return e; }
 __device__ __forceinline__ unsigned list_code(unsigned j, unsigned) { return j; }
@@ -54,9 +57,11 @@ __device__ __forceinline__ unsigned short list_code(unsigned j, unsigned base) {
 constexpr bool kListRelative = true;
 #endif
 
-// The tile's 9 range starts from the grid (all threads of the block must call it).
+// The tile's 9 range starts from the grid (all threads of the block must call it; a
+// no-op with absolute list entries).
 __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
                                            const unsigned *__restrict__ start, int n, TileMap &T) {
+    if (!kListRelative) return;
     if (threadIdx.x < 9) {
         const int s0 = blockIdx.x * blockDim.x;
         const int r = threadIdx.x;
