@@ -64,7 +64,8 @@ class MlpDesc(ctypes.Structure):
                 ("beta2", ctypes.c_double),
                 ("epsilon", ctypes.c_double),
                 ("seed", ctypes.c_ulonglong),
-                ("expectile", ctypes.c_double)]
+                ("expectile", ctypes.c_double),
+                ("finetune_steps", ctypes.c_int)]
 
 
 class SceneDesc(ctypes.Structure):

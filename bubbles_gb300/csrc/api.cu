@@ -226,7 +226,8 @@ std::vector<float> mlp_initial_params(unsigned long long seed) {
 }
 
 bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
-    if (d.batch < 1 || d.train_substeps < 0 || d.steps_per_substep < 0 || !(d.learning_rate > 0) ||
+    if (d.batch < 1 || d.train_substeps < 0 || d.steps_per_substep < 0 || d.finetune_steps < 0 ||
+        !(d.learning_rate > 0) ||
         !(d.expectile > 0 && d.expectile < 1))
         return fail(BBG_ERR_INVALID_ARGUMENT, "invalid MLP training settings");
     CK(cudaStreamSynchronize(s->stream));
@@ -402,11 +403,18 @@ static void launch_prologue(bbg_solver s, int work, float dt, float delta, int m
 }
 
 // After a training substep's corrector: Adam steps on pairs of the converged state.
+// (A learned substep runs finetune_steps of them on its own converged pressure.)
+static int training_steps(bbg_solver s) {
+    const int mm = mlp_mode(s);
+    return mm == 1 ? s->mdesc.steps_per_substep : mm == 2 ? s->mdesc.finetune_steps : 0;
+}
+
 static void launch_training(bbg_solver s, float delta, cudaStream_t cs) {
     const bbg_mlp_desc &d = s->mdesc;
+    const int steps = training_steps(s);
     cudaMemsetAsync(s->mlp.loss, 0, sizeof(double), cs);
-    s->mlp_loss_count = (double)s->mlp.batch * (double)(d.steps_per_substep > 0 ? d.steps_per_substep : 1);
-    for (int k = 0; k < d.steps_per_substep; k++) {
+    s->mlp_loss_count = (double)s->mlp.batch * (double)(steps > 0 ? steps : 1);
+    for (int k = 0; k < steps; k++) {
         launch_mlp_collect(s->P, s->B, s->mlp, pressure_unit(s, delta), cs);
         launch_mlp_train_step(s->mlp, s->mlp.bx, s->mlp.bt, s->mlp.batch, (float)d.learning_rate,
                               (float)d.beta1, (float)d.beta2, (float)d.epsilon, (float)d.expectile, cs);
@@ -507,7 +515,7 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
         }
         if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1,
                                                                       cudaStreamSetCaptureDependencies);
-        if (mlp_mode(s) == 1) launch_training(s, delta, cs);
+        if (training_steps(s) > 0) launch_training(s, delta, cs);
     }
     const float pv = (float)s->desc.pseudo_viscosity * dt;
     if (pv > 0.1) {
@@ -600,11 +608,11 @@ bbg_status substep(bbg_solver s, float dt) {
     s->valid |= bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE);
     r = corrector(s, dt, delta, max_it);
     if (r) return r;
-    if (mlp_mode(s) == 1) {
+    if (training_steps(s) > 0) {
         launch_training(s, delta, s->stream);
         CK_LAUNCH();
-        s->mlp_trained++;
     }
+    if (mlp_mode(s) == 1) s->mlp_trained++;
     return pseudo_viscosity(s, dt);
 }
 
@@ -1346,6 +1354,7 @@ bbg_status bbg_mlp_desc_default(bbg_mlp_desc *d) {
     d->epsilon = 1e-8;
     d->seed = 20240601ull;
     d->expectile = 0.5;
+    d->finetune_steps = 0;
     return BBG_OK;
 }
 

@@ -38,6 +38,12 @@ constexpr int kThreads = kTile;
 constexpr int kNbrMinBlocks = BBG_NBR_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kPfMinBlocks = BBG_PF_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kDensityMinBlocks = 12 * kTile / kMaxTile;
+#ifndef BBG_DENSITY_MASK
+#define BBG_DENSITY_MASK 1
+#endif
+// density pass: branch-free candidate loop with membership bit masks (build-time choice;
+// measured 4 % faster than the branchy loop on GB300)
+constexpr bool kDensityMask = BBG_DENSITY_MASK != 0;
 
 // a neighbour's position and velocity records
 struct PosVel {
@@ -92,6 +98,33 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
         sum = 1.f;
         cnt = 1;
         atomicAdd(&st->crowded, 1u);
+    } else if (kDensityMask) {
+        // branch-free candidate loop: membership of up to 32 consecutive candidates as a bit
+        // mask, the list entries of the members written afterwards
+        tile_rows(P.g, start, cw & ~kWide, [&](int r, unsigned b, unsigned e) {
+            const unsigned base = kListRelative ? ((unsigned)r << kOffBits) - (unsigned)T.lo[r] : 0u;
+            if (kListRelative && e - (unsigned)T.lo[r] > (unsigned)kOffLimit) fits = false;
+            for (unsigned cb = b; cb < e; cb += 32u) {
+                const unsigned ce = min(e, cb + 32u);
+                unsigned m = 0u;
+                for (unsigned j = cb; j < ce; ++j) {
+                    const float4 pj = __ldg(&pos[j]);
+                    const float r2 = dist2(pi, pj);
+                    const bool mem = r2 < P.nb_lo || (r2 <= P.nb_hi && std_member_exact(P, pi, pj));
+                    const float x = 1.f - r2 * P.inv_h2;
+                    sum += mem ? x * x * x : 0.f;
+                    m |= (unsigned)mem << (j - cb);
+                }
+                cnt += __popc(m);
+                if ((unsigned)i - cb < ce - cb) m &= ~(1u << ((unsigned)i - cb));   // the particle itself
+                while (m) {
+                    const unsigned j = cb + (unsigned)(__ffs((int)m) - 1);
+                    m &= m - 1u;
+                    if (listed < kMaxList) list[(size_t)listed * n + (size_t)i] = list_code(j, base);
+                    listed++;
+                }
+            }
+        });
     } else tile_candidates_coded(P.g, start, T, cw & ~kWide, &fits, [&](unsigned j, unsigned base) {
         const float4 pj = __ldg(&pos[j]);
         const float r2 = dist2(pi, pj);

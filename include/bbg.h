@@ -158,6 +158,8 @@ typedef struct {
     double expectile;          /* training loss: squared error weighted (1 - tau) above and
                                   tau below the target (0.5: mean squared error); tau < 0.5
                                   biases estimates low, which suits the monotone update */
+    int finetune_steps;        /* Adam steps after each learned substep on its own converged
+                                  pressure (0: the model is fixed after training) */
 } bbg_mlp_desc;
 
 /* ----- library ----------------------------------------------------------- */
