@@ -280,13 +280,12 @@ def cpu_sample(scene, pos, vel, depth):
 
 
 def launches_per_substep(scene, variant, iters):
-    """Kernels one graph-launched PCISPH substep runs: 4 grid-rebuild kernels (hash and
-    count, scan, place, rank and gather; the scan is 3 launches), density, non-pressure,
-    3 per corrector iteration (predicted density, pressure force, loop control), plus the
-    warm start (start pressure, pressure force) and, learned, the feature pass; 2 more when
-    pseudo-viscosity is active."""
+    """Kernels one graph-launched PCISPH substep runs: 6 for the grid rebuild (hash and
+    count, 3 scan kernels, place, rank and gather), density, non-pressure, 3 per corrector
+    iteration (predicted density, pressure force, loop control), plus the warm start (one
+    kernel; learned: features and the MLP); 2 more when pseudo-viscosity is active."""
     pv = 2 if scene.get("pseudo_viscosity", 10.0) * scene["dt"] > 0.1 else 0
-    extra = {"plain": 0, "warm": 2, "learned": 3}[variant]
+    extra = {"plain": 0, "warm": 1, "learned": 2}[variant]
     return 8 + extra + 3 * iters + pv
 
 
@@ -355,12 +354,15 @@ def run_ours(args, scene, pos):
         # every region below replays the same K substeps from this state
         snap_p, snap_v = g.download()
         snap_pr = g.get(bb.FIELD_PRESSURE) if warm else None
+        snap_dv = g.get(bb.FIELD_DIVERGENCE) if variant == "learned" else None
         list_len = float(np.minimum(g.neighbor_counts() - 1, 64).mean())
 
         def restore(solver, with_pressure):
             solver.upload(snap_p, snap_v)
             if with_pressure:
                 solver.set(bb.FIELD_PRESSURE, snap_pr)
+                if snap_dv is not None:
+                    solver.set(bb.FIELD_DIVERGENCE, snap_dv)
             torch.cuda.synchronize()
         barrier(dist)
 
@@ -415,21 +417,29 @@ def run_ours(args, scene, pos):
         pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
         vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
         pr_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+        dv_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+        learned = variant == "learned"
 
         def e2e_step():
             g.upload(pos_h, vel_h)
             if warm:
                 g.set(bb.FIELD_PRESSURE, pr_h)
+            if learned:
+                g.set(bb.FIELD_DIVERGENCE, dv_h)
             g.advance_time_step(dt)
             g.download(pos_h, vel_h)
             if warm:
                 g.get(bb.FIELD_PRESSURE, out=pr_h)
+            if learned:
+                g.get(bb.FIELD_DIVERGENCE, out=dv_h)
 
         def e2e_reset():
             pos_h[:] = snap_p
             vel_h[:] = snap_v
             if warm:
                 pr_h[:] = snap_pr
+            if learned:
+                dv_h[:] = snap_dv
         e2e_reset()
         for _ in range(max(1, args.warmup)):
             e2e_step()
@@ -530,8 +540,9 @@ def run_ours(args, scene, pos):
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (28 if warm else 24),
-                "d2h_bytes_per_step": n * (28 if warm else 24)},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": n * (24 + (4 if warm else 0) + (4 if variant == "learned" else 0)),
+                "d2h_bytes_per_step": n * (24 + (4 if warm else 0) + (4 if variant == "learned" else 0))},
         "roofline": roof,
         "cpu_baseline": cpu,
         "gpu_launches": launches_timed,

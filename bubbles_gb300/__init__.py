@@ -20,3 +20,4 @@ FIELD_PRED_POSITION = native.FIELD_PRED_POSITION
 FIELD_PRESSURE_FORCE = native.FIELD_PRESSURE_FORCE
 FIELD_PRED_DENSITY = native.FIELD_PRED_DENSITY
 FIELD_DENSITY_ERROR = native.FIELD_DENSITY_ERROR
+FIELD_DIVERGENCE = native.FIELD_DIVERGENCE

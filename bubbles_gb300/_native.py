@@ -22,6 +22,7 @@ MAX_COLLIDERS = 16
 FIELD_POSITION, FIELD_VELOCITY, FIELD_FORCE, FIELD_INTERACTION = 0, 1, 2, 3
 FIELD_DENSITY, FIELD_PRESSURE, FIELD_PRED_POSITION = 4, 5, 6
 FIELD_PRESSURE_FORCE, FIELD_PRED_DENSITY, FIELD_DENSITY_ERROR = 8, 9, 10
+FIELD_DIVERGENCE = 11
 VECTOR_FIELDS = {FIELD_POSITION, FIELD_VELOCITY, FIELD_FORCE, FIELD_INTERACTION,
                  FIELD_PRED_POSITION, FIELD_PRESSURE_FORCE}
 

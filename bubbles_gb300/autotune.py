@@ -52,17 +52,24 @@ def make(scene, pos):
     return Solver(scene, pos=pos)
 
 
+FIELD_PRESSURE, FIELD_DIVERGENCE = 5, 11
+
+
+def restore(g, snap):
+    p, v, pr, dv = snap
+    g.upload(p, v)
+    if pr is not None:
+        g.set(FIELD_PRESSURE, pr)
+    if dv is not None:
+        g.set(FIELD_DIVERGENCE, dv)
+
+
 def time_substeps(g, dt, snap, steps, warm):
     """Seconds for `steps` substeps from the snapshot (after two untimed ones)."""
-    p, v, pr = snap
-    g.upload(p, v)
-    if warm:
-        g.set(5, pr)   # FIELD_PRESSURE
+    restore(g, snap)
     for _ in range(2):
         g.advance_time_step(dt)
-    g.upload(p, v)
-    if warm:
-        g.set(5, pr)
+    restore(g, snap)
     g.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -106,8 +113,9 @@ def tune(config, prep=100, steps=20, variant="plain", seed=0):
         for _ in range(prep):
             g.advance_time_step(dt)
         p, v = g.download()
-        pr = g.get(5) if warm else None
-        best, t = tune_launches(g, dt, (p, v, pr), steps, warm, log)
+        pr = g.get(FIELD_PRESSURE) if warm else None
+        dv = g.get(FIELD_DIVERGENCE) if variant == "learned" else None
+        best, t = tune_launches(g, dt, (p, v, pr, dv), steps, warm, log)
         results.append((t, scale, best))
         g.close()
     t, scale, best = min(results, key=lambda r: r[0])

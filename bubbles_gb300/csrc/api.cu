@@ -203,7 +203,7 @@ bbg_status free_all(bbg_solver s) {
 void free_mlp(bbg_solver s) {
     MlpBufs &M = s->mlp;
     void *ptrs[] = {M.theta, M.grad, M.m1, M.m2, M.w1f, M.w2f, M.tail, M.step, M.loss, M.feat, M.divsum,
-                    M.bx, M.bt};
+                    M.divprev, M.bx, M.bt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     M = MlpBufs();
@@ -239,7 +239,8 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
 #define ALLOC(ptr, cnt) if (!r) r = dalloc(&(ptr), (cnt))
         ALLOC(M.theta, kParams); ALLOC(M.grad, kParams); ALLOC(M.m1, kParams); ALLOC(M.m2, kParams);
         ALLOC(M.w1f, 8 * 32); ALLOC(M.w2f, 64 * 32); ALLOC(M.tail, kTail); ALLOC(M.step, 1);
-        ALLOC(M.loss, 1); ALLOC(M.feat, n); ALLOC(M.divsum, n); ALLOC(M.bx, (size_t)d.batch);
+        ALLOC(M.loss, 1); ALLOC(M.feat, n); ALLOC(M.divsum, n); ALLOC(M.divprev, n);
+        ALLOC(M.bx, (size_t)d.batch);
         ALLOC(M.bt, (size_t)d.batch);
 #undef ALLOC
         if (r) {
@@ -263,6 +264,8 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
     CK(cudaMemsetAsync(M.step, 0, sizeof(unsigned), s->stream));
     CK(cudaMemsetAsync(M.loss, 0, sizeof(double), s->stream));
     CK(cudaMemsetAsync(M.feat, 0, sizeof(float4) * (size_t)s->capacity, s->stream));
+    CK(cudaMemsetAsync(M.divsum, 0, sizeof(float) * (size_t)s->capacity, s->stream));
+    CK(cudaMemsetAsync(M.divprev, 0, sizeof(float) * (size_t)s->capacity, s->stream));
     CK(cudaMemsetAsync(M.tail, 0, sizeof(float) * kTail, s->stream));
     launch_mlp_pack(M, s->stream);
     CK_LAUNCH();
@@ -303,7 +306,7 @@ bbg_status reset_step_state(bbg_solver s) {
 bbg_status grid_update(bbg_solver s) {
     bbg_status r = reset_step_state(s);
     if (r) return r;
-    launch_grid_update(s->P, s->B, s->state, s->pid_cur, s->stream);
+    launch_grid_update(s->P, s->B, s->state, s->pid_cur, s->stream, s->mlp.divsum, s->mlp.divprev);
     CK_LAUNCH();
     s->state = 1 - s->state;
     s->pid_cur = 1 - s->pid_cur;
@@ -389,17 +392,19 @@ static float pressure_unit(bbg_solver s, float delta) { return delta * s->P.targ
 
 // Launches of a substep between the density pass and the corrector loop.
 static void launch_prologue(bbg_solver s, int work, float dt, float delta, int max_it, cudaStream_t cs) {
+    (void)max_it;
     const Params &P = s->P;
     const DevBufs &B = s->B;
     const int mm = mlp_mode(s);
     const bool warm = warm_active(s);
-    launch_non_pressure(P, B, work, warm ? 0 : 1, dt, dt / s->mass, cs, mm ? s->mlp.divsum : nullptr);
+    // the warm start (start pressure, pos.w = p / rho^2) precedes the force pass, which then
+    // also sums the start's pressure force and predicts x* from F + Fp
     if (mm) launch_mlp_features(P, B, s->mlp, work, dt, pressure_unit(s, delta), cs);
     if (warm) {
         if (mm == 2) launch_mlp_warm_start(P, B, s->mlp, work, pressure_unit(s, delta), warm_scale(s), cs);
         else launch_warm_start(P, B, work, warm_scale(s), cs);
-        launch_pressure_force(P, B, work, 0, max_it, dt, dt / s->mass, cs, 2);
     }
+    launch_non_pressure(P, B, work, 1, dt, dt / s->mass, cs, mm ? s->mlp.divsum : nullptr, warm);
 }
 
 // After a training substep's corrector: Adam steps on pairs of the converged state.
@@ -480,7 +485,7 @@ bbg_status capture_substep(bbg_solver s, float dt, int max_it, float delta,
     cudaError_t e = cudaMemsetAsync(B.st, 0, sizeof(StepState), cs);
     if (e == cudaSuccess && s->nscenes > 0)
         e = cudaMemsetAsync(s->d_sst, 0, sizeof(SceneState) * (size_t)s->nscenes, cs);
-    launch_grid_update(P, B, st0, pid0, cs);
+    launch_grid_update(P, B, st0, pid0, cs, s->mlp.divsum, s->mlp.divprev);
     if (s->desc.solver_kind == BBG_SOLVER_SPH) {
         launch_density(P, B, work, 1, cs);
         launch_sph_forces(P, B, work, dt, cs);
@@ -632,7 +637,7 @@ int field_components(int f) {
         case BBG_FIELD_INTERACTION: case BBG_FIELD_PRED_POSITION: case BBG_FIELD_PRESSURE_FORCE:
             return 3;
         case BBG_FIELD_DENSITY: case BBG_FIELD_PRESSURE: case BBG_FIELD_PRED_DENSITY:
-        case BBG_FIELD_DENSITY_ERROR:
+        case BBG_FIELD_DENSITY_ERROR: case BBG_FIELD_DIVERGENCE:
             return 1;
         default:
             return 0;
@@ -656,6 +661,7 @@ float *scalar_field(bbg_solver s, int f) {
         case BBG_FIELD_PRESSURE: return s->B.press;
         case BBG_FIELD_PRED_DENSITY: return s->B.rhostar;
         case BBG_FIELD_DENSITY_ERROR: return s->B.derr;
+        case BBG_FIELD_DIVERGENCE: return s->mlp_alloc ? s->mlp.divsum : nullptr;
         default: return nullptr;
     }
 }
@@ -895,6 +901,8 @@ bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count) {
 static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d_vel, int n) {
     launch_upload(s->B, s->state, s->pid_cur, d_pos, d_vel, n, s->stream);
     CK_LAUNCH();
+    if (s->mlp_alloc)   // no previous substep: no divergence to carry (bbg_set_field can set it)
+        CK(cudaMemsetAsync(s->mlp.divsum, 0, sizeof(float) * (size_t)n, s->stream));
     if (n != s->n) s->epoch++;   // captured launches depend on n, not on the data
     s->n = n;
     s->P.n = n;
@@ -1210,7 +1218,7 @@ bbg_status bbg_get_field(bbg_solver s, int field, float *out) {
     const int comps = field_components(field);
     if (!comps || !out) return fail(BBG_ERR_INVALID_ARGUMENT, "unknown field %d", field);
     if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
-    if (!(s->valid & bit(field)))
+    if (field == BBG_FIELD_DIVERGENCE ? !s->mlp_alloc : !(s->valid & bit(field)))
         return fail(BBG_ERR_STATE, "field %d is not valid in the current particle order", field);
     const size_t n = (size_t)s->n;
     if (field == BBG_FIELD_INTERACTION) {
@@ -1234,6 +1242,8 @@ bbg_status bbg_set_field(bbg_solver s, int field, const float *in) {
     const int comps = field_components(field);
     if (!comps || !in || field == BBG_FIELD_INTERACTION)
         return fail(BBG_ERR_INVALID_ARGUMENT, "field %d cannot be set", field);
+    if (field == BBG_FIELD_DIVERGENCE && !s->mlp_alloc)
+        return fail(BBG_ERR_STATE, "the divergence field belongs to the learned warm start");
     if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
     const size_t n = (size_t)s->n;
     CK(cudaMemcpyAsync(s->B.stage, in, sizeof(float) * comps * n, cudaMemcpyHostToDevice, s->stream));

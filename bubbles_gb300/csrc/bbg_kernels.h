@@ -53,8 +53,9 @@ size_t scan_partials_needed(unsigned cells);
 // exclusive scan of per-cell counts into start[0..cells] (zeroes the counts)
 void launch_cell_scan(unsigned *count, unsigned cells, unsigned *partials, unsigned *start,
                       cudaStream_t s);
+// carry_in / carry_out (optional): one float per particle gathered into the new order
 void launch_grid_update(const Params &P, const DevBufs &B, int src_buf, int pid_src,
-                        cudaStream_t s);
+                        cudaStream_t s, const float *carry_in = nullptr, float *carry_out = nullptr);
 void launch_upload(const DevBufs &B, int buf, int pid_buf, const float *d_pos, const float *d_vel,
                    int n, cudaStream_t s);
 void launch_download(const DevBufs &B, int buf, int pid_buf, float *d_pos, float *d_vel, int n,
@@ -72,9 +73,10 @@ void launch_max_force(const float4 *force, int n, unsigned *out_bits, cudaStream
 // sph.cu
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure,
                     cudaStream_t s);
-// divsum != null: also the velocity-divergence sum of each particle (learned warm start)
+// divsum != null: also the velocity-divergence sum of each particle (learned warm start);
+// warm: the corrector's start pressure is set, add its pressure force and predict from F + Fp
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
-                         float dt_over_m, cudaStream_t s, float *divsum = nullptr);
+                         float dt_over_m, cudaStream_t s, float *divsum = nullptr, bool warm = false);
 void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_first, float dt,
                           float dt_over_m, cudaStream_t s);
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);

@@ -141,7 +141,8 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
               const float4 *__restrict__ vel_in, float4 *__restrict__ pos_out,
               float4 *__restrict__ vel_out, int *__restrict__ pid_out, int *__restrict__ slot,
               unsigned *__restrict__ cell, const float *__restrict__ press_in,
-              float *__restrict__ pprev, StepState *st) {
+              float *__restrict__ pprev, StepState *st, const float *__restrict__ carry_in,
+              float *__restrict__ carry_out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const uint2 e = tmp[t];
@@ -161,6 +162,7 @@ k_rank_gather(int n, const uint2 *__restrict__ tmp, const unsigned *__restrict__
     slot[e.x] = (int)dst;
     cell[dst] = c;
     pprev[dst] = press_in[e.y];   // carried for a warm-started corrector
+    if (carry_out) carry_out[dst] = carry_in[e.y];
 }
 
 size_t scan_partials_needed(unsigned cells) { return (size_t)blocks_for(cells, kScanTile) + 1; }
@@ -173,7 +175,8 @@ void launch_cell_scan(unsigned *count, unsigned cells, unsigned *partials, unsig
     k_scan_apply<<<nb, kScanThreads, 0, s>>>(count, cells, partials, start);
 }
 
-void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src, cudaStream_t s) {
+void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src, cudaStream_t s,
+                        const float *carry_in, float *carry_out) {
     const int n = P.n;
     const unsigned cells = P.g.total;
     const int nb = blocks_for(cells, kScanTile);
@@ -194,7 +197,7 @@ void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src,
     BBG_PBEGIN(B, KID_RANK_GATHER, s, -1);
     k_rank_gather<<<blocks_for(n, kThreads), kThreads, 0, s>>>(
         n, B.tmp, B.cell_old, B.start, B.pos[src], B.vel[src], B.pos[1 - src], B.vel[1 - src],
-        B.pid[1 - pid_src], B.slot, B.cell, B.press, B.pprev, B.st);
+        B.pid[1 - pid_src], B.slot, B.cell, B.press, B.pprev, B.st, carry_in, carry_out);
     BBG_PEND(B, s);
 }
 

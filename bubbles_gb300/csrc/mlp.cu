@@ -3,7 +3,8 @@
 // A per-particle MLP 4 -> 64 -> 64 -> 1 with GELU (tanh form) maps the features of a
 // particle at the start of a substep to an estimate of its converged corrector pressure:
 //   f0 = 100 (rho - rho0) / rho0                 local density error, percent
-//   f1 = -100 dt div(v)                          compression expected over the substep
+//   f1 = -100 dt div(v)                          compression rate (velocity divergence of the
+//                                                previous substep's non-pressure pass)
 //   f2 = (neighbours - 1) / 32                   neighbour count
 //   f3 = p_prev / p_unit                         previous substep's converged pressure
 // and the target is p / p_unit, with p_unit = delta * rho0 / 100 the pressure one
@@ -93,8 +94,9 @@ __device__ __forceinline__ uint32_t layer1_a(float4 f, int t) {
 
 }  // namespace
 
-// Per-particle features at the start of a substep (the density and non-pressure passes
-// have run: vel.w = 1 / rho, div = the velocity divergence sum of the non-pressure pass).
+// Per-particle features at the start of a substep, right after the density pass (vel.w =
+// 1 / rho); the divergence is the previous substep's sum (its non-pressure pass), carried
+// through the grid rebuild, so the warm start can precede this substep's force pass.
 __global__ void k_mlp_features(int n, const float4 *__restrict__ vel, const float *__restrict__ divsum,
                                const int *__restrict__ nbr, const float *__restrict__ pprev,
                                float4 *__restrict__ feat, float inv_rho0, float div_scale,
@@ -424,7 +426,7 @@ void launch_mlp_features(const Params &P, const DevBufs &B, const MlpBufs &M, in
                          float p_unit, cudaStream_t s) {
     // div = m * spiky_dw_c * divsum (non-pressure pass); f1 = -100 dt div
     const float div_scale = -100.f * dt * P.mass * P.spiky_dw_c;
-    k_mlp_features<<<blocks_for(P.n, 256), 256, 0, s>>>(P.n, B.vel[buf], M.divsum, B.nbr, B.pprev, M.feat,
+    k_mlp_features<<<blocks_for(P.n, 256), 256, 0, s>>>(P.n, B.vel[buf], M.divprev, B.nbr, B.pprev, M.feat,
                                                          1.f / P.target_density, div_scale, 1.f / p_unit);
 }
 

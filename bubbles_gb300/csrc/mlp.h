@@ -29,7 +29,8 @@ struct MlpBufs {
     unsigned *step = nullptr;  // Adam steps taken
     double *loss = nullptr;    // sum of squared errors of the training batches
     float4 *feat = nullptr;    // per-particle features (sorted slots)
-    float *divsum = nullptr;   // velocity-divergence sum of the non-pressure pass
+    float *divsum = nullptr;   // velocity-divergence sum of this substep's non-pressure pass
+    float *divprev = nullptr;  // the previous substep's, carried into the current order
     float4 *bx = nullptr;      // training batch: features
     float *bt = nullptr;       //                 targets (pressure / p_unit)
     int batch = 0;

@@ -156,10 +156,14 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
 }
 
 // ComputeNonPressureForceFor (sph_equations3.cpp:80-110), optionally followed by the
-// k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).  With DIV it also
-// accumulates sum_j (1/rho_j) (1 - d/h)^2 / d (v_j - v_i).(x_j - x_i), the velocity
-// divergence up to m * 45 / (pi h^4), a feature of the learned warm start.
-template <bool DIV, int NB>
+// k = 0 PredictVelocityAndPositionFor (pcisph_equations3.cpp:3-28).
+//   predict 0: forces only; 1: the reference's k = 0 prediction (p = 0, Fp = 0, x* from F);
+//   WARM: the corrector's warm start has set p and pos.w = p / rho^2 for every particle,
+//   so the same member walk also sums the pressure force of that start
+//   (PredictPressureForceFor, pcisph_equations3.cpp:114-155) and x* comes from F + Fp.
+// With DIV it also accumulates sum_j (1/rho_j) (1 - d/h)^2 / d (v_j - v_i).(x_j - x_i),
+// the velocity divergence up to m * 45 / (pi h^4), a feature of the learned warm start.
+template <bool DIV, bool WARM, int NB>
 __global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
 k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                const unsigned *__restrict__ cell,
@@ -172,11 +176,14 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const float4 vi = vel[i];
+    const float ai = pi.w;   // WARM: p_i / rho_i^2
     float fx = P.mass * P.gx - P.drag * vi.x;
     float fy = P.mass * P.gy - P.drag * vi.y;
     float fz = P.mass * P.gz - P.drag * vi.z;
+    float tx = 0.f, ty = 0.f, tz = 0.f;
     float dv = 0.f;
     const float kv = P.visc_m2 * P.spiky_d2w_c;
+    const float kg = P.m2 * P.spiky_dw_c;
     tile_members<NB>(
         P, start, T, list, nbr, pos, cell[i], i,
         [&](unsigned j) { return PosVel{__ldg(&pos[j]), __ldg(&vel[j])}; },
@@ -190,6 +197,15 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
             fx += (vj.x - vi.x) * w;
             fy += (vj.y - vi.y) * w;
             fz += (vj.z - vi.z) * w;
+            if (WARM) {
+                // as k_pressure_force: IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
+                if (d - P.h <= -P.iz && d >= P.iz) {
+                    const float c = kg * (ai + pj.w) * x * x * inv_d;
+                    tx += (pj.x - pi.x) * c;
+                    ty += (pj.y - pi.y) * c;
+                    tz += (pj.z - pi.z) * c;
+                }
+            }
             if (DIV && r2 > 0.f) {
                 const float dot = (vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) +
                                   (vj.z - vi.z) * (pj.z - pi.z);
@@ -198,7 +214,13 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
         });
     force[i] = make_float4(fx, fy, fz, 0.f);
     if (DIV) divsum[i] = dv;
-    if (predict) {
+    if (WARM) {
+        const v3 fp = V(-tx, -ty, -tz);
+        pforce[i] = F4(fp);
+        v3 xs;
+        predict_particle(P, dt, dt_over_m, V(fx, fy, fz), fp, V(pi), V(vi), &xs);
+        xstar[i] = F4(xs);
+    } else if (predict) {
         press[i] = 0.f;
         pforce[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         v3 xs;
@@ -565,14 +587,14 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
     BBG_PEND(B, s);
 }
 
-template <bool DIV>
+template <bool DIV, bool WARM>
 static void non_pressure_nb(const Params &P, const DevBufs &B, int buf, int predict, float dt,
                             float dt_over_m, cudaStream_t s, float *divsum) {
     const int t = B.tune.block;
-#define NP_LAUNCH(NB)                                                                                   \
-    k_non_pressure<DIV, NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, \
-                                                            B.list, B.nbr, B.force, B.xstar, B.pforce,  \
-                                                            B.press, divsum, predict, dt, dt_over_m)
+#define NP_LAUNCH(NB)                                                                        \
+    k_non_pressure<DIV, WARM, NB><<<blocks_for(P.n, t), t, 0, s>>>(                          \
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, \
+        B.press, divsum, predict, dt, dt_over_m)
     switch (B.tune.batch_np) {
         case 2: NP_LAUNCH(2); break;
         case 8: NP_LAUNCH(8); break;
@@ -582,10 +604,15 @@ static void non_pressure_nb(const Params &P, const DevBufs &B, int buf, int pred
 }
 
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,
-                         float dt_over_m, cudaStream_t s, float *divsum) {
+                         float dt_over_m, cudaStream_t s, float *divsum, bool warm) {
     BBG_PBEGIN(B, KID_NON_PRESSURE, s, -1);
-    if (divsum) non_pressure_nb<true>(P, B, buf, predict, dt, dt_over_m, s, divsum);
-    else non_pressure_nb<false>(P, B, buf, predict, dt, dt_over_m, s, nullptr);
+    if (divsum) {
+        if (warm) non_pressure_nb<true, true>(P, B, buf, predict, dt, dt_over_m, s, divsum);
+        else non_pressure_nb<true, false>(P, B, buf, predict, dt, dt_over_m, s, divsum);
+    } else {
+        if (warm) non_pressure_nb<false, true>(P, B, buf, predict, dt, dt_over_m, s, nullptr);
+        else non_pressure_nb<false, false>(P, B, buf, predict, dt, dt_over_m, s, nullptr);
+    }
     BBG_PEND(B, s);
 }
 

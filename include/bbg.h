@@ -83,6 +83,9 @@ typedef int bbg_status;
 #define BBG_FIELD_PRESSURE_FORCE 8
 #define BBG_FIELD_PRED_DENSITY 9
 #define BBG_FIELD_DENSITY_ERROR 10
+/* Learned warm start only: each particle's velocity-divergence sum of the last substep,
+ * a feature of the next one (the state a host round trip must carry, with the pressure). */
+#define BBG_FIELD_DIVERGENCE 11
 
 typedef struct bbg_solver_s *bbg_solver;
 

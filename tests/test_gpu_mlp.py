@@ -91,29 +91,45 @@ def test_mlp_training_reduces_loss(gpu, small):
 
 
 def test_features_match_definitions(gpu, moved):
+    """Features of a substep: density error and neighbour count of its start state, the
+    previous substep's pressure, and the velocity divergence of the previous substep's
+    start state (carried, so the warm start can precede the force pass)."""
     sc, p, v = moved
     g = learned_solver(sc, p, v, train_substeps=1000)
     g.advance_time_step(sc["dt"])
+    f0 = g.mlp_features()
+    assert np.all(f0[:, 1] == 0.0)   # nothing carried across an upload
+    assert np.all(f0[:, 3] == 0.0)
+    p1, v1 = g.download()
+    pr1 = g.get(bb.FIELD_PRESSURE)
+    div1 = g.get(bb.FIELD_DIVERGENCE)   # computed by the first substep at (p, v)
+    g.advance_time_step(sc["dt"])
     f = g.mlp_features()
-    o = O.OracleSim(sc, p, v, variant="f64")
+    o = O.OracleSim(sc, p1, v1, variant="f64")
     o.update_grid_distribution()
     o.compute_density(0)
     rho = o.get(O.DENSITY)
     assert np.max(np.abs(f[:, 0] - 100.0 * (rho / 1000.0 - 1.0))) <= 1e-3
     counts = g.neighbor_counts()
     assert np.array_equal(f[:, 2], ((counts - 1) / 32.0).astype(np.float32))
-    assert np.all(f[:, 3] == 0.0)   # no previous pressure after an upload
-    # velocity divergence: brute force over the step-start neighbour sets
+    delta = o.compute_delta(sc["dt"])
+    p_unit = np.float32(delta) * np.float32(1000.0) * np.float32(0.01)
+    assert np.allclose(f[:, 3], pr1 / p_unit, rtol=1e-5, atol=1e-6)
+    # velocity divergence of (p, v): brute force over the step-start neighbour sets
     h = 2.0 * sc["spacing"]
+    o0 = O.OracleSim(sc, p, v, variant="f64")
+    o0.update_grid_distribution()
+    o0.compute_density(0)
+    rho0 = o0.get(O.DENSITY)
     d = p[:, None, :] - p[None, :, :]
     r = np.sqrt((d ** 2).sum(-1))
     with np.errstate(divide="ignore", invalid="ignore"):
         w = np.where((r < h) & (r > 0), (1.0 - r / h) ** 2 / r, 0.0)
     dv = ((v[None, :, :] - v[:, None, :]) * (-d)).sum(-1)
-    divsum = (w * dv / rho[None, :]).sum(1)
+    divsum = (w * dv / rho0[None, :]).sum(1)
+    assert np.max(np.abs(div1 - divsum)) <= 1e-3 * max(1.0, np.abs(divsum).max())
     m = sc["mass"]
-    div = m * 45.0 / (np.pi * h ** 4) * divsum
-    want = -100.0 * sc["dt"] * div
+    want = -100.0 * sc["dt"] * m * 45.0 / (np.pi * h ** 4) * divsum
     assert np.max(np.abs(f[:, 1] - want)) <= 1e-3 * max(1.0, np.abs(want).max())
     g.close()
 
