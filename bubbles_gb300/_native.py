@@ -66,7 +66,8 @@ class MlpDesc(ctypes.Structure):
                 ("epsilon", ctypes.c_double),
                 ("seed", ctypes.c_ulonglong),
                 ("expectile", ctypes.c_double),
-                ("finetune_steps", ctypes.c_int)]
+                ("finetune_steps", ctypes.c_int),
+                ("refresh_interval", ctypes.c_int)]
 
 
 class SceneDesc(ctypes.Structure):

@@ -83,7 +83,7 @@ struct bbg_solver_s {
         int state = -1, pid = -1, max_it = 0, variant = -1;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
-    } graphs[4];
+    } graphs[8];   // ping-pong parities x corrector variants
     int graph_next = 0;
     unsigned epoch = 1;          // bumped whenever captured launch arguments may change
     bool use_graphs = true;
@@ -93,6 +93,7 @@ struct bbg_solver_s {
     bbg_mlp_desc mdesc;
     bool mlp_alloc = false;
     int mlp_trained = 0;         // substeps used for training so far
+    long long mlp_since = 0;     // learned substeps since the last refresh (refresh_interval)
     double mlp_loss_count = 1;   // samples behind the loss accumulator
     // batch of scenes stacked along z
     int nscenes = 0;
@@ -271,6 +272,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
     CK_LAUNCH();
     CK(cudaStreamSynchronize(s->stream));
     s->mlp_trained = 0;
+    s->mlp_since = 0;
     s->epoch++;
     return BBG_OK;
 }
@@ -367,7 +369,20 @@ void add_substep_stats(bbg_solver s, float dt) {
 static int mlp_mode(bbg_solver s) {
     if (s->desc.pressure_init != BBG_PRESSURE_INIT_LEARNED || s->desc.solver_kind != BBG_SOLVER_PCISPH)
         return 0;
-    return s->mlp_trained < s->mdesc.train_substeps ? 1 : 2;
+    if (s->mlp_trained < s->mdesc.train_substeps) return 1;
+    // refresh: every refresh_interval-th substep after training runs plain and trains again
+    if (s->mdesc.refresh_interval > 0 && s->mlp_since >= s->mdesc.refresh_interval) return 1;
+    return 2;
+}
+
+// Bookkeeping after a substep has been launched in mode mm.
+static void mlp_after_substep(bbg_solver s, int mm) {
+    if (mm == 1) {
+        if (s->mlp_trained < s->mdesc.train_substeps) s->mlp_trained++;
+        s->mlp_since = 0;
+    } else if (mm == 2) {
+        s->mlp_since++;
+    }
 }
 
 static bool warm_active(bbg_solver s) {
@@ -579,7 +594,7 @@ bbg_status substep(bbg_solver s, float dt) {
                 hit = &g;
         if (!hit) {
             hit = &s->graphs[s->graph_next];
-            s->graph_next = (s->graph_next + 1) % 4;
+            s->graph_next = (s->graph_next + 1) % 8;
             bbg_status r = capture_substep(s, dt, max_it, delta, *hit);
             if (r) return r;
             hit->epoch = s->epoch;
@@ -590,8 +605,9 @@ bbg_status substep(bbg_solver s, float dt) {
             hit->tol_bits = fbits(s->P.max_err_ratio);
             hit->variant = mlp_mode(s);
         }
+        const int mm = mlp_mode(s);
         CK(cudaGraphLaunch(hit->exec, s->stream));
-        if (mlp_mode(s) == 1) s->mlp_trained++;
+        mlp_after_substep(s, mm);
         s->last_max_it = max_it;
         s->last_tol = s->P.max_err_ratio;
         after_substep(s, dt);
@@ -617,7 +633,7 @@ bbg_status substep(bbg_solver s, float dt) {
         launch_training(s, delta, s->stream);
         CK_LAUNCH();
     }
-    if (mlp_mode(s) == 1) s->mlp_trained++;
+    mlp_after_substep(s, mlp_mode(s));
     return pseudo_viscosity(s, dt);
 }
 
@@ -1365,6 +1381,7 @@ bbg_status bbg_mlp_desc_default(bbg_mlp_desc *d) {
     d->seed = 20240601ull;
     d->expectile = 0.5;
     d->finetune_steps = 0;
+    d->refresh_interval = 0;
     return BBG_OK;
 }
 

@@ -163,6 +163,8 @@ typedef struct {
                                   biases estimates low, which suits the monotone update */
     int finetune_steps;        /* Adam steps after each learned substep on its own converged
                                   pressure (0: the model is fixed after training) */
+    int refresh_interval;      /* after training, every refresh_interval-th substep runs the
+                                  plain corrector and trains on it again (0: never) */
 } bbg_mlp_desc;
 
 /* ----- library ----------------------------------------------------------- */
