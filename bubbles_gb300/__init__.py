@@ -7,7 +7,7 @@ library or a CUDA device every call raises `BbgError`.
 from ._native import BbgError, device_count, load  # noqa: F401
 from . import _native as native  # noqa: F401
 from .solver import (BatchSolver, PciSphSolver3, Solver, SphSolver3, build_grid,  # noqa: F401
-                     compute_delta_denom, compute_mass, desc_from_scene)
+                     compute_delta_denom, compute_mass, desc_from_scene, format_g)
 from . import scenes  # noqa: F401
 
 FIELD_POSITION = native.FIELD_POSITION
@@ -21,3 +21,7 @@ FIELD_PRESSURE_FORCE = native.FIELD_PRESSURE_FORCE
 FIELD_PRED_DENSITY = native.FIELD_PRED_DENSITY
 FIELD_DENSITY_ERROR = native.FIELD_DENSITY_ERROR
 FIELD_DIVERGENCE = native.FIELD_DIVERGENCE
+FRAME_POSITION = native.FRAME_POSITION
+FRAME_VELOCITY = native.FRAME_VELOCITY
+FRAME_DENSITY = native.FRAME_DENSITY
+FRAME_MASS = native.FRAME_MASS

@@ -23,6 +23,7 @@ FIELD_POSITION, FIELD_VELOCITY, FIELD_FORCE, FIELD_INTERACTION = 0, 1, 2, 3
 FIELD_DENSITY, FIELD_PRESSURE, FIELD_PRED_POSITION = 4, 5, 6
 FIELD_PRESSURE_FORCE, FIELD_PRED_DENSITY, FIELD_DENSITY_ERROR = 8, 9, 10
 FIELD_DIVERGENCE = 11
+FRAME_POSITION, FRAME_VELOCITY, FRAME_DENSITY, FRAME_MASS = 0x01, 0x02, 0x04, 0x20
 VECTOR_FIELDS = {FIELD_POSITION, FIELD_VELOCITY, FIELD_FORCE, FIELD_INTERACTION,
                  FIELD_PRED_POSITION, FIELD_PRESSURE_FORCE}
 
@@ -170,6 +171,9 @@ SIGNATURES = {
     "bbg_batch_upload": [_P, _FP, _FP],
     "bbg_batch_download": [_P, _FP, _FP],
     "bbg_batch_scene_stats": [_P, _IP, _DP],
+    "bbg_frame_text": [_P, _I, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+    "bbg_frame_append": [_P, _I, ctypes.c_char_p],
+    "bbg_format_g": [ctypes.c_float, ctypes.c_char_p, _IP],
     "bbg_mlp_desc_default": [ctypes.POINTER(MlpDesc)],
     "bbg_mlp_configure": [_P, ctypes.POINTER(MlpDesc)],
     "bbg_mlp_get_params": [_P, _FP],

@@ -3,6 +3,8 @@
 // grid.cu and sph.cu.
 #include "../../include/bbg.h"
 #include "bbg_kernels.h"
+#include "frame.h"
+#include "gfmt.h"
 #include "host_math.h"
 #include "mlp.h"
 
@@ -103,6 +105,7 @@ struct bbg_solver_s {
     ShapeDev *d_box = nullptr;
     SceneState *d_sst = nullptr;
     unsigned short *d_scene = nullptr;
+    FrameBufs frame;             // particle-frame writer buffers (allocated on first use)
 };
 
 namespace {
@@ -172,9 +175,18 @@ void drop_graphs(bbg_solver s) {
 
 void free_mlp(bbg_solver s);
 
+void free_frame(bbg_solver s) {
+    FrameBufs &F = s->frame;
+    void *ptrs[] = {F.lines, F.lens, F.scan_in, F.offset, F.partials, F.out};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    F = FrameBufs();
+}
+
 bbg_status free_all(bbg_solver s) {
     drop_graphs(s);
     free_mlp(s);
+    free_frame(s);
     void *batch[] = {s->d_zb, s->d_box, s->d_sst, s->d_scene};
     for (void *p : batch)
         if (p) cudaFree(p);
@@ -251,7 +263,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
         CK(mlp_prepare());
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->desc.device));
-        M.infer_blocks = 4 * (sms > 0 ? sms : 1);   // 4 blocks of 128 threads fit an SM
+        M.infer_blocks = 6 * (sms > 0 ? sms : 1);   // 6 blocks of 128 threads fit an SM
         M.batch = d.batch;
         s->mlp_alloc = true;
     }
@@ -1668,5 +1680,89 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
     s->B.tune.batch_pd = t->batch_pd;
     s->B.tune.batch_pf = t->batch_pf;
     s->epoch++;   // captured graphs hold the old launch shapes
+    return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// particle frames (SerializerSaveSphDataSet3 format)
+// ----------------------------------------------------------------------------
+namespace {
+bbg_status frame_build(bbg_solver s, int flags, std::vector<char> *text) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!(flags & kFrameSupported) || (flags & ~kFrameSupported))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "frame flags must combine position, velocity, density and mass");
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    if ((flags & kFrameDensity) && !(s->valid & bit(BBG_FIELD_DENSITY)))
+        return fail(BBG_ERR_STATE, "density is not valid in the current particle order");
+    FrameBufs &F = s->frame;
+    if (F.capacity < s->capacity) {
+        free_frame(s);
+        const size_t n = (size_t)s->capacity;
+        bbg_status r = BBG_OK;
+        if (!r) r = dalloc(&F.lines, n * kFrameLineCap);
+        if (!r) r = dalloc(&F.lens, n);
+        if (!r) r = dalloc(&F.scan_in, n);
+        if (!r) r = dalloc(&F.offset, n + 1);
+        if (!r) r = dalloc(&F.partials, scan_partials_needed((unsigned)n));
+        if (!r) r = dalloc(&F.out, n * kFrameLineCap);
+        if (r) {
+            free_frame(s);
+            return r;
+        }
+        F.capacity = s->capacity;
+    }
+    launch_frame_lines(s->n, flags, s->B.pos[s->state], s->B.vel[s->state], s->B.rho, s->B.slot, s->mass, F,
+                       s->stream);
+    CK_LAUNCH();
+    unsigned body = 0;
+    CK(cudaMemcpyAsync(s->h_u, &F.offset[s->n], sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    memcpy(&body, s->h_u, sizeof(unsigned));
+    char fmt[16];
+    int k = 0;
+    if (flags & kFramePosition) fmt[k++] = 'p';
+    if (flags & kFrameVelocity) fmt[k++] = 'v';
+    if (flags & kFrameDensity) fmt[k++] = 'd';
+    if (flags & kFrameMass) fmt[k++] = 'm';
+    fmt[k] = 0;
+    char head[256];
+    const int hl = snprintf(head, sizeof(head),
+                            "FluidBegin\n\t\"Type\" particles\n\t\"Count\" %d\n\t\"Format\" %s\n"
+                            "\t\"Spacing\" %g\n\tDataBegin\n",
+                            s->n, fmt, (double)(float)s->desc.target_spacing);   // Float spacing
+    static const char tail[] = "\tDataEnd\nFluidEnd\n";
+    text->resize((size_t)hl + body + sizeof(tail) - 1);
+    memcpy(text->data(), head, (size_t)hl);
+    CK(cudaMemcpy(text->data() + hl, F.out, body, cudaMemcpyDeviceToHost));
+    memcpy(text->data() + hl + body, tail, sizeof(tail) - 1);
+    return BBG_OK;
+}
+}  // namespace
+
+bbg_status bbg_frame_text(bbg_solver s, int flags, char *buf, size_t capacity, size_t *length) {
+    std::vector<char> text;
+    if (bbg_status r = frame_build(s, flags, &text)) return r;
+    if (length) *length = text.size();
+    if (!buf || capacity < text.size())
+        return fail(BBG_ERR_CAPACITY, "the frame needs %zu bytes", text.size());
+    memcpy(buf, text.data(), text.size());
+    return BBG_OK;
+}
+
+bbg_status bbg_frame_append(bbg_solver s, int flags, const char *path) {
+    if (!path) return fail(BBG_ERR_INVALID_ARGUMENT, "null path");
+    std::vector<char> text;
+    if (bbg_status r = frame_build(s, flags, &text)) return r;
+    FILE *fp = fopen(path, "a+");
+    if (!fp) return fail(BBG_ERR_INVALID_ARGUMENT, "cannot open %s", path);
+    const size_t w = fwrite(text.data(), 1, text.size(), fp);
+    fclose(fp);
+    if (w != text.size()) return fail(BBG_ERR_INVALID_ARGUMENT, "short write to %s", path);
+    return BBG_OK;
+}
+
+bbg_status bbg_format_g(float value, char *out, int *length) {
+    if (!out || !length) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
+    *length = gfmt::format_g(value, out);
     return BBG_OK;
 }

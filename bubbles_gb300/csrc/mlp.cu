@@ -30,17 +30,6 @@ namespace {
 constexpr float kGeluC = 0.7978845608028654f;   // sqrt(2 / pi)
 constexpr float kGeluA = 0.044715f;
 
-__device__ __forceinline__ float tanh_fast(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ __forceinline__ float gelu_fast(float x) {
-    const float u = kGeluC * fmaf(kGeluA * x * x, x, x);
-    return 0.5f * x * (1.f + tanh_fast(u));
-}
-
 // FP32 GELU and its derivative for training
 __device__ __forceinline__ void gelu_grad(float x, float *y, float *dy) {
     const float x2 = x * x;
@@ -112,29 +101,27 @@ __global__ void k_mlp_features(int n, const float4 *__restrict__ vel, const floa
 // clamp(MLP(features), 0, largest training target), rho* = rho, err = 0, pos.w = p / rho^2.
 // Layer-2 B fragments live in shared memory (8 KB per block), the layer-1 fragments,
 // bias and w3 in registers; GELU runs in BF16x2 arithmetic.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 6)
 k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restrict__ w1f,
                  const uint32_t *__restrict__ w2f, const float *__restrict__ tail, float p_unit, float scale,
                  float4 *__restrict__ pos, const float *__restrict__ rho, float *__restrict__ press,
                  float *__restrict__ rhostar, float *__restrict__ derr, float *__restrict__ raw) {
     __shared__ uint2 sW2[32 * 32];   // [fragment pair q / 2][lane]
+    __shared__ float2 sB2[32], sW3[32];   // (b2, w3) column pairs 2p, 2p + 1
     const int lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
     for (int k = threadIdx.x; k < 32 * 32; k += blockDim.x) {
         const int qp = k >> 5, l = k & 31;
         sW2[k] = make_uint2(__ldg(&w2f[(2 * qp) * 32 + l]), __ldg(&w2f[(2 * qp + 1) * 32 + l]));
     }
+    if (threadIdx.x < 32) {
+        const int c = 2 * threadIdx.x;
+        sB2[threadIdx.x] = make_float2(__ldg(&tail[kTailB2 + c]), __ldg(&tail[kTailB2 + c + 1]));
+        sW3[threadIdx.x] = make_float2(__ldg(&tail[kTailW3 + c]), __ldg(&tail[kTailW3 + c + 1]));
+    }
     uint32_t b1f[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) b1f[q] = __ldg(&w1f[q * 32 + lane]);
-    float bias2[16], w3[16];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        bias2[2 * nt] = __ldg(&tail[kTailB2 + 8 * nt + 2 * t]);
-        bias2[2 * nt + 1] = __ldg(&tail[kTailB2 + 8 * nt + 2 * t + 1]);
-        w3[2 * nt] = __ldg(&tail[kTailW3 + 8 * nt + 2 * t]);
-        w3[2 * nt + 1] = __ldg(&tail[kTailW3 + 8 * nt + 2 * t + 1]);
-    }
     const float b3 = __ldg(&tail[kTailB3]);
     const float ymax = __ldg(&tail[kTailYmax]);
     __syncthreads();
@@ -159,10 +146,11 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
         float acc[8][4];
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
-            acc[nt][0] = bias2[2 * nt];
-            acc[nt][1] = bias2[2 * nt + 1];
-            acc[nt][2] = bias2[2 * nt];
-            acc[nt][3] = bias2[2 * nt + 1];
+            const float2 b = sB2[4 * nt + t];   // columns 8 nt + 2 t, + 1
+            acc[nt][0] = b.x;
+            acc[nt][1] = b.y;
+            acc[nt][2] = b.x;
+            acc[nt][3] = b.y;
         }
 #pragma unroll
         for (int kc = 0; kc < 4; kc++) {
@@ -176,12 +164,13 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
         float ya = 0.f, yb = 0.f;
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
+            const float2 w = sW3[4 * nt + t];
             const float2 ha = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][0], acc[nt][1]))));
             const float2 hb = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][2], acc[nt][3]))));
-            ya = fmaf(ha.x, w3[2 * nt], ya);
-            ya = fmaf(ha.y, w3[2 * nt + 1], ya);
-            yb = fmaf(hb.x, w3[2 * nt], yb);
-            yb = fmaf(hb.y, w3[2 * nt + 1], yb);
+            ya = fmaf(ha.x, w.x, ya);
+            ya = fmaf(ha.y, w.y, ya);
+            yb = fmaf(hb.x, w.x, yb);
+            yb = fmaf(hb.y, w.y, yb);
         }
         ya += __shfl_xor_sync(0xffffffffu, ya, 1);
         ya += __shfl_xor_sync(0xffffffffu, ya, 2);

@@ -275,6 +275,20 @@ class Solver:
             out[name] = (ms[i], cnt[i])
         return out, total.value
 
+    # --- particle frames (reference text format) ------------------------------------
+    def frame_text(self, flags=N.FRAME_POSITION):
+        """The SerializerSaveSphDataSet3 block of the current state, as bytes."""
+        need = ctypes.c_size_t()
+        st = N.load().bbg_frame_text(self.h, int(flags), None, 0, ctypes.byref(need))
+        if st not in (N.OK, 4):   # 4: capacity (size query)
+            N.call("bbg_frame_text", self.h, int(flags), None, 0, ctypes.byref(need))
+        buf = ctypes.create_string_buffer(need.value)
+        N.call("bbg_frame_text", self.h, int(flags), buf, need.value, ctypes.byref(need))
+        return buf.raw[:need.value]
+
+    def frame_append(self, path, flags=N.FRAME_POSITION):
+        N.call("bbg_frame_append", self.h, int(flags), str(path).encode())
+
     # --- launch tuning ----------------------------------------------------------
     def tuning(self):
         t = N.Tuning()
@@ -417,6 +431,14 @@ class PciSphSolver3(Solver):
 
 class SphSolver3(PciSphSolver3):
     """Reference-named facade of SphSolver3 (src/core/sph_solver.h:76-96)."""
+
+
+def format_g(value):
+    """printf("%g") of a float32 value through the frame writer's formatter (host)."""
+    out = ctypes.create_string_buffer(16)
+    n = ctypes.c_int()
+    N.call("bbg_format_g", float(value), out, ctypes.byref(n))
+    return out.raw[:n.value].decode()
 
 
 def build_grid(domain_min, domain_max, spacing, scale):

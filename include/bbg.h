@@ -221,6 +221,26 @@ bbg_status bbg_use_cuda_graphs(bbg_solver s, int enable);
 /* Read the statistics of the last substep (synchronises). */
 bbg_status bbg_get_stats(bbg_solver s, bbg_step_stats *stats);
 
+/* ----- particle frames --------------------------------------------------------- */
+/* The block SerializerSaveSphDataSet3 (src/third/serializer.cpp:880-923) appends to a
+ * frame file, for the caller-order particles: FluidBegin, "Type" particles, "Count",
+ * "Format", "Spacing", DataBegin, one line per particle (two tabs, the selected fields as
+ * %g numbers), DataEnd, FluidEnd.  Lines are formatted and packed on the device; the
+ * numbers are exactly printf("%g") of the FP32 state.  Flags: the reference's
+ * SERIALIZER_POSITION / VELOCITY / DENSITY / MASS (src/third/serializer.h:7-12). */
+#define BBG_FRAME_POSITION 0x01
+#define BBG_FRAME_VELOCITY 0x02
+#define BBG_FRAME_DENSITY 0x04
+#define BBG_FRAME_MASS 0x20
+/* Into buf (not terminated); *length is the frame's size, also when buf is too small
+ * (BBG_ERR_CAPACITY). */
+bbg_status bbg_frame_text(bbg_solver s, int flags, char *buf, size_t capacity, size_t *length);
+/* Appends the block to a file (fopen "a+", as the reference). */
+bbg_status bbg_frame_append(bbg_solver s, int flags, const char *path);
+/* printf("%g", (double)value) through the device formatter's code, on the host (at most
+ * 14 characters, not terminated). */
+bbg_status bbg_format_g(float value, char *out, int *length);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

@@ -114,6 +114,8 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_frame_text": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_double,
+                                             ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -334,3 +336,20 @@ def build_grid(dmin, dmax, spacing, scale, variant="f32"):
     total = load(variant).orc_build_grid(_ptr(a), _ptr(b), spacing, scale, _ptr(dims, _I32),
                                          _ptr(geo))
     return dims, geo, total
+
+
+def frame_text(pos, vel=None, rho=None, mass=0.0, spacing=0.0, flags=0x01, variant="f32"):
+    """SerializerSaveSphDataSet3's frame block for the given state (bytes), as the reference
+    prints it: every value rounded to the build's Float, then printf("%g")."""
+    lib = load(variant)
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    n = len(pos)
+    v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+    r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+    args = (n, int(flags), _ptr(pos), _ptr(v) if v is not None else None,
+            _ptr(r) if r is not None else None, float(mass), float(spacing))
+    need = lib.orc_frame_text(*args, None, 0)
+    buf = ctypes.create_string_buffer(need + 1)
+    lib.orc_frame_text(*args, buf, need + 1)
+    return buf.raw[:need]
+

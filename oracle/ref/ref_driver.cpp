@@ -8,6 +8,7 @@
 #include <cutil.h>
 #include <interaction.h>
 #include <pcisph_solver.h>
+#include <serializer.h>
 #include <shape.h>
 #include <sph_solver.h>
 #include <transform.h>
@@ -220,5 +221,8 @@ void ref_get_buckets(RefSim *s, int32_t *counts, int32_t *ids) {
         for (int q = 0; q < 100; q++) ids[100 * i + q] = q < b->Count() ? b->Get(q) : -1;
     }
 }
+
+/* Appends SerializerSaveSphDataSet3's particle frame of the current state to `path`. */
+void ref_save_frame(RefSim *s, const char *path, int flags) { SerializerSaveSphDataSet3(s->data, path, flags); }
 
 }  // extern "C"

@@ -70,6 +70,7 @@ def load(variant):
         "ref_set_field": (None, [_P, ctypes.c_int, _D]),
         "ref_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "ref_get_buckets": (None, [_P, _I32, _I32]),
+        "ref_save_frame": (None, [_P, ctypes.c_char_p, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -129,6 +130,15 @@ class RefSim:
         self.lib.ref_get_cells(self.h, cell_of.ctypes.data_as(_U32), counts.ctypes.data_as(_U32),
                                chains.ctypes.data_as(_U32))
         return cell_of, counts, chains
+
+    def frame(self, flags):
+        """Bytes SerializerSaveSphDataSet3 appends for the current state."""
+        import tempfile
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "frame.txt")
+            self.lib.ref_save_frame(self.h, path.encode(), int(flags))
+            with open(path, "rb") as f:
+                return f.read()
 
     def buckets(self):
         counts = np.zeros(self.n, np.int32)

@@ -17,6 +17,8 @@
 #include <float.h>
 #include <math.h>
 #include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1303,4 +1305,63 @@ int orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids) {
         if (s->bfull[i] > ORC_BUCKET) over++;
     }
     return over;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Particle frames (src/third/serializer.cpp:20-45, 813-923)                             */
+/* ------------------------------------------------------------------------------------ */
+typedef struct {
+    char *buf;
+    size_t cap, len;
+} frame_out;
+
+static void frame_put(frame_out *o, const char *fmt, ...) {
+    char tmp[128];
+    va_list ap;
+    va_start(ap, fmt);
+    int k = vsnprintf(tmp, sizeof(tmp), fmt, ap);
+    va_end(ap);
+    for (int j = 0; j < k; j++, o->len++)
+        if (o->len < o->cap) o->buf[o->len] = tmp[j];
+}
+
+size_t orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
+                      double mass, double spacing, char *buf, size_t capacity) {
+    frame_out o = {buf, buf ? capacity : 0, 0};
+    char fmt[8];
+    int k = 0;
+    if (flags & 0x01) fmt[k++] = 'p';
+    if (flags & 0x02) fmt[k++] = 'v';
+    if (flags & 0x04) fmt[k++] = 'd';
+    if (flags & 0x20) fmt[k++] = 'm';
+    fmt[k] = 0;
+    frame_put(&o, "FluidBegin\n");
+    frame_put(&o, "\t\"Type\" particles\n");
+    frame_put(&o, "\t\"Count\" %d\n", n);
+    frame_put(&o, "\t\"Format\" %s\n", fmt);
+    frame_put(&o, "\t\"Spacing\" %g\n", (double)(Float)spacing);
+    frame_put(&o, "\tDataBegin\n");
+    for (int i = 0; i < n; i++) {
+        int space = 0;
+        frame_put(&o, "\t\t");
+        if (flags & 0x01) {
+            frame_put(&o, "%g %g %g", (double)(Float)pos[3 * i], (double)(Float)pos[3 * i + 1],
+                      (double)(Float)pos[3 * i + 2]);
+            space = 1;
+        }
+        if (flags & 0x02) {
+            frame_put(&o, space ? " %g %g %g" : "%g %g %g", (double)(Float)vel[3 * i],
+                      (double)(Float)vel[3 * i + 1], (double)(Float)vel[3 * i + 2]);
+            space = 1;
+        }
+        if (flags & 0x04) {
+            frame_put(&o, space ? " %g" : "%g", (double)(Float)rho[i]);
+            space = 1;
+        }
+        if (flags & 0x20) frame_put(&o, space ? " %g" : "%g", (double)(Float)mass);
+        frame_put(&o, "\n");
+    }
+    frame_put(&o, "\tDataEnd\n");
+    frame_put(&o, "FluidEnd\n");
+    return o.len;
 }

@@ -30,6 +30,7 @@
 #ifndef BUBBLES_SPH_ORACLE_H
 #define BUBBLES_SPH_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -158,6 +159,15 @@ int      orc_get_cells(const orc_sim *s, uint32_t *cell_of_particle, uint32_t *c
 /* Buckets: counts[n], ids[n*100] (-1 padded).  Returns the number of particles whose
  * neighbour count exceeded the 100-slot bucket (truncated, as the reference does). */
 int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
+
+/* Particle frame of SerializerSaveSphDataSet3 (src/third/serializer.cpp:880-923 with
+ * PushParticleSetToFile :813-878 and PrintToFile :20-45): header, one line per particle
+ * (two tabs, the selected fields printed "%g" from Float values, separated by spaces),
+ * trailer.  Flags are SERIALIZER_POSITION/VELOCITY/DENSITY/MASS (0x01/0x02/0x04/0x20);
+ * vel and rho may be NULL when not selected.  Writes at most `capacity` bytes into buf and
+ * returns the frame's full length (sequential, one thread, as the reference). */
+size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
+                        double mass, double spacing, char *buf, size_t capacity);
 
 #ifdef __cplusplus
 }

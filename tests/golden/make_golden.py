@@ -12,8 +12,13 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   positions after Advance(2e-3) with its CFL substep loop.
   sph_<v>.npz     800-particle SPH dam break: fields after 3 as-shipped substeps
                   (ComputePressureForceCPU integrating in place, single thread).
+  frame_f32.npz   the particle frames SerializerSaveSphDataSet3 (third/serializer.cpp)
+                  appends for the FP32 PCISPH state after those 3 substeps, with the
+                  position/velocity/density/mass flags and with position only, beside the
+                  state they print.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py           # every fixture
+    python tests/golden/make_golden.py frames    # frame_f32.npz only
 """
 import json
 import os
@@ -97,9 +102,28 @@ def make(variant):
     np.savez_compressed(os.path.join(HERE, "sph_%s.npz" % variant), **o2)
 
 
+FRAME_FLAGS = {"pvdm": 0x01 | 0x02 | 0x04 | 0x20, "p": 0x01}   # SERIALIZER_* (third/serializer.h)
+
+
+def make_frames():
+    sc, pos = pcisph_scene()
+    r = R.RefSim(sc, pos, variant="f32")
+    for _ in range(3):
+        r.advance_time_step(sc["dt"])
+    out = {"scene": np.array(json.dumps(clean(sc))), "pos0": pos,
+           "mass": np.array(r.scalars_dict()["mass"])}
+    for name in ("pos", "vel", "density"):
+        out["step3_" + name] = r.get(FIELDS[name])
+    for name, flags in FRAME_FLAGS.items():
+        out["frame_" + name] = np.frombuffer(r.frame(flags), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "frame_f32.npz"), **out)
+
+
 if __name__ == "__main__":
     if not R.available():
         sys.exit("the reference checkout is not available here; fixtures unchanged")
-    for v in ("f32", "f64"):
-        make(v)
+    if sys.argv[1:] != ["frames"]:
+        for v in ("f32", "f64"):
+            make(v)
+    make_frames()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
