@@ -174,6 +174,10 @@ SIGNATURES = {
     "bbg_frame_text": [_P, _I, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "bbg_frame_append": [_P, _I, ctypes.c_char_p],
     "bbg_format_g": [ctypes.c_float, ctypes.c_char_p, _IP],
+    "bbg_checkpoint_save": [_P, ctypes.c_char_p],
+    "bbg_checkpoint_load": [_P, ctypes.c_char_p],
+    "bbg_checkpoint_write": [_P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+    "bbg_checkpoint_read": [_P, ctypes.c_char_p, ctypes.c_size_t],
     "bbg_mlp_desc_default": [ctypes.POINTER(MlpDesc)],
     "bbg_mlp_configure": [_P, ctypes.POINTER(MlpDesc)],
     "bbg_mlp_get_params": [_P, _FP],

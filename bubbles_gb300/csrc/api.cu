@@ -215,7 +215,7 @@ bbg_status free_all(bbg_solver s) {
 
 void free_mlp(bbg_solver s) {
     MlpBufs &M = s->mlp;
-    void *ptrs[] = {M.theta, M.grad, M.m1, M.m2, M.w1f, M.w2f, M.tail, M.step, M.loss, M.feat, M.divsum,
+    void *ptrs[] = {M.theta, M.grad, M.lpart, M.m1, M.m2, M.w1f, M.w2f, M.tail, M.step, M.loss, M.feat, M.divsum,
                     M.divprev, M.bx, M.bt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -250,7 +250,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
         const size_t n = (size_t)s->capacity;
         bbg_status r = BBG_OK;
 #define ALLOC(ptr, cnt) if (!r) r = dalloc(&(ptr), (cnt))
-        ALLOC(M.theta, kParams); ALLOC(M.grad, kParams); ALLOC(M.m1, kParams); ALLOC(M.m2, kParams);
+        ALLOC(M.theta, kParams); ALLOC(M.grad, (size_t)kGradRows * kParams); ALLOC(M.lpart, kGradRows); ALLOC(M.m1, kParams); ALLOC(M.m2, kParams);
         ALLOC(M.w1f, 8 * 32); ALLOC(M.w2f, 64 * 32); ALLOC(M.tail, kTail); ALLOC(M.step, 1);
         ALLOC(M.loss, 1); ALLOC(M.feat, n); ALLOC(M.divsum, n); ALLOC(M.divprev, n);
         ALLOC(M.bx, (size_t)d.batch);
@@ -271,7 +271,6 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
     const std::vector<float> th = mlp_initial_params(d.seed);
     MlpBufs &M = s->mlp;
     CK(cudaMemcpyAsync(M.theta, th.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemsetAsync(M.grad, 0, sizeof(float) * kParams, s->stream));
     CK(cudaMemsetAsync(M.m1, 0, sizeof(float) * kParams, s->stream));
     CK(cudaMemsetAsync(M.m2, 0, sizeof(float) * kParams, s->stream));
     CK(cudaMemsetAsync(M.step, 0, sizeof(unsigned), s->stream));
@@ -1765,4 +1764,252 @@ bbg_status bbg_format_g(float value, char *out, int *length) {
     if (!out || !length) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
     *length = gfmt::format_g(value, out);
     return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// checkpoint: binary snapshot of the solver state for exact resume
+// ----------------------------------------------------------------------------
+namespace {
+
+constexpr char kCkptMagic[8] = {'B', 'B', 'G', 'C', 'K', 'P', 'T', '1'};
+constexpr uint32_t kCkptVersion = 1;
+// per-particle fields a snapshot carries when they are valid, in file order
+constexpr int kCkptFields[] = {BBG_FIELD_POSITION,       BBG_FIELD_VELOCITY,      BBG_FIELD_FORCE,
+                               BBG_FIELD_DENSITY,        BBG_FIELD_PRESSURE,      BBG_FIELD_PRED_POSITION,
+                               BBG_FIELD_PRESSURE_FORCE, BBG_FIELD_PRED_DENSITY,  BBG_FIELD_DENSITY_ERROR,
+                               BBG_FIELD_DIVERGENCE};
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, header_bytes, desc_bytes, shape_bytes, mlp_desc_bytes, reserved0;
+    int32_t n, nshapes, nscenes, mlp;
+    uint32_t fields;   // bit f set: field f stored
+    uint32_t valid;    // the solver's valid-field mask
+    float mass;
+    int32_t mlp_trained;
+    int64_t mlp_since;
+    double mlp_loss_count;
+    double mlp_loss;
+    uint32_t adam_step, reserved1;
+};
+
+bool same_desc(const bbg_solver_desc &a, const bbg_solver_desc &b) {
+#define EQ(f) (a.f == b.f)
+    bool same = EQ(solver_kind) && EQ(eos_exponent) && EQ(negative_pressure_scale) && EQ(viscosity) &&
+                EQ(pseudo_viscosity) && EQ(sound_speed) && EQ(drag_coefficient) && EQ(target_density) &&
+                EQ(target_spacing) && EQ(relative_kernel_radius) && EQ(mass) && EQ(grid_spacing_scale) &&
+                EQ(time_step_limit_scale) && EQ(pcisph_mode) && EQ(max_iterations) &&
+                EQ(max_density_error_ratio) && EQ(pressure_init) && EQ(warm_rule) && EQ(warm_scale);
+    for (int k = 0; k < 3; k++) same = same && EQ(gravity[k]) && EQ(domain_min[k]) && EQ(domain_max[k]);
+#undef EQ
+    return same;
+}
+
+struct Writer {
+    std::vector<char> *out;
+    void put(const void *p, size_t bytes) {
+        const char *c = static_cast<const char *>(p);
+        out->insert(out->end(), c, c + bytes);
+    }
+};
+
+struct Reader {
+    const char *p;
+    size_t left;
+    bool get(void *dst, size_t bytes) {
+        if (bytes > left) return false;
+        memcpy(dst, p, bytes);
+        p += bytes;
+        left -= bytes;
+        return true;
+    }
+};
+
+bbg_status ckpt_build(bbg_solver s, std::vector<char> *out) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    CkptHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kCkptMagic, sizeof(h.magic));
+    h.version = kCkptVersion;
+    h.header_bytes = sizeof(CkptHeader);
+    h.desc_bytes = sizeof(bbg_solver_desc);
+    h.shape_bytes = sizeof(ShapeDev);
+    h.mlp_desc_bytes = sizeof(bbg_mlp_desc);
+    h.n = s->n;
+    h.nshapes = s->P.nshapes;
+    h.nscenes = s->nscenes;
+    h.mlp = s->mlp_alloc ? 1 : 0;
+    h.valid = s->valid;
+    h.mass = s->mass;
+    for (int f : kCkptFields) {
+        const bool have = f == BBG_FIELD_DIVERGENCE ? s->mlp_alloc : (s->valid & bit(f)) != 0;
+        if (have) h.fields |= bit(f);
+    }
+    if (s->mlp_alloc) {
+        h.mlp_trained = s->mlp_trained;
+        h.mlp_since = s->mlp_since;
+        h.mlp_loss_count = s->mlp_loss_count;
+        CK(cudaMemcpyAsync(s->h_u, s->mlp.step, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(&h.mlp_loss, s->mlp.loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        memcpy(&h.adam_step, s->h_u, sizeof(unsigned));
+    }
+    out->clear();
+    Writer w{out};
+    w.put(&h, sizeof(h));
+    w.put(&s->desc, sizeof(bbg_solver_desc));
+    w.put(s->P.shapes, sizeof(ShapeDev) * (size_t)s->P.nshapes);
+    w.put(s->scene_count.data(), sizeof(int) * (size_t)s->nscenes);
+    std::vector<float> buf;
+    for (int f : kCkptFields) {
+        if (!(h.fields & bit(f))) continue;
+        buf.resize((size_t)field_components(f) * (size_t)s->n);
+        if (bbg_status r = bbg_get_field(s, f, buf.data())) return r;
+        w.put(buf.data(), sizeof(float) * buf.size());
+    }
+    if (s->mlp_alloc) {
+        w.put(&s->mdesc, sizeof(bbg_mlp_desc));
+        buf.resize(3 * (size_t)kParams + kTail);
+        float *b = buf.data();
+        CK(cudaMemcpyAsync(b, s->mlp.theta, sizeof(float) * kParams, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(b + kParams, s->mlp.m1, sizeof(float) * kParams, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(b + 2 * kParams, s->mlp.m2, sizeof(float) * kParams, cudaMemcpyDeviceToHost,
+                           s->stream));
+        CK(cudaMemcpyAsync(b + 3 * kParams, s->mlp.tail, sizeof(float) * kTail, cudaMemcpyDeviceToHost,
+                           s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        w.put(b, sizeof(float) * buf.size());
+    }
+    return BBG_OK;
+}
+
+bbg_status ckpt_restore(bbg_solver s, const char *data, size_t length) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!data) return fail(BBG_ERR_INVALID_ARGUMENT, "null checkpoint");
+    Reader rd{data, length};
+    CkptHeader h;
+    if (!rd.get(&h, sizeof(h)) || memcmp(h.magic, kCkptMagic, sizeof(h.magic)) != 0)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "not a solver checkpoint");
+    if (h.version != kCkptVersion || h.header_bytes != sizeof(CkptHeader) ||
+        h.desc_bytes != sizeof(bbg_solver_desc) || h.shape_bytes != sizeof(ShapeDev) ||
+        h.mlp_desc_bytes != sizeof(bbg_mlp_desc))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "checkpoint written by an incompatible library version");
+    if (h.n <= 0 || h.nshapes < 0 || h.nshapes > kMaxColliders || h.nscenes < 0)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint header");
+    if (h.n > s->capacity) return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", h.n, s->capacity);
+    bbg_solver_desc desc;
+    if (!rd.get(&desc, sizeof(desc))) return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+    if (!same_desc(desc, s->desc))
+        return fail(BBG_ERR_STATE, "the checkpoint was written by a solver with another description");
+    std::vector<ShapeDev> shapes((size_t)h.nshapes);
+    std::vector<int> counts((size_t)h.nscenes);
+    if (!rd.get(shapes.data(), sizeof(ShapeDev) * shapes.size()) ||
+        !rd.get(counts.data(), sizeof(int) * counts.size()))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+    if (h.nscenes != s->nscenes || counts != s->scene_count)
+        return fail(BBG_ERR_STATE, "the checkpoint's scene layout differs from this batch");
+    if ((h.mlp != 0) != s->mlp_alloc)
+        return fail(BBG_ERR_STATE, "learned warm start %s in the checkpoint but %s in this solver",
+                    h.mlp ? "present" : "absent", s->mlp_alloc ? "present" : "absent");
+    const uint32_t need = bit(BBG_FIELD_POSITION) | bit(BBG_FIELD_VELOCITY);
+    if ((h.fields & need) != need) return fail(BBG_ERR_INVALID_ARGUMENT, "checkpoint without positions");
+    // every field before anything changes: a truncated file leaves the solver as it was
+    std::vector<std::vector<float>> fields;
+    for (int f : kCkptFields) {
+        if (!(h.fields & bit(f))) continue;
+        fields.emplace_back((size_t)field_components(f) * (size_t)h.n);
+        if (!rd.get(fields.back().data(), sizeof(float) * fields.back().size()))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+    }
+    bbg_mlp_desc md;
+    std::vector<float> mlp;
+    if (h.mlp) {
+        mlp.resize(3 * (size_t)kParams + kTail);
+        if (!rd.get(&md, sizeof(md)) || !rd.get(mlp.data(), sizeof(float) * mlp.size()))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+    }
+    // colliders and particles
+    for (int i = 0; i < h.nshapes; i++) s->P.shapes[i] = shapes[(size_t)i];
+    s->P.nshapes = h.nshapes;
+    s->epoch++;
+    const float *pos = fields[0].data(), *vel = fields[1].data();
+    if (bbg_status r = bbg_upload_particles(s, pos, vel, h.n)) return r;
+    if (!s->setup_done)
+        if (bbg_status r = bbg_setup(s)) return r;
+    s->mass = h.mass;
+    const float mo = s->mass / (float)s->desc.target_density;
+    s->mod2 = mo * mo;
+    fill_params(s);
+    s->epoch++;
+    if (h.mlp) {
+        if (bbg_status r = mlp_allocate(s, md)) return r;
+        const float *b = mlp.data();
+        MlpBufs &M = s->mlp;
+        CK(cudaMemcpyAsync(M.theta, b, sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(M.m1, b + kParams, sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(M.m2, b + 2 * kParams, sizeof(float) * kParams, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(M.tail, b + 3 * kParams, sizeof(float) * kTail, cudaMemcpyHostToDevice, s->stream));
+        memcpy(s->h_u, &h.adam_step, sizeof(unsigned));
+        CK(cudaMemcpyAsync(M.step, s->h_u, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(M.loss, &h.mlp_loss, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        launch_mlp_pack(M, s->stream);
+        CK_LAUNCH();
+        CK(cudaStreamSynchronize(s->stream));
+        s->mlp_trained = h.mlp_trained;
+        s->mlp_since = h.mlp_since;
+        s->mlp_loss_count = h.mlp_loss_count;
+    }
+    size_t k = 0;
+    for (int f : kCkptFields) {
+        if (!(h.fields & bit(f))) continue;
+        const std::vector<float> &v = fields[k++];
+        if (f == BBG_FIELD_POSITION || f == BBG_FIELD_VELOCITY) continue;
+        if (bbg_status r = bbg_set_field(s, f, v.data())) return r;
+    }
+    s->valid = h.valid;
+    s->grid_valid = false;
+    s->epoch++;
+    return BBG_OK;
+}
+
+}  // namespace
+
+bbg_status bbg_checkpoint_write(bbg_solver s, void *buf, size_t capacity, size_t *length) {
+    std::vector<char> data;
+    if (bbg_status r = ckpt_build(s, &data)) return r;
+    if (length) *length = data.size();
+    if (!buf || capacity < data.size())
+        return fail(BBG_ERR_CAPACITY, "the checkpoint needs %zu bytes", data.size());
+    memcpy(buf, data.data(), data.size());
+    return BBG_OK;
+}
+
+bbg_status bbg_checkpoint_read(bbg_solver s, const void *buf, size_t length) {
+    return ckpt_restore(s, static_cast<const char *>(buf), length);
+}
+
+bbg_status bbg_checkpoint_save(bbg_solver s, const char *path) {
+    if (!path) return fail(BBG_ERR_INVALID_ARGUMENT, "null path");
+    std::vector<char> data;
+    if (bbg_status r = ckpt_build(s, &data)) return r;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return fail(BBG_ERR_INVALID_ARGUMENT, "cannot open %s", path);
+    const size_t w = fwrite(data.data(), 1, data.size(), fp);
+    const int closed = fclose(fp);
+    if (w != data.size() || closed != 0) return fail(BBG_ERR_INVALID_ARGUMENT, "short write to %s", path);
+    return BBG_OK;
+}
+
+bbg_status bbg_checkpoint_load(bbg_solver s, const char *path) {
+    if (!path) return fail(BBG_ERR_INVALID_ARGUMENT, "null path");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(BBG_ERR_NOT_FOUND, "cannot open %s", path);
+    std::vector<char> data;
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = fread(chunk, 1, sizeof(chunk), fp)) > 0) data.insert(data.end(), chunk, chunk + got);
+    fclose(fp);
+    return ckpt_restore(s, data.data(), data.size());
 }

@@ -21,6 +21,8 @@
 #include "bbg_kernels.h"
 #include "mlp.h"
 
+#include <algorithm>
+
 #include <cuda_bf16.h>
 
 namespace bbg {
@@ -213,11 +215,13 @@ __global__ void k_mlp_collect(int n, int batch, const unsigned *__restrict__ ste
     if (y > 0.f) atomicMax(reinterpret_cast<unsigned *>(ymax), __float_as_uint(y));
 }
 
-// Forward + backward of one 128-sample block; weight gradients reduced in shared memory
-// and added to grad (FP32 atomics); sum of (weighted) squared errors added to *loss.
+// Forward + backward of 128-sample tiles (tile, tile + gridDim.x, ...): each block sums
+// its tiles' weight gradients into its own row of gpart and their (weighted) squared
+// errors into lpart[block], always in the same order, so training is deterministic (no
+// atomics; the Adam kernel adds the rows in block order).
 __global__ void __launch_bounds__(128)
 k_mlp_train(int batch, const float4 *__restrict__ bx, const float *__restrict__ bt,
-            const float *__restrict__ theta, float *__restrict__ grad, double *__restrict__ loss,
+            const float *__restrict__ theta, float *__restrict__ gpart, double *__restrict__ lpart,
             float expectile) {
     extern __shared__ float smem[];
     float *sW2 = smem;                    // [64][64]
@@ -242,126 +246,144 @@ k_mlp_train(int batch, const float4 *__restrict__ bx, const float *__restrict__ 
     }
     __syncthreads();
     const float b3 = theta[kOffB3];
-    const int s = blockIdx.x * 128 + t;
-    const bool valid = s < batch;
-    const float4 x = valid ? bx[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float target = valid ? bt[s] : 0.f;
-    sX[0 * 128 + t] = x.x;
-    sX[1 * 128 + t] = x.y;
-    sX[2 * 128 + t] = x.z;
-    sX[3 * 128 + t] = x.w;
-    // forward
-    for (int a = 0; a < kHid; a++) {
-        float z = sB1[a];
-        z = fmaf(x.x, sW1[0 * kHid + a], z);
-        z = fmaf(x.y, sW1[1 * kHid + a], z);
-        z = fmaf(x.z, sW1[2 * kHid + a], z);
-        z = fmaf(x.w, sW1[3 * kHid + a], z);
-        float h, d;
-        gelu_grad(z, &h, &d);
-        sH1[a * 128 + t] = h;
-        sD1[a * 128 + t] = d;
-    }
-    float z2[kHid];
-#pragma unroll
-    for (int k = 0; k < kHid; k++) z2[k] = sB2[k];
-    for (int a = 0; a < kHid; a++) {
-        const float h = sH1[a * 128 + t];
-#pragma unroll
-        for (int k = 0; k < kHid; k++) z2[k] = fmaf(h, sW2[a * kHid + k], z2[k]);
-    }
-    float y = b3;
-#pragma unroll
-    for (int k = 0; k < kHid; k++) {
-        float h, d;
-        gelu_grad(z2[k], &h, &d);
-        sH2[k * 128 + t] = h;
-        y = fmaf(sW3[k], h, y);
-        z2[k] = d;   // keep GELU'(z2)
-    }
-    const float err = valid ? y - target : 0.f;
-    // asymmetric squared error (expectile tau): over-estimates weigh (1 - tau) / 0.5,
-    // under-estimates tau / 0.5; tau = 0.5 is the mean squared error
-    const float wgt = (err > 0.f ? 1.f - expectile : expectile) * 2.f;
-    const float dy = 2.f * wgt * err / (float)batch;
-    sDY[t] = dy;
-    // backward through layer 3 and GELU 2
-#pragma unroll
-    for (int k = 0; k < kHid; k++) {
-        z2[k] = dy * sW3[k] * z2[k];   // dz2
-        sD2[k * 128 + t] = z2[k];
-    }
-    // backward through layer 2 and GELU 1
-    for (int a = 0; a < kHid; a++) {
-        float acc = 0.f;
-#pragma unroll
-        for (int k = 0; k < kHid; k++) acc = fmaf(sW2[a * kHid + k], z2[k], acc);
-        sD1[a * 128 + t] *= acc;   // dz1
-    }
-    // squared error of the block
-    double l = (double)wgt * (double)err * (double)err;
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-    if ((t & 31) == 0) sLoss[t >> 5] = l;
-    __syncthreads();
-    if (t == 0) atomicAdd(loss, sLoss[0] + sLoss[1] + sLoss[2] + sLoss[3]);
-    // dW2[a][k] = sum_s h1[a][s] dz2[k][s]: thread -> row a = t / 2, 32 columns
-    {
-        const int a = t >> 1, k0 = (t & 1) * 32;
-        float acc[32];
-#pragma unroll
-        for (int kk = 0; kk < 32; kk++) acc[kk] = 0.f;
-        for (int q = 0; q < 128; q++) {
-            const float h = sH1[a * 128 + q];
-#pragma unroll
-            for (int kk = 0; kk < 32; kk++) acc[kk] = fmaf(h, sD2[(k0 + kk) * 128 + q], acc[kk]);
+    float *grad = gpart + (size_t)blockIdx.x * kParams;
+    for (int tile = blockIdx.x; tile * 128 < batch; tile += gridDim.x) {
+        const bool first = tile == (int)blockIdx.x;
+        // a block's own gradient row: the first tile stores, later tiles add (same thread)
+        auto put = [&](int idx, float v) { grad[idx] = first ? v : grad[idx] + v; };
+        const int s = tile * 128 + t;
+        const bool valid = s < batch;
+        const float4 x = valid ? bx[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float target = valid ? bt[s] : 0.f;
+        sX[0 * 128 + t] = x.x;
+        sX[1 * 128 + t] = x.y;
+        sX[2 * 128 + t] = x.z;
+        sX[3 * 128 + t] = x.w;
+        // forward
+        for (int a = 0; a < kHid; a++) {
+            float z = sB1[a];
+            z = fmaf(x.x, sW1[0 * kHid + a], z);
+            z = fmaf(x.y, sW1[1 * kHid + a], z);
+            z = fmaf(x.z, sW1[2 * kHid + a], z);
+            z = fmaf(x.w, sW1[3 * kHid + a], z);
+            float h, d;
+            gelu_grad(z, &h, &d);
+            sH1[a * 128 + t] = h;
+            sD1[a * 128 + t] = d;
         }
-#pragma unroll
-        for (int kk = 0; kk < 32; kk++) atomicAdd(&grad[kOffW2 + a * kHid + k0 + kk], acc[kk]);
-    }
-    // dW1[f][a] = sum_s x[f][s] dz1[a][s]: thread -> a = t / 2, f = 2 (t & 1) + {0, 1}
-    {
-        const int a = t >> 1, f0 = (t & 1) * 2;
-        float g0 = 0.f, g1 = 0.f;
-        for (int q0 = 0; q0 < 128; q0++) {
-            const int q = (q0 + t) & 127;
-            const float d = sD1[a * 128 + q];
-            g0 = fmaf(sX[f0 * 128 + q], d, g0);
-            g1 = fmaf(sX[(f0 + 1) * 128 + q], d, g1);
+        float z2[kHid];
+    #pragma unroll
+        for (int k = 0; k < kHid; k++) z2[k] = sB2[k];
+        for (int a = 0; a < kHid; a++) {
+            const float h = sH1[a * 128 + t];
+    #pragma unroll
+            for (int k = 0; k < kHid; k++) z2[k] = fmaf(h, sW2[a * kHid + k], z2[k]);
         }
-        atomicAdd(&grad[kOffW1 + f0 * kHid + a], g0);
-        atomicAdd(&grad[kOffW1 + (f0 + 1) * kHid + a], g1);
-    }
-    // bias and layer-3 gradients: rows summed with a rotated start (no bank conflicts)
-    if (t < kHid) {
-        float gb2 = 0.f, gw3 = 0.f;
-        for (int q0 = 0; q0 < 128; q0++) {
-            const int q = (q0 + t) & 127;
-            gb2 += sD2[t * 128 + q];
-            gw3 = fmaf(sH2[t * 128 + q], sDY[q], gw3);
+        float y = b3;
+    #pragma unroll
+        for (int k = 0; k < kHid; k++) {
+            float h, d;
+            gelu_grad(z2[k], &h, &d);
+            sH2[k * 128 + t] = h;
+            y = fmaf(sW3[k], h, y);
+            z2[k] = d;   // keep GELU'(z2)
         }
-        atomicAdd(&grad[kOffB2 + t], gb2);
-        atomicAdd(&grad[kOffW3 + t], gw3);
-    } else {
-        const int a = t - kHid;
-        float gb1 = 0.f;
-        for (int q0 = 0; q0 < 128; q0++) gb1 += sD1[a * 128 + ((q0 + t) & 127)];
-        atomicAdd(&grad[kOffB1 + a], gb1);
-    }
-    if (t < 32) {
-        float gb3 = sDY[t] + sDY[t + 32] + sDY[t + 64] + sDY[t + 96];
-        for (int o = 16; o > 0; o >>= 1) gb3 += __shfl_xor_sync(0xffffffffu, gb3, o);
-        if (t == 0) atomicAdd(&grad[kOffB3], gb3);
+        const float err = valid ? y - target : 0.f;
+        // asymmetric squared error (expectile tau): over-estimates weigh (1 - tau) / 0.5,
+        // under-estimates tau / 0.5; tau = 0.5 is the mean squared error
+        const float wgt = (err > 0.f ? 1.f - expectile : expectile) * 2.f;
+        const float dy = 2.f * wgt * err / (float)batch;
+        sDY[t] = dy;
+        // backward through layer 3 and GELU 2
+    #pragma unroll
+        for (int k = 0; k < kHid; k++) {
+            z2[k] = dy * sW3[k] * z2[k];   // dz2
+            sD2[k * 128 + t] = z2[k];
+        }
+        // backward through layer 2 and GELU 1
+        for (int a = 0; a < kHid; a++) {
+            float acc = 0.f;
+    #pragma unroll
+            for (int k = 0; k < kHid; k++) acc = fmaf(sW2[a * kHid + k], z2[k], acc);
+            sD1[a * 128 + t] *= acc;   // dz1
+        }
+        // squared error of the block
+        double l = (double)wgt * (double)err * (double)err;
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if ((t & 31) == 0) sLoss[t >> 5] = l;
+        __syncthreads();
+        if (t == 0) {
+            const double bl = sLoss[0] + sLoss[1] + sLoss[2] + sLoss[3];
+            lpart[blockIdx.x] = first ? bl : lpart[blockIdx.x] + bl;
+        }
+        // dW2[a][k] = sum_s h1[a][s] dz2[k][s]: thread -> row a = t / 2, 32 columns
+        {
+            const int a = t >> 1, k0 = (t & 1) * 32;
+            float acc[32];
+    #pragma unroll
+            for (int kk = 0; kk < 32; kk++) acc[kk] = 0.f;
+            for (int q = 0; q < 128; q++) {
+                const float h = sH1[a * 128 + q];
+    #pragma unroll
+                for (int kk = 0; kk < 32; kk++) acc[kk] = fmaf(h, sD2[(k0 + kk) * 128 + q], acc[kk]);
+            }
+    #pragma unroll
+            for (int kk = 0; kk < 32; kk++) put(kOffW2 + a * kHid + k0 + kk, acc[kk]);
+        }
+        // dW1[f][a] = sum_s x[f][s] dz1[a][s]: thread -> a = t / 2, f = 2 (t & 1) + {0, 1}
+        {
+            const int a = t >> 1, f0 = (t & 1) * 2;
+            float g0 = 0.f, g1 = 0.f;
+            for (int q0 = 0; q0 < 128; q0++) {
+                const int q = (q0 + t) & 127;
+                const float d = sD1[a * 128 + q];
+                g0 = fmaf(sX[f0 * 128 + q], d, g0);
+                g1 = fmaf(sX[(f0 + 1) * 128 + q], d, g1);
+            }
+            put(kOffW1 + f0 * kHid + a, g0);
+            put(kOffW1 + (f0 + 1) * kHid + a, g1);
+        }
+        // bias and layer-3 gradients: rows summed with a rotated start (no bank conflicts)
+        if (t < kHid) {
+            float gb2 = 0.f, gw3 = 0.f;
+            for (int q0 = 0; q0 < 128; q0++) {
+                const int q = (q0 + t) & 127;
+                gb2 += sD2[t * 128 + q];
+                gw3 = fmaf(sH2[t * 128 + q], sDY[q], gw3);
+            }
+            put(kOffB2 + t, gb2);
+            put(kOffW3 + t, gw3);
+        } else {
+            const int a = t - kHid;
+            float gb1 = 0.f;
+            for (int q0 = 0; q0 < 128; q0++) gb1 += sD1[a * 128 + ((q0 + t) & 127)];
+            put(kOffB1 + a, gb1);
+        }
+        if (t < 32) {
+            float gb3 = sDY[t] + sDY[t + 32] + sDY[t + 64] + sDY[t + 96];
+            for (int o = 16; o > 0; o >>= 1) gb3 += __shfl_xor_sync(0xffffffffu, gb3, o);
+            if (t == 0) put(kOffB3, gb3);
+        }
+        __syncthreads();   // the tile's shared rows are rewritten by the next tile
     }
 }
 
-// Adam on the FP32 master parameters (bias corrections from the device step counter),
-// gradient cleared for the next batch.
-__global__ void k_mlp_adam(float *__restrict__ theta, float *__restrict__ grad, float *__restrict__ m1,
+// Adam on the FP32 master parameters (bias corrections from the device step counter); the
+// gradient is the sum of the training blocks' rows in block order, the batch loss the sum
+// of their partial losses in block order.
+__global__ void k_mlp_adam(float *__restrict__ theta, const float *__restrict__ gpart, int rows,
+                           const double *__restrict__ lpart, double *__restrict__ loss, float *__restrict__ m1,
                            float *__restrict__ m2, const unsigned *__restrict__ step, float lr, float beta1,
                            float beta2, float eps) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) {
+        double l = 0.0;
+        for (int b = 0; b < rows; b++) l += lpart[b];
+        *loss += l;
+    }
     if (p >= kParams) return;
-    const float gr = grad[p];
+    float gr = 0.f;
+    for (int b = 0; b < rows; b++) gr += gpart[(size_t)b * kParams + p];
     const float a = beta1 * m1[p] + (1.f - beta1) * gr;
     const float b = beta2 * m2[p] + (1.f - beta2) * gr * gr;
     m1[p] = a;
@@ -370,7 +392,6 @@ __global__ void k_mlp_adam(float *__restrict__ theta, float *__restrict__ grad, 
     const float c1 = 1.f / (1.f - powf(beta1, tstep));
     const float c2 = 1.f / (1.f - powf(beta2, tstep));
     theta[p] -= lr * (a * c1) / (sqrtf(b * c2) + eps);
-    grad[p] = 0.f;
 }
 
 // BF16 B fragments of the tensor-core layers and the FP32 tail from the master
@@ -451,10 +472,10 @@ cudaError_t mlp_prepare() {
 
 void launch_mlp_train_step(const MlpBufs &M, const float4 *bx, const float *bt, int batch, float lr,
                            float beta1, float beta2, float eps, float expectile, cudaStream_t s) {
-    k_mlp_train<<<blocks_for(batch, 128), 128, mlp_train_smem(), s>>>(batch, bx, bt, M.theta, M.grad, M.loss,
-                                                                      expectile);
-    k_mlp_adam<<<blocks_for(kParams, 256), 256, 0, s>>>(M.theta, M.grad, M.m1, M.m2, M.step, lr, beta1,
-                                                         beta2, eps);
+    const int rows = std::min(blocks_for(batch, 128), kGradRows);
+    k_mlp_train<<<rows, 128, mlp_train_smem(), s>>>(batch, bx, bt, M.theta, M.grad, M.lpart, expectile);
+    k_mlp_adam<<<blocks_for(kParams, 256), 256, 0, s>>>(M.theta, M.grad, rows, M.lpart, M.loss, M.m1, M.m2,
+                                                         M.step, lr, beta1, beta2, eps);
     k_mlp_pack<<<1, 256, 0, s>>>(M.theta, M.w1f, M.w2f, M.tail, M.step, 1);
 }
 

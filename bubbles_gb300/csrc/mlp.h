@@ -20,9 +20,12 @@ constexpr int kParams = kOffB3 + 1;
 // training target (estimates are clamped to it; 0 = no bound)
 constexpr int kTailB2 = 0, kTailW3 = kHid, kTailB3 = 2 * kHid, kTailYmax = 2 * kHid + 1;
 constexpr int kTail = 2 * kHid + 2;
+constexpr int kGradRows = 128;   // training blocks (each loops over 128-sample tiles)
 
 struct MlpBufs {
-    float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;   // kParams each
+    float *theta = nullptr, *m1 = nullptr, *m2 = nullptr;   // kParams each
+    float *grad = nullptr;     // kGradRows x kParams: per-block gradient rows of a training step
+    double *lpart = nullptr;   // kGradRows: per-block losses of a training step
     uint32_t *w1f = nullptr;   // 8 x 32 BF16x2 B fragments of [W1; b1]
     uint32_t *w2f = nullptr;   // 64 x 32 BF16x2 B fragments of W2
     float *tail = nullptr;     // kTail

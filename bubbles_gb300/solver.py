@@ -120,6 +120,11 @@ class Solver:
     def setup(self):
         N.call("bbg_setup", self.h)
 
+    def particle_count(self):
+        n = ctypes.c_int()
+        N.call("bbg_particle_count", self.h, ctypes.byref(n))
+        return n.value
+
     def set_colliders(self, colliders):
         scene = dict(self.scene, colliders=colliders)
         shapes, count = shapes_from_scene(scene)
@@ -288,6 +293,29 @@ class Solver:
 
     def frame_append(self, path, flags=N.FRAME_POSITION):
         N.call("bbg_frame_append", self.h, int(flags), str(path).encode())
+
+    # --- checkpoint (exact resume) ----------------------------------------------
+    def checkpoint(self):
+        """The solver state as checkpoint bytes (bbg_checkpoint_write)."""
+        need = ctypes.c_size_t()
+        st = N.load().bbg_checkpoint_write(self.h, None, 0, ctypes.byref(need))
+        if st not in (N.OK, 4):   # 4: capacity (size query)
+            N.call("bbg_checkpoint_write", self.h, None, 0, ctypes.byref(need))
+        buf = ctypes.create_string_buffer(need.value)
+        N.call("bbg_checkpoint_write", self.h, buf, need.value, ctypes.byref(need))
+        return buf.raw[:need.value]
+
+    def restore(self, data):
+        """Continue from checkpoint bytes written by a solver with the same description."""
+        N.call("bbg_checkpoint_read", self.h, bytes(data), len(data))
+        self.n = self.particle_count()
+
+    def save_checkpoint(self, path):
+        N.call("bbg_checkpoint_save", self.h, str(path).encode())
+
+    def load_checkpoint(self, path):
+        N.call("bbg_checkpoint_load", self.h, str(path).encode())
+        self.n = self.particle_count()
 
     # --- launch tuning ----------------------------------------------------------
     def tuning(self):

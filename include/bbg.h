@@ -241,6 +241,23 @@ bbg_status bbg_frame_append(bbg_solver s, int flags, const char *path);
  * 14 characters, not terminated). */
 bbg_status bbg_format_g(float value, char *out, int *length);
 
+/* ----- checkpoint (exact resume) ------------------------------------------------ */
+/* The reference saves text frames only (SerializerSaveSphDataSet3,
+ * src/third/serializer.cpp:1027) and reloads positions and velocities from them
+ * (SerializerLoadSphDataSet3, :562-577), so its resume loses pressure, forces and the CFL
+ * input.  A checkpoint holds the full state in binary: the solver description (checked
+ * on load), the colliders, the scene layout of a batch, every valid per-particle field in
+ * caller order (positions, velocities, forces, density, pressure, predicted state, the
+ * carried divergence) and the learned warm start's weights, Adam moments and training
+ * counters.  Loading it into a solver created with the same description (any device,
+ * capacity >= the particle count) continues the run bit for bit.  Native byte order. */
+bbg_status bbg_checkpoint_save(bbg_solver s, const char *path);
+bbg_status bbg_checkpoint_load(bbg_solver s, const char *path);
+/* The same bytes through memory; *length is the size, also when buf is too small
+ * (BBG_ERR_CAPACITY). */
+bbg_status bbg_checkpoint_write(bbg_solver s, void *buf, size_t capacity, size_t *length);
+bbg_status bbg_checkpoint_read(bbg_solver s, const void *buf, size_t length);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

@@ -54,17 +54,19 @@ def test_mlp_params_round_trip(gpu, small):
     g.close()
 
 
-@pytest.mark.parametrize("expectile", [0.5, 0.3])
-def test_mlp_gradient_matches_autograd(gpu, small, expectile):
+@pytest.mark.parametrize("expectile,batch", [(0.5, 1000), (0.3, 1000), (0.5, 40000)])
+def test_mlp_gradient_matches_autograd(gpu, small, expectile, batch):
     """With Adam's epsilon far above |g| one step moves theta by -lr * g / eps, which
-    exposes the gradient of the training kernel (plain and expectile-weighted loss)."""
+    exposes the gradient of the training kernel (plain and expectile-weighted loss; a
+    batch of 40,000 makes each of the 128 training blocks sum several 128-sample tiles)."""
     sc, p = small
-    g = learned_solver(sc, p, learning_rate=1.0, epsilon=1e3, beta1=0.0, beta2=0.0, expectile=expectile)
+    mlp = dict(learning_rate=1.0, epsilon=1e3, beta1=0.0, beta2=0.0, expectile=expectile)
+    g = bb.Solver(dict(sc, pressure_init="learned", mlp=mlp), pos=p, capacity=max(len(p), batch))
     th = random_params(3, 0.5)
     g.mlp_set_params(th)
     rng = np.random.default_rng(2)
-    x = rng.normal(0.0, 1.0, (1000, 4)).astype(np.float32)
-    t = rng.normal(0.0, 1.0, 1000).astype(np.float32)
+    x = rng.normal(0.0, 1.0, (batch, 4)).astype(np.float32)
+    t = rng.normal(0.0, 1.0, batch).astype(np.float32)
     g.mlp_train_batch(x, t)
     moved = (th.astype(np.float64) - g.mlp_params()) * 1e3   # = g / (1 + |g| / eps)
     loss, grad = loss_and_grad(th, x, t, expectile)
@@ -88,6 +90,24 @@ def test_mlp_training_reduces_loss(gpu, small):
         losses.append(g.mlp_status()["last_loss"])
     assert losses[-1] < 0.1 * losses[0]
     g.close()
+
+
+def test_mlp_training_is_deterministic(gpu, small):
+    """Gradients and losses are summed in a fixed order: two solvers trained on the same
+    batches hold bit-identical weights, moments and losses."""
+    sc, p = small
+    rng = np.random.default_rng(9)
+    x = rng.normal(0.0, 1.0, (30000, 4)).astype(np.float32)
+    t = (np.tanh(x[:, 0]) + 0.5 * x[:, 3]).astype(np.float32)
+    out = []
+    for _ in range(2):
+        g = bb.Solver(dict(sc, pressure_init="learned", mlp=dict(learning_rate=3e-3)), pos=p, capacity=30000)
+        for _ in range(5):
+            g.mlp_train_batch(x, t)
+        out.append((g.mlp_params(), g.mlp_status()["last_loss"]))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
 
 
 def test_features_match_definitions(gpu, moved):
