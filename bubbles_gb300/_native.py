@@ -174,6 +174,10 @@ SIGNATURES = {
     "bbg_frame_text": [_P, _I, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "bbg_frame_append": [_P, _I, ctypes.c_char_p],
     "bbg_format_g": [ctypes.c_float, ctypes.c_char_p, _IP],
+    "bbg_frame_load": [_P, ctypes.c_char_p, _IP],
+    "bbg_frame_load_text": [_P, ctypes.c_char_p, ctypes.c_size_t, _IP],
+    "bbg_frame_find_section": [ctypes.c_char_p, ctypes.c_size_t, _IP, _IP, ctypes.POINTER(ctypes.c_size_t),
+                               ctypes.POINTER(ctypes.c_size_t)],
     "bbg_checkpoint_save": [_P, ctypes.c_char_p],
     "bbg_checkpoint_load": [_P, ctypes.c_char_p],
     "bbg_checkpoint_write": [_P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],

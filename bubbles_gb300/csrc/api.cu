@@ -8,6 +8,7 @@
 #include "host_math.h"
 #include "mlp.h"
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -106,6 +107,7 @@ struct bbg_solver_s {
     SceneState *d_sst = nullptr;
     unsigned short *d_scene = nullptr;
     FrameBufs frame;             // particle-frame writer buffers (allocated on first use)
+    FrameReadBufs fread;         // frame reader buffers (grown on use)
 };
 
 namespace {
@@ -181,6 +183,12 @@ void free_frame(bbg_solver s) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     F = FrameBufs();
+    FrameReadBufs &R = s->fread;
+    void *rptrs[] = {R.text, R.chunk, R.chunk_start, R.chunk_part, R.line, R.vals, R.valid, R.flag_copy,
+                     R.index, R.line_part, R.pow5, R.pow10};
+    for (void *p : rptrs)
+        if (p) cudaFree(p);
+    R = FrameReadBufs();
 }
 
 bbg_status free_all(bbg_solver s) {
@@ -2013,3 +2021,133 @@ bbg_status bbg_checkpoint_load(bbg_solver s, const char *path) {
     fclose(fp);
     return ckpt_restore(s, data.data(), data.size());
 }
+
+// ----------------------------------------------------------------------------
+// particle frames: reading (SerializerLoadSphDataSet3 / SerializerLoadParticles3)
+// ----------------------------------------------------------------------------
+namespace {
+
+// frees and reallocates (no copy): the reader's buffers only grow
+template <class T>
+bbg_status reserve(T **p, size_t need) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    CK(cudaMalloc((void **)p, sizeof(T) * (need ? need : 1)));
+    return BBG_OK;
+}
+
+bbg_status frame_load(bbg_solver s, const char *text, size_t length, int *flags) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!text || !flags) return fail(BBG_ERR_INVALID_ARGUMENT, "null text or flags");
+    FrameSection sec;
+    const int found_section = frame_find_section(text, length, *flags, &sec);
+    if (found_section == 1) return fail(BBG_ERR_INVALID_ARGUMENT, "unknown letter in the section's \"Format\"");
+    if (found_section == 2)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "no complete fluid section (FluidBegin, DataBegin, DataEnd)");
+    if (sec.count <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "the section's \"Count\" is %d", sec.count);
+    if (sec.count > s->capacity)
+        return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", sec.count, s->capacity);
+    const size_t bytes = sec.data_end - sec.data_begin;
+    if (bytes == 0 || bytes >= 0xffffffffu)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "the section's data block has %zu bytes", bytes);
+    FrameReadBufs &R = s->fread;
+    const size_t chunks = (bytes + kLineChunk - 1) / kLineChunk;
+    if (R.text_cap < bytes) {
+        R.text_cap = 0;
+        if (bbg_status r = reserve(&R.text, bytes)) return r;
+        R.text_cap = bytes;
+    }
+    if (R.chunk_cap < chunks + 1) {
+        const size_t need = chunks + 1;
+        R.chunk_cap = 0;
+        bbg_status r = reserve(&R.chunk, need);
+        if (!r) r = reserve(&R.chunk_start, need);
+        if (!r) r = reserve(&R.chunk_part, scan_partials_needed((unsigned)need));
+        if (r) return r;
+        R.chunk_cap = need;
+    }
+    if (!R.pow5) {
+        std::vector<double> p5(kPow5Hi - kPow5Lo + 1), p10(kPow10Max + 1);
+        static const double lut[] = {1.0, 0.1, 0.01, 0.001, 0.0001, 0.00001, 0.000001, 0.0000001};
+        for (int e = kPow5Lo; e <= kPow5Hi; e++) p5[(size_t)(e - kPow5Lo)] = std::pow(5.0, e);
+        for (int r = 0; r <= kPow10Max; r++) p10[(size_t)r] = r < 8 ? lut[r] : std::pow(10.0, -r);
+        bbg_status r = reserve(&R.pow10, p10.size());
+        if (!r) r = reserve(&R.pow5, p5.size());
+        if (r) return r;
+        CK(cudaMemcpy(R.pow5, p5.data(), sizeof(double) * p5.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(R.pow10, p10.data(), sizeof(double) * p10.size(), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpyAsync(R.text, text + sec.data_begin, bytes, cudaMemcpyHostToDevice, s->stream));
+    unsigned lines = 0;
+    CK(frame_split_lines(bytes, R, &lines, s->h_u, s->stream));
+    CK_LAUNCH();
+    if (R.line_cap < (size_t)lines + 1) {
+        const size_t need = (size_t)lines + 1;
+        R.line_cap = 0;
+        bbg_status r = reserve(&R.line, need);
+        if (!r) r = reserve(&R.vals, 6 * need);
+        if (!r) r = reserve(&R.valid, need);
+        if (!r) r = reserve(&R.flag_copy, need);
+        if (!r) r = reserve(&R.index, need);
+        if (!r) r = reserve(&R.line_part, scan_partials_needed((unsigned)need));
+        if (r) return r;
+        R.line_cap = need;
+    }
+    unsigned found = 0;
+    CK(frame_parse_lines(bytes, lines, sec.flags, R, &found, s->h_u, s->stream));
+    CK_LAUNCH();
+    if (found < (unsigned)sec.count)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "the section holds %u particle lines, fewer than its Count %d",
+                    found, sec.count);
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    launch_frame_scatter(lines, sec.count, R, dp, dv, s->stream);
+    CK_LAUNCH();
+    if (bbg_status r = upload_common(s, dp, dv, sec.count)) return r;
+    CK(cudaStreamSynchronize(s->stream));
+    *flags = sec.flags;
+    return BBG_OK;
+}
+
+}  // namespace
+
+bbg_status bbg_frame_load_text(bbg_solver s, const char *text, size_t length, int *flags) {
+    return frame_load(s, text, length, flags);
+}
+
+bbg_status bbg_frame_find_section(const char *text, size_t length, int *flags, int *count, size_t *data_begin,
+                                  size_t *data_end) {
+    if (!text || !flags) return fail(BBG_ERR_INVALID_ARGUMENT, "null text or flags");
+    FrameSection sec;
+    const int st = frame_find_section(text, length, *flags, &sec);
+    if (st == 1) return fail(BBG_ERR_INVALID_ARGUMENT, "unknown letter in the section's \"Format\"");
+    if (st == 2) return fail(BBG_ERR_NOT_FOUND, "no complete fluid section (FluidBegin, DataBegin, DataEnd)");
+    *flags = sec.flags;
+    if (count) *count = sec.count;
+    if (data_begin) *data_begin = sec.data_begin;
+    if (data_end) *data_end = sec.data_end;
+    return BBG_OK;
+}
+
+bbg_status bbg_frame_load(bbg_solver s, const char *path, int *flags) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!path || !flags) return fail(BBG_ERR_INVALID_ARGUMENT, "null path or flags");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(BBG_ERR_NOT_FOUND, "cannot open %s", path);
+    // read until the first section is complete: files of appended frames can be long
+    std::vector<char> data;
+    size_t block = (size_t)16 << 20;
+    FrameSection sec;
+    int st = 2;
+    for (;;) {
+        const size_t old = data.size();
+        data.resize(old + block);
+        const size_t got = fread(data.data() + old, 1, block, fp);
+        data.resize(old + got);
+        st = frame_find_section(data.data(), data.size(), *flags, &sec);
+        if (st != 2 || got < block) break;
+        block *= 2;
+    }
+    fclose(fp);
+    return frame_load(s, data.data(), data.size(), flags);
+}
+

@@ -294,6 +294,17 @@ class Solver:
     def frame_append(self, path, flags=N.FRAME_POSITION):
         N.call("bbg_frame_append", self.h, int(flags), str(path).encode())
 
+    def frame_load(self, source, flags=0):
+        """SerializerLoadSphDataSet3: the first fluid section of a frame (a path, or the
+        frame's bytes) becomes this solver's particles; returns the section's flags."""
+        fl = ctypes.c_int(int(flags))
+        if isinstance(source, (bytes, bytearray)):
+            N.call("bbg_frame_load_text", self.h, bytes(source), len(source), ctypes.byref(fl))
+        else:
+            N.call("bbg_frame_load", self.h, str(source).encode(), ctypes.byref(fl))
+        self.n = self.particle_count()
+        return fl.value
+
     # --- checkpoint (exact resume) ----------------------------------------------
     def checkpoint(self):
         """The solver state as checkpoint bytes (bbg_checkpoint_write)."""
@@ -467,6 +478,16 @@ def format_g(value):
     n = ctypes.c_int()
     N.call("bbg_format_g", float(value), out, ctypes.byref(n))
     return out.raw[:n.value].decode()
+
+
+def frame_section(text, flags=0):
+    """The first fluid section of a frame text (host only): (flags, count, data_begin,
+    data_end) with the data lines at text[data_begin:data_end]."""
+    fl, cnt = ctypes.c_int(int(flags)), ctypes.c_int()
+    a, b = ctypes.c_size_t(), ctypes.c_size_t()
+    N.call("bbg_frame_find_section", bytes(text), len(text), ctypes.byref(fl), ctypes.byref(cnt),
+           ctypes.byref(a), ctypes.byref(b))
+    return fl.value, cnt.value, a.value, b.value
 
 
 def build_grid(domain_min, domain_max, spacing, scale):

@@ -240,6 +240,24 @@ bbg_status bbg_frame_append(bbg_solver s, int flags, const char *path);
 /* printf("%g", (double)value) through the device formatter's code, on the host (at most
  * 14 characters, not terminated). */
 bbg_status bbg_format_g(float value, char *out, int *length);
+/* SerializerLoadSphDataSet3 (src/third/serializer.cpp:562-577): the particles of the
+ * first fluid section of a frame become the solver's particles (positions and velocities;
+ * zero where the section's format lacks them), as if built by a ParticleSetBuilder3 and
+ * uploaded.  The header is read on the host (SerializerFindFluidSection, :145-181); the data
+ * lines are split and parsed on the device with the reference's number reader
+ * (src/third/obj_loader.cpp:56-168, 270-278) in the same double operations, so every value
+ * equals the reference's (NaN payloads aside).  Lines are skipped as the reference skips
+ * them (empty, blank, '#'; with the 'o' rule, boundary value 0); the data ends at the first
+ * line holding "DataEnd".  *flags: in, the flags used when the section has no "Format";
+ * out, the section's.  Errors: no complete section, an unknown format letter, fewer
+ * particle lines than "Count" (the reference reads past its array there), more particles
+ * than the capacity.  A file is read only up to the end of its first section. */
+bbg_status bbg_frame_load(bbg_solver s, const char *path, int *flags);
+bbg_status bbg_frame_load_text(bbg_solver s, const char *text, size_t length, int *flags);
+/* The header step alone (host only, no GPU): the first fluid section's flags (in/out as
+ * above), "Count", and its data lines [*data_begin, *data_end) as byte offsets. */
+bbg_status bbg_frame_find_section(const char *text, size_t length, int *flags, int *count,
+                                  size_t *data_begin, size_t *data_end);
 
 /* ----- checkpoint (exact resume) ------------------------------------------------ */
 /* The reference saves text frames only (SerializerSaveSphDataSet3,

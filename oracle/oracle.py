@@ -114,6 +114,8 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_frame_parse": (ctypes.c_long, [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), _D, _D, _D, _I32, ctypes.c_long]),
         "orc_frame_text": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t]),
     }
@@ -352,4 +354,23 @@ def frame_text(pos, vel=None, rho=None, mass=0.0, spacing=0.0, flags=0x01, varia
     buf = ctypes.create_string_buffer(need + 1)
     lib.orc_frame_text(*args, buf, need + 1)
     return buf.raw[:need]
+
+
+def frame_parse(text, flags=0, variant="f32"):
+    """SerializerLoadParticles3 restated: (flags, header count, pos, vel, density, boundary)
+    of the first fluid section of a frame text; raises ValueError where the reference stops."""
+    lib = load(variant)
+    cap = text.count(b"\n") + text.count(b"\r") + 1
+    pos = np.zeros((cap, 3))
+    vel = np.zeros((cap, 3))
+    rho = np.zeros(cap)
+    bnd = np.zeros(cap, np.int32)
+    fl, cnt = ctypes.c_int(flags), ctypes.c_int(0)
+    n = lib.orc_frame_parse(text, len(text), ctypes.byref(fl), ctypes.byref(cnt), _ptr(pos), _ptr(vel),
+                            _ptr(rho), _ptr(bnd, _I32), cap)
+    if n == -1:
+        raise ValueError("unknown format letter")
+    if n < 0:
+        raise ValueError("no complete fluid section")
+    return fl.value, cnt.value, pos[:n], vel[:n], rho[:n], bnd[:n]
 

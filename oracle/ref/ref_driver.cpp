@@ -222,6 +222,26 @@ void ref_get_buckets(RefSim *s, int32_t *counts, int32_t *ids) {
     }
 }
 
+/* SerializerLoadParticles3 on a frame file: the first fluid section's particles (at most
+ * `capacity` stored; NULL outputs skipped).  Returns the number read (-1: no file). */
+int ref_load_frame(const char *path, int *flags, double *pos, double *vel, double *rho, int *boundary,
+                   int capacity) {
+    std::vector<SerializedParticle> parts;
+    int f = *flags;
+    int n = SerializerLoadParticles3(&parts, path, f);
+    *flags = f;
+    for (int i = 0; i < n && i < capacity; i++) {
+        const SerializedParticle &q = parts[(size_t)i];
+        for (int k = 0; k < 3; k++) {
+            if (pos) pos[3 * i + k] = (double)q.position[k];
+            if (vel) vel[3 * i + k] = (double)q.velocity[k];
+        }
+        if (rho) rho[i] = (double)q.density;
+        if (boundary) boundary[i] = q.boundary;
+    }
+    return n;
+}
+
 /* Appends SerializerSaveSphDataSet3's particle frame of the current state to `path`. */
 void ref_save_frame(RefSim *s, const char *path, int flags) { SerializerSaveSphDataSet3(s->data, path, flags); }
 

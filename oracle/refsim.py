@@ -71,6 +71,8 @@ def load(variant):
         "ref_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "ref_get_buckets": (None, [_P, _I32, _I32]),
         "ref_save_frame": (None, [_P, ctypes.c_char_p, ctypes.c_int]),
+        "ref_load_frame": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _D, _D, _D, _I32,
+                                          ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -145,3 +147,25 @@ class RefSim:
         ids = np.zeros((self.n, 100), np.int32)
         self.lib.ref_get_buckets(self.h, counts.ctypes.data_as(_I32), ids.ctypes.data_as(_I32))
         return counts, ids
+
+
+def load_frame(text, flags=0, variant="f32", capacity=None):
+    """SerializerLoadParticles3 of the reference on a frame text: (flags, pos, vel, density,
+    boundary) of the first fluid section."""
+    import tempfile
+    lib = load(variant)
+    cap = capacity if capacity is not None else max(16, text.count(b"\n") + text.count(b"\r") + 1)
+    pos = np.zeros((cap, 3))
+    vel = np.zeros((cap, 3))
+    rho = np.zeros(cap)
+    bnd = np.zeros(cap, np.int32)
+    fl = ctypes.c_int(flags)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "frame.txt")
+        with open(path, "wb") as f:
+            f.write(text)
+        n = lib.ref_load_frame(path.encode(), ctypes.byref(fl), pos.ctypes.data_as(_D), vel.ctypes.data_as(_D),
+                               rho.ctypes.data_as(_D), bnd.ctypes.data_as(_I32), cap)
+    n = min(n, cap)
+    return fl.value, pos[:n], vel[:n], rho[:n], bnd[:n]
+

@@ -1365,3 +1365,213 @@ size_t orc_frame_text(int n, int flags, const double *pos, const double *vel, co
     frame_put(&o, "FluidEnd\n");
     return o.len;
 }
+
+/* ParseFloat's number reader (src/third/obj_loader.cpp:56-168): decimal mantissa summed in
+ * double, exponent applied as ldexp(m * pow(5, e), e); a malformed token leaves 0. */
+static double frame_parse_double(const char *s, const char *end) {
+    static const double lut[] = {1.0, 0.1, 0.01, 0.001, 0.0001, 0.00001, 0.000001, 0.0000001};
+    double mantissa = 0.0;
+    int exponent = 0, read = 0;
+    char sign = '+', exp_sign = '+';
+    const char *c = s;
+    if (s >= end) return 0.0;
+#define DIGIT(x) ((unsigned)((x) - '0') < 10u)
+    if (*c == '+' || *c == '-') {
+        sign = *c;
+        c++;
+    } else if (!DIGIT(*c)) {
+        return 0.0;
+    }
+    while (c != end && DIGIT(*c)) {
+        mantissa *= 10;
+        mantissa += (int)(*c - '0');
+        c++;
+        read++;
+    }
+    if (read == 0) return 0.0;
+    if (c == end) goto assemble;
+    if (*c == '.') {
+        c++;
+        read = 1;
+        while (c != end && DIGIT(*c)) {
+            mantissa += (int)(*c - '0') * (read < 8 ? lut[read] : pow(10.0, -read));
+            read++;
+            c++;
+        }
+    } else if (*c != 'e' && *c != 'E') {
+        goto assemble;
+    }
+    if (c == end) goto assemble;
+    if (*c == 'e' || *c == 'E') {
+        c++;
+        if (c != end && (*c == '+' || *c == '-')) {
+            exp_sign = *c;
+            c++;
+        } else if (c == end || !DIGIT(*c)) {   /* the character at the end is a delimiter */
+            return 0.0;
+        }
+        read = 0;
+        while (c != end && DIGIT(*c)) {
+            exponent *= 10;
+            exponent += (int)(*c - '0');
+            c++;
+            read++;
+        }
+        exponent *= (exp_sign == '+' ? 1 : -1);
+        if (read == 0) return 0.0;
+    }
+assemble:
+#undef DIGIT
+    return (sign == '+' ? 1 : -1) * (exponent ? ldexp(mantissa * pow(5.0, exponent), exponent) : mantissa);
+}
+
+/* ParseFloat: skip spaces/tabs, the token ends at a space, tab, '\r' or the line's end. */
+static Float frame_parse_float(const char **t, const char *line_end) {
+    const char *p = *t;
+    while (p < line_end && (*p == ' ' || *p == '\t')) p++;
+    const char *e = p;
+    while (e < line_end && *e != ' ' && *e != '\t' && *e != '\r') e++;
+    *t = e;
+    return (Float)frame_parse_double(p, e);
+}
+
+static void frame_skip_blanks(const char **t, const char *line_end) {
+    while (*t < line_end && (**t == ' ' || **t == '\t')) (*t)++;
+}
+
+/* GetLine (src/third/obj_loader.cpp:253-268): a line ends at "\n", "\r\n" or "\r". */
+static int frame_next_line(const char *text, size_t length, size_t *pos, size_t *a, size_t *b) {
+    size_t i = *pos;
+    if (i >= length) return 0;
+    *a = i;
+    while (i < length && text[i] != '\n' && text[i] != '\r') i++;
+    *b = i;
+    if (i < length) i += (text[i] == '\r' && i + 1 < length && text[i + 1] == '\n') ? 2 : 1;
+    *pos = i;
+    return 1;
+}
+
+/* The line's characters as a C string sees them (up to an embedded NUL). */
+static size_t frame_c_end(const char *text, size_t a, size_t b) {
+    size_t i = a;
+    while (i < b && text[i] != '\0') i++;
+    return i;
+}
+
+static int frame_flags_from(const char *f, size_t len) {
+    int flags = 0;
+    for (size_t i = 0; i < len; i++) {
+        switch (f[i]) {
+            case 'p': case 'P': flags |= 0x01; break;
+            case 'v': case 'V': flags |= 0x02; break;
+            case 'd': case 'D': flags |= 0x04; break;
+            case 'm': case 'M': flags |= 0x20; break;
+            case 'b': case 'B': flags |= 0x08; break;
+            case 'n': case 'N': flags |= 0x10; break;
+            case 'l': case 'L': flags |= 0x40; break;
+            case 'o': case 'O': flags |= 0x100; break;
+            case 'z': case 'Z': flags |= 0x80; break;
+            default: return -1;
+        }
+    }
+    return flags;
+}
+
+long orc_frame_parse(const char *text, size_t length, int *flags, int *count, double *pos, double *vel,
+                     double *rho, int *boundary, long capacity) {
+    size_t at = 0, a, b;
+    int in_region = 0, pcount = 0, found = 0;
+    const char *fmt = NULL;
+    size_t fmt_len = 0;
+    /* header: tokens split at spaces, tabs and the line end */
+    while (!found && frame_next_line(text, length, &at, &a, &b)) {
+        const size_t ce = frame_c_end(text, a, b);
+        size_t tok = a;
+        for (size_t i = a; i <= b && !found; i++) {
+            const int sep = i == b || text[i] == ' ' || text[i] == '\t' || text[i] == '\0';
+            if (!sep) continue;
+            const size_t tl = i - tok;
+            if (tl > 0) {
+                const char *t = text + tok;
+                if (!in_region) {
+                    if (tl == 10 && !memcmp(t, "FluidBegin", 10)) in_region = 1;
+                } else if (tl == 7 && !memcmp(t, "\"Count\"", 7)) {
+                    /* the value follows the separator; a token ending the line is processed
+                       with index 0, so its value is read from the line's second character */
+                    const char *v = text + (i < b ? i + 1 : a + 1);
+                    while (v < text + ce && (*v == ' ' || *v == '\t')) v++;
+                    pcount = (int)frame_parse_float(&v, text + ce);
+                } else if (tl == 8 && !memcmp(t, "\"Format\"", 8)) {
+                    const char *v = text + (i < b ? i + 1 : a + 1);
+                    while (v < text + ce && (*v == ' ' || *v == '\t')) v++;
+                    fmt = v;
+                    fmt_len = 0;
+                    while (v + fmt_len < text + ce && v[fmt_len] != ' ' && v[fmt_len] != '\t') fmt_len++;
+                } else if (tl == 9 && !memcmp(t, "DataBegin", 9)) {
+                    found = 1;
+                } else if (tl == 8 && !memcmp(t, "FluidEnd", 8)) {
+                    in_region = 0;
+                }
+            }
+            tok = i + 1;
+        }
+    }
+    if (count) *count = pcount;
+    if (fmt && fmt_len > 0) {
+        const int f = frame_flags_from(fmt, fmt_len);
+        if (f < 0) return -1;
+        *flags = f;
+    }
+    if (!found) return -2;
+    const int fl = *flags;
+    long size = 0;
+    int ended = 0;
+    while (frame_next_line(text, length, &at, &a, &b)) {
+        const char *end = text + frame_c_end(text, a, b);
+        const char *t = text + a;
+        if (t == end) continue;
+        frame_skip_blanks(&t, end);
+        if (t == end || *t == '#') continue;
+        {
+            int has_end = 0;
+            for (const char *q = t; q + 7 <= end && !has_end; q++) has_end = !memcmp(q, "DataEnd", 7);
+            if (has_end) {
+                ended = 1;
+                break;
+            }
+        }
+        Float p3[3] = {0, 0, 0}, v3[3] = {0, 0, 0}, d = 0;
+        int bnd = 0;
+        if (fl & 0x01) {
+            for (int k = 0; k < 3; k++) p3[k] = frame_parse_float(&t, end);
+            frame_skip_blanks(&t, end);
+        }
+        if (fl & 0x02) {
+            for (int k = 0; k < 3; k++) v3[k] = frame_parse_float(&t, end);
+            frame_skip_blanks(&t, end);
+        }
+        if (fl & 0x04) {
+            d = frame_parse_float(&t, end);
+            frame_skip_blanks(&t, end);
+        }
+        if (fl & 0x20) {
+            (void)frame_parse_float(&t, end);
+            frame_skip_blanks(&t, end);
+        }
+        if (fl & 0x08) {
+            bnd = (int)frame_parse_float(&t, end);
+            frame_skip_blanks(&t, end);
+            if ((fl & 0x100) && !bnd) continue;
+        }
+        if (size < capacity) {
+            for (int k = 0; k < 3; k++) {
+                if (pos) pos[3 * size + k] = (double)p3[k];
+                if (vel) vel[3 * size + k] = (double)v3[k];
+            }
+            if (rho) rho[size] = (double)d;
+            if (boundary) boundary[size] = bnd;
+        }
+        size++;
+    }
+    return ended ? size : -2;
+}

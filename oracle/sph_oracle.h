@@ -169,6 +169,18 @@ int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
 size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
                         double mass, double spacing, char *buf, size_t capacity);
 
+/* SerializerLoadParticles3 (src/third/serializer.cpp:540-560): the first fluid section of a
+ * frame text -- header tokens (SerializerFindFluidSection / SerializerFluidProcessToken,
+ * :83-181), then one particle per data line up to the first non-comment line holding
+ * "DataEnd" (_SerializerLoadParticles3, :450-538), every number read by ParseFloat
+ * (src/third/obj_loader.cpp:56-168, 270-278).  *flags: in, the flags used when the
+ * section has no "Format"; out, the section's.  Stores at most `capacity` particles
+ * (pos/vel xyz, density, boundary; any may be NULL) and returns how many data lines were
+ * read; *count receives the header's "Count".  Returns -1 for an unknown format letter,
+ * -2 without a fluid section or without "DataEnd". */
+long     orc_frame_parse(const char *text, size_t length, int *flags, int *count, double *pos,
+                         double *vel, double *rho, int *boundary, long capacity);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,10 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
   frame_f32.npz   the particle frames SerializerSaveSphDataSet3 (third/serializer.cpp)
                   appends for the FP32 PCISPH state after those 3 substeps, with the
                   position/velocity/density/mass flags and with position only, beside the
-                  state they print.
+                  state they print; what SerializerLoadParticles3 reads back from the first
+                  frame; and a hand-written frame of awkward lines (comments, blank lines,
+                  CR and CRLF ends, tabs, malformed and out-of-range numbers) with what the
+                  reference reads from it.
 
     python tests/golden/make_golden.py           # every fixture
     python tests/golden/make_golden.py frames    # frame_f32.npz only
@@ -102,6 +105,24 @@ def make(variant):
     np.savez_compressed(os.path.join(HERE, "sph_%s.npz" % variant), **o2)
 
 
+# a frame section written by hand: the reader's corner cases (the reference reads it, the
+# stored arrays are its result)
+AWKWARD = (b"# a comment before the section\n"
+           b"FluidBegin\n\t\"Type\" particles\n\t\"Count\" 10\n\t\"Format\" pv\n\t\"Spacing\" 0.02\n"
+           b"\tDataBegin\n"
+           b"\t\t0.1 0.2 0.3 1 2 3\n"
+           b"\t\t-0.5 +0.25 1e-3 -1.5e+2 2.5E-1 0\n"
+           b"\t\t7 8 9 0.000001 123456789 -0\r\n"
+           b"\n"
+           b"   # comment line inside data DataEnd\n"
+           b"\t\t1.23456789012345 0.333333333333333333 1e10 1e-10 -7.25e+03 3.4028235e38\n"
+           b"\t\t.5 nan -inf 1e+ 1.5e 12abc\n"
+           b"  \t 5\t6\t7 8 9 10\n"
+           b"\t\t1e-45 1e-46 2e38 4e38 1.17549435e-38 -3.14159265358979\r\t\t42\n"
+           b"\t\t1.0e400 1e-400 00012.50000 -.25 +-1 0x10\n"
+           b"\t\t0e500 1.e5 5e 7e- 0.1234567891234 99999999999999999999999\n"
+           b"\tDataEnd\nFluidEnd\n")
+
 FRAME_FLAGS = {"pvdm": 0x01 | 0x02 | 0x04 | 0x20, "p": 0x01}   # SERIALIZER_* (third/serializer.h)
 
 
@@ -116,6 +137,12 @@ def make_frames():
         out["step3_" + name] = r.get(FIELDS[name])
     for name, flags in FRAME_FLAGS.items():
         out["frame_" + name] = np.frombuffer(r.frame(flags), dtype=np.uint8)
+    fl, p, v, d, _ = R.load_frame(r.frame(FRAME_FLAGS["pvdm"]), 0)
+    out["load_pvdm_flags"], out["load_pvdm_pos"], out["load_pvdm_vel"], out["load_pvdm_density"] = \
+        np.array(fl), p, v, d
+    out["awkward_frame"] = np.frombuffer(AWKWARD, dtype=np.uint8)
+    fl, p, v, d, _ = R.load_frame(AWKWARD, 0)
+    out["awkward_flags"], out["awkward_pos"], out["awkward_vel"] = np.array(fl), p, v
     np.savez_compressed(os.path.join(HERE, "frame_f32.npz"), **out)
 
 

@@ -1,8 +1,10 @@
-"""Particle frames in the reference's text format (SerializerSaveSphDataSet3).
+"""Particle frames in the reference's text format (SerializerSaveSphDataSet3 writes them,
+SerializerLoadSphDataSet3 reads them).
 
-The oracle's restatement (oracle/sph_oracle.c, orc_frame_text) is pinned against the bytes
-the reference serializer itself wrote (tests/golden/frame_f32.npz); the device writer and
-its host formatter are compared with both, byte for byte.
+The oracle's restatements (oracle/sph_oracle.c: orc_frame_text, orc_frame_parse) are pinned
+against the reference itself (tests/golden/frame_f32.npz: the bytes its serializer wrote,
+the values its reader read, from its own frame and from a frame of awkward lines); the
+device writer and reader are compared with both, byte for byte and bit for bit.
 """
 import json
 import os
@@ -16,6 +18,16 @@ from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "frame_f32.npz")
 PVDM = bb.FRAME_POSITION | bb.FRAME_VELOCITY | bb.FRAME_DENSITY | bb.FRAME_MASS
+
+
+def bits_equal(a, b):
+    """Bitwise equality of float arrays, any NaN matching any NaN (payloads differ by CPU)."""
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    if a.shape != b.shape:
+        return False
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32)))
 
 
 def golden():
@@ -94,6 +106,38 @@ def test_host_formatter_reproduces_reference_lines(native):
         assert "\t\t" + " ".join(fields) == ref[start + i], i
 
 
+def test_oracle_reader_is_the_reference_reader():
+    """The oracle's SerializerLoadParticles3 restatement reads what the reference read, from
+    a frame it wrote and from the hand-written frame of awkward lines."""
+    g, _ = golden()
+    fl, cnt, p, v, d, _ = O.frame_parse(g["frame_pvdm"].tobytes())
+    assert fl == int(g["load_pvdm_flags"]) == PVDM and cnt == len(p) == 1440
+    assert bits_equal(p, g["load_pvdm_pos"]) and bits_equal(v, g["load_pvdm_vel"])
+    assert bits_equal(d, g["load_pvdm_density"])
+    fl, cnt, p, v, _, _ = O.frame_parse(g["awkward_frame"].tobytes())
+    assert fl == int(g["awkward_flags"]) and cnt == len(p) == 10
+    assert bits_equal(p, g["awkward_pos"]) and bits_equal(v, g["awkward_vel"])
+
+
+def test_section_finder(native):
+    g, _ = golden()
+    text = g["awkward_frame"].tobytes()
+    fl, cnt, a, b = bb.frame_section(text)
+    assert (fl, cnt) == (3, 10)
+    assert text[a:].startswith(b"\t\t0.1 0.2 0.3") and text[b:].startswith(b"\tDataEnd\n")
+    assert b"# comment line inside data DataEnd" in text[a:b]   # a comment does not end the data
+    two = g["frame_pvdm"].tobytes() + g["frame_p"].tobytes()
+    fl, cnt, a, b = bb.frame_section(two)
+    assert fl == PVDM and two[b:].startswith(b"\tDataEnd\nFluidEnd\nFluidBegin")   # the first section
+    assert bb.frame_section(b"FluidBegin\n\t\"Count\" 2\n\tDataBegin\n\t\t1 2 3\n\tDataEnd\n", 1)[0] == 1
+    for bad in (text.replace(b"\tDataEnd", b"\tDataStop"), text.replace(b"DataBegin", b"DataBeg"),
+                text.replace(b"FluidBegin", b"FluidStart")):
+        with pytest.raises(bb.BbgError):
+            bb.frame_section(bad)
+    with pytest.raises(bb.BbgError):
+        bb.frame_section(text.replace(b"\"Format\" pv", b"\"Format\" pq"))   # unknown letter
+
+
 # ---------------------------------------------------------------------------------------
 # GPU: the device writer
 # ---------------------------------------------------------------------------------------
@@ -155,3 +199,64 @@ def test_frame_full_size_1m(gpu):
         want = O.frame_text(p, v, rho, s.scalars()["mass"], sc["spacing"], PVDM)
         assert len(text) == len(want)
         assert text == want
+
+
+# ---------------------------------------------------------------------------------------
+# GPU: the device reader
+# ---------------------------------------------------------------------------------------
+@pytest.mark.gpu
+def test_frame_load_matches_reference_reader(gpu):
+    g, sc = golden()
+    with bb.Solver(sc, capacity=1440) as s:
+        assert s.frame_load(g["frame_pvdm"].tobytes()) == PVDM
+        p, v = s.download()
+        assert s.n == 1440
+        assert bits_equal(p, g["load_pvdm_pos"]) and bits_equal(v, g["load_pvdm_vel"])
+    with bb.Solver(sc, capacity=16) as s:
+        assert s.frame_load(g["awkward_frame"].tobytes()) == int(g["awkward_flags"])
+        p, v = s.download()
+        assert bits_equal(p, g["awkward_pos"]) and bits_equal(v, g["awkward_vel"])
+
+
+@pytest.mark.gpu
+def test_frame_load_full_size_round_trip(gpu, tmp_path):
+    """1,048,576 particles in motion: frame written on the device, appended twice to a file,
+    read back on the device from the file's first section; equal to the oracle's reading,
+    and within the six printed digits of the state."""
+    sc, pos = bb.scenes.pcisph_1m()
+    with bb.Solver(sc, pos=pos) as s:
+        for _ in range(3):
+            s.advance_time_step(sc["dt"])
+        p0, v0 = s.download()
+        text = s.frame_text(PVDM)
+        path = tmp_path / "frames.txt"
+        s.frame_append(path, PVDM)
+        s.frame_append(path, PVDM)
+    fl, cnt, pw, vw, _, _ = O.frame_parse(text)
+    assert cnt == len(pw) == len(pos)
+    with bb.Solver(sc, capacity=len(pos)) as r:
+        assert r.frame_load(path) == PVDM
+        p, v = r.download()
+    assert bits_equal(p, pw) and bits_equal(v, vw)
+    assert np.all(np.abs(p - p0) <= 5.2e-6 * np.maximum(np.abs(p0), 1e-30))   # six digits
+    assert np.all(np.abs(v - v0) <= 5.2e-6 * np.maximum(np.abs(v0), 1e-30))
+
+
+@pytest.mark.gpu
+def test_frame_load_refusals(gpu, small):
+    sc, pos = small
+    g, _ = golden()
+    text = g["frame_pvdm"].tobytes()
+    with bb.Solver(sc, pos=pos[:100], capacity=1440) as s:
+        before = s.download()
+        for bad in (text.replace(b"\tDataEnd", b"\tDataStop"),            # unterminated
+                    text.replace(b"\"Count\" 1440", b"\"Count\" 1441"),   # fewer lines than Count
+                    text.replace(b"\"Format\" pvdm", b"\"Format\" pvdq")):  # unknown letter
+            with pytest.raises(bb.BbgError):
+                s.frame_load(bad)
+            after = s.download()
+            assert np.array_equal(before[0], after[0])
+    with bb.Solver(sc, capacity=1000) as s:
+        with pytest.raises(bb.BbgError):
+            s.frame_load(text)   # capacity
+
