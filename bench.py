@@ -314,6 +314,49 @@ def timed_substeps(g, dt, steps, stream, flush, events=True):
     return ms, iters, errs
 
 
+def frame_io(bb, g, scene, n, device, reps=5):
+    """Particle frames of the final state in the reference's text format, end to end through
+    the C ABI: the device writer formats and packs the frame and delivers its bytes to host
+    memory (SerializerSaveSphDataSet3's block); the device reader takes the bytes back
+    (SerializerLoadSphDataSet3) into a second solver.  Median of `reps` calls each; the CPU
+    leg times the oracle's restatement of the reference serializer and reader (single
+    thread, as the reference) on a slice of the same frame and scales it per particle."""
+    from oracle import oracle as O
+    flags = bb.FRAME_POSITION | bb.FRAME_VELOCITY | bb.FRAME_DENSITY | bb.FRAME_MASS
+    size = len(g.frame_text(flags))
+    out = bytearray(size)
+    w = []
+    for _ in range(reps + 1):
+        t0 = time.perf_counter()
+        g.frame_text(flags, out=out)
+        w.append(time.perf_counter() - t0)
+    text = bytes(out)
+    r = bb.Solver(dict(scene), capacity=n, device=device)
+    rd = []
+    for _ in range(reps + 1):
+        t0 = time.perf_counter()
+        r.frame_load(text)
+        rd.append(time.perf_counter() - t0)
+    r.close()
+    w, rd = float(np.median(w[1:])), float(np.median(rd[1:]))
+    # CPU: a slice of 131,072 particles of the same frame
+    fl, cnt, p, v, d, _ = O.frame_parse(text)
+    m = min(len(p), 131072)
+    mass = g.scalars()["mass"]
+    t0 = time.perf_counter()
+    sub = O.frame_text(p[:m], v[:m], d[:m], mass, scene["spacing"], flags)
+    cw = (time.perf_counter() - t0) * len(p) / m
+    t0 = time.perf_counter()
+    O.frame_parse(sub)
+    cr = (time.perf_counter() - t0) * len(p) / m
+    return {"particles": n, "flags": "pvdm", "bytes": size,
+            "write_ms": 1e3 * w, "write_gb_per_s": size / w / 1e9,
+            "read_ms": 1e3 * rd, "read_gb_per_s": size / rd / 1e9,
+            "cpu": {"kind": "port", "cores": 1, "write_ms": 1e3 * cw, "read_ms": 1e3 * cr,
+                    "sample": "%d particles of the same frame, scaled per particle" % m},
+            "measured": "host wall clock around the C-ABI calls (frame bytes in pageable host memory)"}
+
+
 def run_ours(args, scene, pos):
     import torch
 
@@ -455,6 +498,9 @@ def run_ours(args, scene, pos):
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
         batch_offsets = g.layout() if scene.get("batch") else None
+        frames = None
+        if not scene.get("batch") and not args.no_frames and rank == 0:
+            frames = frame_io(bb, g, scene, n, local)
         g.close()
 
     if rank != 0:
@@ -549,6 +595,8 @@ def run_ours(args, scene, pos):
         "clocks": sampler.summary(),
         "kernels": per_kernel,
     }
+    if frames is not None:
+        line["frame_io"] = frames
     print(json.dumps(line), flush=True)
     barrier(dist)
 
@@ -568,6 +616,7 @@ def main():
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
+    ap.add_argument("--no-frames", action="store_true", help="skip the particle-frame writer / reader timing")
     ap.add_argument("--no-tuning", action="store_true",
                     help="ignore bubbles_gb300/tuned/<config>.json (autotuner output)")
     ap.add_argument("--variant", default="learned", choices=["plain", "warm", "learned"],

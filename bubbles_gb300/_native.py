@@ -88,6 +88,13 @@ class Shape(ctypes.Structure):
                 ("friction", ctypes.c_double)]
 
 
+class EmitterDesc(ctypes.Structure):
+    _fields_ = [("shape", Shape), ("use_bounds", ctypes.c_int),
+                ("bounds_min", ctypes.c_double * 3), ("bounds_max", ctypes.c_double * 3),
+                ("spacing", ctypes.c_double), ("jitter", ctypes.c_double),
+                ("initial_velocity", ctypes.c_double * 3), ("max_particles", ctypes.c_int)]
+
+
 class StepStats(ctypes.Structure):
     _fields_ = [("substeps", ctypes.c_int),
                 ("iterations", ctypes.c_int),
@@ -171,13 +178,15 @@ SIGNATURES = {
     "bbg_batch_upload": [_P, _FP, _FP],
     "bbg_batch_download": [_P, _FP, _FP],
     "bbg_batch_scene_stats": [_P, _IP, _DP],
-    "bbg_frame_text": [_P, _I, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+    "bbg_frame_text": [_P, _I, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "bbg_frame_append": [_P, _I, ctypes.c_char_p],
     "bbg_format_g": [ctypes.c_float, ctypes.c_char_p, _IP],
     "bbg_frame_load": [_P, ctypes.c_char_p, _IP],
     "bbg_frame_load_text": [_P, ctypes.c_char_p, ctypes.c_size_t, _IP],
     "bbg_frame_find_section": [ctypes.c_char_p, ctypes.c_size_t, _IP, _IP, ctypes.POINTER(ctypes.c_size_t),
                                ctypes.POINTER(ctypes.c_size_t)],
+    "bbg_emitter_desc_default": [ctypes.POINTER(EmitterDesc)],
+    "bbg_emit_volume": [_P, ctypes.POINTER(EmitterDesc), _I, _IP],
     "bbg_checkpoint_save": [_P, ctypes.c_char_p],
     "bbg_checkpoint_load": [_P, ctypes.c_char_p],
     "bbg_checkpoint_write": [_P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],

@@ -3,6 +3,7 @@
 // grid.cu and sph.cu.
 #include "../../include/bbg.h"
 #include "bbg_kernels.h"
+#include "emit.h"
 #include "frame.h"
 #include "gfmt.h"
 #include "host_math.h"
@@ -14,6 +15,7 @@
 #include <cstring>
 #include <new>
 #include <random>
+#include <string>
 #include <vector>
 
 using namespace bbg;
@@ -108,6 +110,7 @@ struct bbg_solver_s {
     unsigned short *d_scene = nullptr;
     FrameBufs frame;             // particle-frame writer buffers (allocated on first use)
     FrameReadBufs fread;         // frame reader buffers (grown on use)
+    EmitBufs emit;               // emitter buffers (grown on use)
 };
 
 namespace {
@@ -189,6 +192,11 @@ void free_frame(bbg_solver s) {
     for (void *p : rptrs)
         if (p) cudaFree(p);
     R = FrameReadBufs();
+    EmitBufs &E = s->emit;
+    void *eptrs[] = {E.target, E.offset, E.flag, E.flag_copy, E.index, E.part};
+    for (void *p : eptrs)
+        if (p) cudaFree(p);
+    E = EmitBufs();
 }
 
 bbg_status free_all(bbg_solver s) {
@@ -1694,7 +1702,9 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
 // particle frames (SerializerSaveSphDataSet3 format)
 // ----------------------------------------------------------------------------
 namespace {
-bbg_status frame_build(bbg_solver s, int flags, std::vector<char> *text) {
+// Formats the frame's particle lines on the device; *head receives the header text and
+// *body the byte count of the lines waiting in s->frame.out.
+bbg_status frame_build(bbg_solver s, int flags, std::string *head, size_t *body) {
     if (bbg_status r = check_solver(s)) return r;
     if (!(flags & kFrameSupported) || (flags & ~kFrameSupported))
         return fail(BBG_ERR_INVALID_ARGUMENT, "frame flags must combine position, velocity, density and mass");
@@ -1721,10 +1731,11 @@ bbg_status frame_build(bbg_solver s, int flags, std::vector<char> *text) {
     launch_frame_lines(s->n, flags, s->B.pos[s->state], s->B.vel[s->state], s->B.rho, s->B.slot, s->mass, F,
                        s->stream);
     CK_LAUNCH();
-    unsigned body = 0;
     CK(cudaMemcpyAsync(s->h_u, &F.offset[s->n], sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    memcpy(&body, s->h_u, sizeof(unsigned));
+    unsigned lines_bytes = 0;
+    memcpy(&lines_bytes, s->h_u, sizeof(unsigned));
+    *body = lines_bytes;
     char fmt[16];
     int k = 0;
     if (flags & kFramePosition) fmt[k++] = 'p';
@@ -1732,39 +1743,46 @@ bbg_status frame_build(bbg_solver s, int flags, std::vector<char> *text) {
     if (flags & kFrameDensity) fmt[k++] = 'd';
     if (flags & kFrameMass) fmt[k++] = 'm';
     fmt[k] = 0;
-    char head[256];
-    const int hl = snprintf(head, sizeof(head),
+    char h[256];
+    const int hl = snprintf(h, sizeof(h),
                             "FluidBegin\n\t\"Type\" particles\n\t\"Count\" %d\n\t\"Format\" %s\n"
                             "\t\"Spacing\" %g\n\tDataBegin\n",
                             s->n, fmt, (double)(float)s->desc.target_spacing);   // Float spacing
-    static const char tail[] = "\tDataEnd\nFluidEnd\n";
-    text->resize((size_t)hl + body + sizeof(tail) - 1);
-    memcpy(text->data(), head, (size_t)hl);
-    CK(cudaMemcpy(text->data() + hl, F.out, body, cudaMemcpyDeviceToHost));
-    memcpy(text->data() + hl + body, tail, sizeof(tail) - 1);
+    head->assign(h, (size_t)hl);
     return BBG_OK;
 }
+
+const char kFrameTail[] = "\tDataEnd\nFluidEnd\n";
+constexpr size_t kFrameTailLen = sizeof(kFrameTail) - 1;
 }  // namespace
 
 bbg_status bbg_frame_text(bbg_solver s, int flags, char *buf, size_t capacity, size_t *length) {
-    std::vector<char> text;
-    if (bbg_status r = frame_build(s, flags, &text)) return r;
-    if (length) *length = text.size();
-    if (!buf || capacity < text.size())
-        return fail(BBG_ERR_CAPACITY, "the frame needs %zu bytes", text.size());
-    memcpy(buf, text.data(), text.size());
+    std::string head;
+    size_t body = 0;
+    if (bbg_status r = frame_build(s, flags, &head, &body)) return r;
+    const size_t total = head.size() + body + kFrameTailLen;
+    if (length) *length = total;
+    if (!buf || capacity < total) return fail(BBG_ERR_CAPACITY, "the frame needs %zu bytes", total);
+    memcpy(buf, head.data(), head.size());
+    CK(cudaMemcpy(buf + head.size(), s->frame.out, body, cudaMemcpyDeviceToHost));
+    memcpy(buf + head.size() + body, kFrameTail, kFrameTailLen);
     return BBG_OK;
 }
 
 bbg_status bbg_frame_append(bbg_solver s, int flags, const char *path) {
     if (!path) return fail(BBG_ERR_INVALID_ARGUMENT, "null path");
-    std::vector<char> text;
-    if (bbg_status r = frame_build(s, flags, &text)) return r;
+    std::string head;
+    size_t body = 0;
+    if (bbg_status r = frame_build(s, flags, &head, &body)) return r;
+    std::vector<char> text(head.size() + body + kFrameTailLen);
+    memcpy(text.data(), head.data(), head.size());
+    CK(cudaMemcpy(text.data() + head.size(), s->frame.out, body, cudaMemcpyDeviceToHost));
+    memcpy(text.data() + head.size() + body, kFrameTail, kFrameTailLen);
     FILE *fp = fopen(path, "a+");
     if (!fp) return fail(BBG_ERR_INVALID_ARGUMENT, "cannot open %s", path);
     const size_t w = fwrite(text.data(), 1, text.size(), fp);
-    fclose(fp);
-    if (w != text.size()) return fail(BBG_ERR_INVALID_ARGUMENT, "short write to %s", path);
+    const int closed = fclose(fp);
+    if (w != text.size() || closed != 0) return fail(BBG_ERR_INVALID_ARGUMENT, "short write to %s", path);
     return BBG_OK;
 }
 
@@ -2149,5 +2167,149 @@ bbg_status bbg_frame_load(bbg_solver s, const char *path, int *flags) {
     }
     fclose(fp);
     return frame_load(s, data.data(), data.size(), flags);
+}
+
+// ----------------------------------------------------------------------------
+// seeding: VolumeParticleEmitter3 (src/core/emitter.cpp:8-12, 241-330)
+// ----------------------------------------------------------------------------
+bbg_status bbg_emitter_desc_default(bbg_emitter_desc *d) {
+    if (!d) return fail(BBG_ERR_INVALID_ARGUMENT, "null desc");
+    memset(d, 0, sizeof(*d));
+    d->shape.type = BBG_SHAPE_BOX;
+    d->shape.size[0] = d->shape.size[1] = d->shape.size[2] = 1.0;
+    d->spacing = 0.02;
+    d->max_particles = 0x7fffffff;   // IntInfinity
+    return BBG_OK;
+}
+
+namespace {
+
+// rand_float (src/core/geometry.h:1900-1902): rand() over RAND_MAX + 1 as floats
+float rand_float() { return (float)rand() / ((float)RAND_MAX + 1.f); }
+
+// The emitter's lattice: bounds (the shape's, a translated object box, or the given ones,
+// ordered like a Bounds3f) and BccLatticePointGenerator::ForEach's loop counts, in the
+// reference's float operations.
+Lattice emitter_lattice(const bbg_emitter_desc &e) {
+    Lattice L;
+    float lo[3], hi[3];
+    if (e.use_bounds) {
+        for (int k = 0; k < 3; k++) {
+            const float a = (float)e.bounds_min[k], b = (float)e.bounds_max[k];
+            lo[k] = a < b ? a : b;
+            hi[k] = a > b ? a : b;
+        }
+    } else {
+        for (int k = 0; k < 3; k++) {
+            const float h = e.shape.type == BBG_SHAPE_BOX ? (float)((double)(float)e.shape.size[k] / 2.0)
+                                                          : (float)e.shape.size[0];
+            const float t = (float)e.shape.center[k];
+            lo[k] = -h + t;
+            hi[k] = h + t;
+        }
+    }
+    const float sp = (float)e.spacing, half = sp / 2;
+    const float width = hi[0] - lo[0], height = hi[1] - lo[1], depth = hi[2] - lo[2];
+    auto count = [](float step, float off, float extent) {
+        int c = 0;
+        while ((float)c * step + off <= extent) c++;
+        return c;
+    };
+    for (int k = 0; k < 3; k++) L.lo[k] = lo[k];
+    L.spacing = sp;
+    L.half = half;
+    L.layers = count(half, 0.f, depth);
+    L.i0 = count(sp, 0.f, width);
+    L.j0 = count(sp, 0.f, height);
+    L.i1 = count(sp, half, width);
+    L.j1 = count(sp, half, height);
+    const long long s0 = (long long)L.i0 * L.j0, s1 = (long long)L.i1 * L.j1;
+    L.total = (long long)(L.layers / 2) * (s0 + s1) + (L.layers % 2 ? s0 : 0);
+    return L;
+}
+
+}  // namespace
+
+bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *e, int append, int *emitted) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!e) return fail(BBG_ERR_INVALID_ARGUMENT, "null emitter");
+    if (e->shape.type != BBG_SHAPE_BOX && e->shape.type != BBG_SHAPE_SPHERE)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "emitter shape must be a box or a sphere");
+    if (!(e->spacing > 0) || e->max_particles < 0 || !(e->jitter >= 0))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "emitter needs spacing > 0, jitter >= 0, max_particles >= 0");
+    if (append && s->n > 0 && s->nscenes > 0)
+        return fail(BBG_ERR_STATE, "appending to a batch of scenes is not supported");
+    const Lattice L = emitter_lattice(*e);
+    if (L.total >= 0x7fffffffll)
+        return fail(BBG_ERR_CAPACITY, "the emitter's lattice has %lld points", L.total);
+    const float sp = (float)e->spacing;
+    const float max_jitter = (float)(0.5 * (double)(float)e->jitter * (double)sp);
+    // the rand() sequence of the reference's loop: two values per lattice point, the
+    // second landing in u[0] (vec2f u(rand_float(), rand_float()) as built); the offsets
+    // are max_jitter * SampleSphere(u) in float operations
+    const size_t P = (size_t)L.total;
+    const bool jitter = max_jitter != 0.f;
+    std::vector<float> off(jitter ? 3 * P : 0);
+    for (size_t t = 0; t < P; t++) {
+        const float u1 = rand_float();
+        const float u0 = rand_float();
+        if (!jitter) continue;
+        const float usqrt = 2 * std::sqrt(u1 * (1 - u1));
+        const float utheta = (float)(2 * 3.14159265358979323846 * (double)u0);
+        off[3 * t] = std::cos(utheta) * usqrt * max_jitter;
+        off[3 * t + 1] = std::sin(utheta) * usqrt * max_jitter;
+        off[3 * t + 2] = (1 - 2 * u1) * max_jitter;
+    }
+    int count = 0;
+    if (P > 0) {
+        EmitBufs &E = s->emit;
+        if (E.cap < P + 1) {
+            E.cap = 0;
+            bbg_status r = reserve(&E.target, 3 * (P + 1));
+            if (!r) r = reserve(&E.offset, 3 * (P + 1));
+            if (!r) r = reserve(&E.flag, P + 1);
+            if (!r) r = reserve(&E.flag_copy, P + 1);
+            if (!r) r = reserve(&E.index, P + 1);
+            if (!r) r = reserve(&E.part, scan_partials_needed((unsigned)(P + 1)));
+            if (r) return r;
+            E.cap = P + 1;
+        }
+        if (jitter) CK(cudaMemcpyAsync(E.offset, off.data(), sizeof(float) * off.size(), cudaMemcpyHostToDevice,
+                                       s->stream));
+        ShapeDev sd = shape_dev(e->shape);
+        unsigned inside = 0;
+        CK(emit_test(L, sd, float_above(1e-8), float_above(1e-6), jitter, E, &inside, s->h_u, s->stream));
+        CK_LAUNCH();
+        count = (int)(inside < (unsigned)e->max_particles ? inside : (unsigned)e->max_particles);
+    }
+    const int first = append ? s->n : 0;
+    if (first + count > s->capacity)
+        return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", first + count, s->capacity);
+    if (emitted) *emitted = count;
+    if (count == 0) return BBG_OK;
+    // velocity(target) + initVel with the zero velocity field
+    const float3 v = make_float3(0.f + (float)e->initial_velocity[0], 0.f + (float)e->initial_velocity[1],
+                                 0.f + (float)e->initial_velocity[2]);
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    launch_emit_scatter(L, count, s->emit, v, dp, dv, s->stream);
+    CK_LAUNCH();
+    if (!append || s->n == 0) {
+        if (bbg_status r = upload_common(s, dp, dv, count)) return r;
+    } else {
+        // ContinuousParticleSetBuilder3::AddParticle + Commit: the new particles follow the
+        // existing ones (ids n .. n + count - 1); the next substep re-sorts them
+        launch_append(s->B, s->state, s->pid_cur, dp, dv, s->n, count, s->stream);
+        CK_LAUNCH();
+        if (s->mlp_alloc)
+            CK(cudaMemsetAsync(s->mlp.divsum + s->n, 0, sizeof(float) * (size_t)count, s->stream));
+        s->n += count;
+        s->P.n = s->n;
+        s->grid_valid = false;
+        s->valid &= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_DENSITY) |
+                    bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
+        s->epoch++;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
 }
 

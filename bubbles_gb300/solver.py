@@ -45,20 +45,26 @@ def desc_from_scene(scene, device=0):
     return d
 
 
+def fill_shape(dst, c):
+    """A bbg_shape from a shape dict ({"type": "box", "size", "center", "reverse"} or
+    {"type": "sphere", "radius", ...})."""
+    dst.type = N.SHAPE_BOX if c["type"] == "box" else N.SHAPE_SPHERE
+    dst.reverse = 1 if c.get("reverse", False) else 0
+    for k in range(3):
+        dst.center[k] = float(c.get("center", (0.0, 0.0, 0.0))[k])
+    if c["type"] == "box":
+        for k in range(3):
+            dst.size[k] = float(c["size"][k])
+    else:
+        dst.size[0] = float(c["radius"])
+    dst.friction = float(c.get("friction", 0.0))
+
+
 def shapes_from_scene(scene):
     cols = scene.get("colliders", [])
     arr = (N.Shape * max(1, len(cols)))()
     for i, c in enumerate(cols):
-        arr[i].type = N.SHAPE_BOX if c["type"] == "box" else N.SHAPE_SPHERE
-        arr[i].reverse = 1 if c.get("reverse", False) else 0
-        for k in range(3):
-            arr[i].center[k] = float(c.get("center", (0.0, 0.0, 0.0))[k])
-        if c["type"] == "box":
-            for k in range(3):
-                arr[i].size[k] = float(c["size"][k])
-        else:
-            arr[i].size[0] = float(c["radius"])
-        arr[i].friction = float(c.get("friction", 0.0))
+        fill_shape(arr[i], c)
     return arr, len(cols)
 
 
@@ -119,6 +125,30 @@ class Solver:
 
     def setup(self):
         N.call("bbg_setup", self.h)
+
+    def emit_volume(self, shape, spacing, jitter=0.0, velocity=(0.0, 0.0, 0.0), max_particles=None,
+                    bounds=None, append=False):
+        """VolumeParticleEmitter3 of a box or sphere shape dict on the device (the jitter uses
+        the C library's rand(), seeded by the caller); returns how many particles were
+        emitted.  append=False replaces the particles, True adds them after the existing."""
+        e = N.EmitterDesc()
+        N.call("bbg_emitter_desc_default", ctypes.byref(e))
+        fill_shape(e.shape, shape)
+        if bounds is not None:
+            e.use_bounds = 1
+            for k in range(3):
+                e.bounds_min[k] = float(bounds[0][k])
+                e.bounds_max[k] = float(bounds[1][k])
+        e.spacing = float(spacing)
+        e.jitter = float(jitter)
+        for k in range(3):
+            e.initial_velocity[k] = float(velocity[k])
+        if max_particles is not None:
+            e.max_particles = int(max_particles)
+        out = ctypes.c_int()
+        N.call("bbg_emit_volume", self.h, ctypes.byref(e), int(bool(append)), ctypes.byref(out))
+        self.n = self.particle_count()
+        return out.value
 
     def particle_count(self):
         n = ctypes.c_int()
@@ -281,15 +311,20 @@ class Solver:
         return out, total.value
 
     # --- particle frames (reference text format) ------------------------------------
-    def frame_text(self, flags=N.FRAME_POSITION):
-        """The SerializerSaveSphDataSet3 block of the current state, as bytes."""
+    def frame_text(self, flags=N.FRAME_POSITION, out=None):
+        """The SerializerSaveSphDataSet3 block of the current state, as bytes; with `out`
+        (a writable buffer such as a bytearray) it is written there and its length returned."""
         need = ctypes.c_size_t()
+        if out is not None:
+            buf = np.frombuffer(out, dtype=np.uint8)
+            N.call("bbg_frame_text", self.h, int(flags), buf.ctypes.data, buf.nbytes, ctypes.byref(need))
+            return need.value
         st = N.load().bbg_frame_text(self.h, int(flags), None, 0, ctypes.byref(need))
         if st not in (N.OK, 4):   # 4: capacity (size query)
             N.call("bbg_frame_text", self.h, int(flags), None, 0, ctypes.byref(need))
-        buf = ctypes.create_string_buffer(need.value)
-        N.call("bbg_frame_text", self.h, int(flags), buf, need.value, ctypes.byref(need))
-        return buf.raw[:need.value]
+        buf = np.empty(need.value, np.uint8)
+        N.call("bbg_frame_text", self.h, int(flags), buf.ctypes.data, buf.nbytes, ctypes.byref(need))
+        return buf.tobytes()
 
     def frame_append(self, path, flags=N.FRAME_POSITION):
         N.call("bbg_frame_append", self.h, int(flags), str(path).encode())

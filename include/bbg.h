@@ -276,6 +276,33 @@ bbg_status bbg_checkpoint_load(bbg_solver s, const char *path);
 bbg_status bbg_checkpoint_write(bbg_solver s, void *buf, size_t capacity, size_t *length);
 bbg_status bbg_checkpoint_read(bbg_solver s, const void *buf, size_t length);
 
+/* ----- particle seeding (VolumeParticleEmitter3) --------------------------------- */
+/* VolumeParticleEmitter3 (src/core/emitter.h:39-69, emitter.cpp:241-330) with a box or
+ * sphere shape, one-shot, the zero velocity field: the BCC lattice of
+ * BccLatticePointGenerator::ForEach (src/generator/bcclattice.cpp:6-36) over the shape's
+ * bounds (or the given ones), each point moved by 0.5 * jitter * spacing *
+ * SampleSphere(rand_float(), rand_float()), kept when Shape::SignedDistance <= 0, at most
+ * max_particles, velocity = initial_velocity.  The lattice and the inside test run on the
+ * device, one thread per lattice point, in the reference's float operations; the jitter
+ * offsets are the C library's rand() sequence (seed it with srand as for the reference),
+ * two values per lattice point like the reference's loop.  When max_particles stops the
+ * reference's loop early it draws fewer values than this call (the emitted particles are
+ * the same). */
+typedef struct {
+    bbg_shape shape;                 /* box or sphere (friction unused) */
+    int use_bounds;                  /* 1: the lattice spans [bounds_min, bounds_max] */
+    double bounds_min[3], bounds_max[3];
+    double spacing;
+    double jitter;                   /* 0: the exact lattice */
+    double initial_velocity[3];
+    int max_particles;               /* IntInfinity (2^31 - 1) by default */
+} bbg_emitter_desc;
+bbg_status bbg_emitter_desc_default(bbg_emitter_desc *desc);
+/* append = 0: the emitted particles replace the solver's (a ParticleSetBuilder3 filled by
+ * Emit, then MakeParticleSet and upload); append = 1: they follow the existing particles
+ * (ContinuousParticleSetBuilder3::AddParticle and Commit), ids n .. n + emitted - 1. */
+bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *desc, int append, int *emitted);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

@@ -114,6 +114,8 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_emit_volume": (ctypes.c_long, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, ctypes.c_double,
+                                            ctypes.c_double, _D, ctypes.c_long, _D, _D, ctypes.c_long]),
         "orc_frame_parse": (ctypes.c_long, [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int), _D, _D, _D, _I32, ctypes.c_long]),
         "orc_frame_text": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_double,
@@ -373,4 +375,28 @@ def frame_parse(text, flags=0, variant="f32"):
     if n < 0:
         raise ValueError("no complete fluid section")
     return fl.value, cnt.value, pos[:n], vel[:n], rho[:n], bnd[:n]
+
+
+def emit_volume(shape, spacing, jitter=0.0, velocity=(0.0, 0.0, 0.0), max_particles=2**31 - 1, bounds=None,
+                variant="f32", capacity=None):
+    """VolumeParticleEmitter3::Emit restated (the caller seeds the C library's rand()):
+    (positions, velocities) of the particles emitted in a box or sphere shape dict."""
+    lib = load(variant)
+    sh = Shape()
+    box = shape["type"] == "box"
+    sh.type = SHAPE_BOX if box else SHAPE_SPHERE
+    sh.reverse = int(bool(shape.get("reverse", False)))
+    for k in range(3):
+        sh.center[k] = shape.get("center", (0.0, 0.0, 0.0))[k]
+        sh.size[k] = shape["size"][k] if box else (shape["radius"] if k == 0 else 0.0)
+    bmin = np.array(bounds[0] if bounds else (0, 0, 0), np.float64)
+    bmax = np.array(bounds[1] if bounds else (0, 0, 0), np.float64)
+    v = np.array(velocity, np.float64)
+    if capacity is None:
+        capacity = 1 << 22
+    pos = np.zeros((capacity, 3))
+    vel = np.zeros((capacity, 3))
+    n = lib.orc_emit_volume(ctypes.byref(sh), int(bounds is not None), _ptr(bmin), _ptr(bmax), float(spacing),
+                            float(jitter), _ptr(v), int(max_particles), _ptr(pos), _ptr(vel), capacity)
+    return pos[:min(n, capacity)], vel[:min(n, capacity)]
 

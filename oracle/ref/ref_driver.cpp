@@ -5,6 +5,7 @@
  * golden fixtures under tests/golden/.  Parameters use the oracle's orc_params layout.
  */
 #include <collider.h>
+#include <emitter.h>
 #include <cutil.h>
 #include <interaction.h>
 #include <pcisph_solver.h>
@@ -220,6 +221,35 @@ void ref_get_buckets(RefSim *s, int32_t *counts, int32_t *ids) {
         counts[i] = b->Count();
         for (int q = 0; q < 100; q++) ids[100 * i + q] = q < b->Count() ? b->Get(q) : -1;
     }
+}
+
+/* VolumeParticleEmitter3::Emit (src/core/emitter.cpp:241-330) of a box or sphere
+ * (MakeBox / MakeSphere with a translation) into a ParticleSetBuilder3 after srand(seed):
+ * the lattice spans the shape's bounds, or [bmin, bmax] when use_bounds.  Returns the
+ * number emitted (at most `capacity` stored). */
+int ref_emit_volume(int type, int reverse, const double *center, const double *size, int use_bounds,
+                    const double *bmin, const double *bmax, double spacing, double jitter, const double *vel,
+                    int max_particles, unsigned seed, double *pos, double *vel_out, int capacity) {
+    Transform t = Translate(V3(center));
+    Shape *shape = type == 1 ? MakeBox(t, V3(size), reverse != 0) : MakeSphere(t, (Float)size[0], reverse != 0);
+    ParticleSetBuilder3 builder;
+    VolumeParticleEmitter3 *em;
+    if (use_bounds)
+        em = new VolumeParticleEmitter3(shape, Bounds3f(V3(bmin), V3(bmax)), (Float)spacing, V3(vel), vec3f(0), 0,
+                                        max_particles, (Float)jitter);
+    else
+        em = new VolumeParticleEmitter3(shape, (Float)spacing, V3(vel), vec3f(0), 0, max_particles, (Float)jitter);
+    srand(seed);
+    em->Emit(&builder);
+    const int n = (int)builder.positions.size();
+    for (int i = 0; i < n && i < capacity; i++) {
+        for (int k = 0; k < 3; k++) {
+            pos[3 * i + k] = (double)builder.positions[(size_t)i][k];
+            vel_out[3 * i + k] = (double)builder.velocities[(size_t)i][k];
+        }
+    }
+    delete em;
+    return n;
 }
 
 /* SerializerLoadParticles3 on a frame file: the first fluid section's particles (at most

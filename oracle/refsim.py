@@ -71,6 +71,8 @@ def load(variant):
         "ref_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "ref_get_buckets": (None, [_P, _I32, _I32]),
         "ref_save_frame": (None, [_P, ctypes.c_char_p, ctypes.c_int]),
+        "ref_emit_volume": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _D, _D, ctypes.c_int, _D, _D, ctypes.c_double,
+                                           ctypes.c_double, _D, ctypes.c_int, ctypes.c_uint, _D, _D, ctypes.c_int]),
         "ref_load_frame": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _D, _D, _D, _I32,
                                           ctypes.c_int]),
     }
@@ -168,4 +170,25 @@ def load_frame(text, flags=0, variant="f32", capacity=None):
                                rho.ctypes.data_as(_D), bnd.ctypes.data_as(_I32), cap)
     n = min(n, cap)
     return fl.value, pos[:n], vel[:n], rho[:n], bnd[:n]
+
+
+def emit_volume(shape, spacing, jitter=0.0, velocity=(0.0, 0.0, 0.0), max_particles=2**31 - 1, seed=1,
+                bounds=None, variant="f32", capacity=4 << 20):
+    """VolumeParticleEmitter3 of the reference (box or sphere shape dict as in scenes) after
+    srand(seed): (positions, velocities) of the emitted particles."""
+    lib = load(variant)
+    box = shape["type"] == "box"
+    center = np.array(shape.get("center", (0.0, 0.0, 0.0)), np.float64)
+    size = np.array(shape["size"] if box else (shape["radius"], 0.0, 0.0), np.float64)
+    bmin = np.array(bounds[0] if bounds else (0, 0, 0), np.float64)
+    bmax = np.array(bounds[1] if bounds else (0, 0, 0), np.float64)
+    v = np.array(velocity, np.float64)
+    pos = np.zeros((capacity, 3))
+    vel = np.zeros((capacity, 3))
+    n = lib.ref_emit_volume(1 if box else 2, int(bool(shape.get("reverse", False))), center.ctypes.data_as(_D),
+                            size.ctypes.data_as(_D), int(bounds is not None), bmin.ctypes.data_as(_D),
+                            bmax.ctypes.data_as(_D), float(spacing), float(jitter), v.ctypes.data_as(_D),
+                            int(max_particles), int(seed), pos.ctypes.data_as(_D), vel.ctypes.data_as(_D),
+                            capacity)
+    return pos[:min(n, capacity)], vel[:min(n, capacity)]
 

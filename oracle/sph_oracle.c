@@ -1575,3 +1575,83 @@ long orc_frame_parse(const char *text, size_t length, int *flags, int *count, do
     }
     return ended ? size : -2;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* Volume emission (src/core/emitter.cpp:8-12, 241-330; bcclattice.cpp:6-36)           */
+/* ------------------------------------------------------------------------------------ */
+/* rand_float (src/core/geometry.h:1900-1902): a float quotient in both builds */
+static Float emit_rand_float(void) { return (Float)((float)rand() / ((float)RAND_MAX + 1.f)); }
+/* std::sqrt / std::cos / std::sin of a Float: the float functions in the FP32 build */
+#define FSQRT(x) _Generic((x), float: sqrtf, default: sqrt)(x)
+#define FCOS(x) _Generic((x), float: cosf, default: cos)(x)
+#define FSIN(x) _Generic((x), float: sinf, default: sin)(x)
+
+long orc_emit_volume(const orc_shape *shape, int use_bounds, const double bmin[3], const double bmax[3],
+                     double spacing, double jitter, const double vel[3], long max_particles, double *pos,
+                     double *vel_out, long capacity) {
+    oshape s;
+    s.type = shape->type;
+    s.reverse = shape->reverse ? 1 : 0;
+    s.t = V((Float)shape->center[0], (Float)shape->center[1], (Float)shape->center[2]);
+    s.sx = (Float)shape->size[0]; s.sy = (Float)shape->size[1]; s.sz = (Float)shape->size[2];
+    s.radius = (Float)shape->size[0];
+    s.friction = (Float)shape->friction;
+    v3 lo, hi;
+    if (use_bounds) {
+        for (int k = 0; k < 3; k++) {
+            Float a = (Float)bmin[k], b = (Float)bmax[k];
+            ((Float *)&lo)[k] = a < b ? a : b;
+            ((Float *)&hi)[k] = a > b ? a : b;
+        }
+    } else {
+        /* ObjectToWorld of the object bounds (box.cpp:59-64, sphere.cpp:43-45): a translation */
+        Float hx, hy, hz;
+        if (s.type == ORC_SHAPE_BOX) {
+            hx = s.sx / 2.0; hy = s.sy / 2.0; hz = s.sz / 2.0;
+        } else {
+            hx = hy = hz = s.radius;
+        }
+        lo = V(-hx + s.t.x, -hy + s.t.y, -hz + s.t.z);
+        hi = V(hx + s.t.x, hy + s.t.y, hz + s.t.z);
+    }
+    const Float sp = (Float)spacing;
+    const Float half = sp / 2;
+    const Float width = hi.x - lo.x, height = hi.y - lo.y, depth = hi.z - lo.z;
+    const Float max_jitter = (Float)(0.5 * (double)(Float)jitter * (double)sp);
+    const v3 v0 = V((Float)0 + (Float)vel[0], (Float)0 + (Float)vel[1], (Float)0 + (Float)vel[2]);
+    long emitted = 0;
+    int has_off = 0, stop = 0;
+    for (int k = 0; (Float)k * half <= depth && !stop; k++) {
+        const Float pz = (Float)k * half + lo.z;
+        const Float off = has_off ? half : 0;
+        for (int j = 0; (Float)j * sp + off <= height && !stop; j++) {
+            const Float py = (Float)j * sp + off + lo.y;
+            for (int i = 0; (Float)i * sp + off <= width && !stop; i++) {
+                const Float px = (Float)i * sp + off + lo.x;
+                /* vec2f u(rand_float(), rand_float()): the second call lands in u[0] */
+                const Float u1 = emit_rand_float();
+                const Float u0 = emit_rand_float();
+                const Float usqrt = 2 * FSQRT(u1 * (1 - u1));
+                const Float utheta = (Float)(2 * 3.14159265358979323846 * (double)u0);
+                const v3 dir = V(FCOS(utheta) * usqrt, FSIN(utheta) * usqrt, 1 - 2 * u1);
+                const v3 target = vadd(V(px, py, pz), vmul(dir, max_jitter));
+                const Float d = shape_closest_distance(&s, target);
+                const Float sd = shape_is_inside(&s, target) ? -absf_(d) : absf_(d);
+                if (sd <= 0) {
+                    if (emitted < max_particles) {
+                        if (emitted < capacity) {
+                            pos[3 * emitted] = target.x; pos[3 * emitted + 1] = target.y; pos[3 * emitted + 2] = target.z;
+                            vel_out[3 * emitted] = v0.x; vel_out[3 * emitted + 1] = v0.y;
+                            vel_out[3 * emitted + 2] = v0.z;
+                        }
+                        emitted++;
+                    } else {
+                        stop = 1;
+                    }
+                }
+            }
+        }
+        has_off = !has_off;
+    }
+    return emitted;
+}

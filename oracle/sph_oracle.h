@@ -169,6 +169,17 @@ int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
 size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
                         double mass, double spacing, char *buf, size_t capacity);
 
+/* VolumeParticleEmitter3::Emit into a ParticleSetBuilder3 (src/core/emitter.cpp:8-12,
+ * 241-330) for a box or sphere: the BCC lattice of BccLatticePointGenerator::ForEach
+ * (src/generator/bcclattice.cpp:6-36) over the shape's bounds (or [bmin, bmax] when
+ * use_bounds), each point moved by max_jitter * SampleSphere(rand(), rand()), kept when
+ * Shape::SignedDistance <= 0, up to max_particles.  Two rand() values per visited lattice
+ * point, as the reference; velocities = initial velocity.  Returns the count (at most
+ * `capacity` stored). */
+long     orc_emit_volume(const orc_shape *shape, int use_bounds, const double bmin[3], const double bmax[3],
+                         double spacing, double jitter, const double vel[3], long max_particles, double *pos,
+                         double *vel_out, long capacity);
+
 /* SerializerLoadParticles3 (src/third/serializer.cpp:540-560): the first fluid section of a
  * frame text -- header tokens (SerializerFindFluidSection / SerializerFluidProcessToken,
  * :83-181), then one particle per data line up to the first non-comment line holding

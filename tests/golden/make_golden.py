@@ -20,8 +20,13 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   CR and CRLF ends, tabs, malformed and out-of-range numbers) with what the
                   reference reads from it.
 
+  emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
+                  srand(seed) for boxes and spheres, with and without jitter, explicit
+                  bounds, a reversed box and a binding max_particles (EMIT_CASES).
+
     python tests/golden/make_golden.py           # every fixture
     python tests/golden/make_golden.py frames    # frame_f32.npz only
+    python tests/golden/make_golden.py emit      # emit_f32.npz only
 """
 import json
 import os
@@ -146,11 +151,37 @@ def make_frames():
     np.savez_compressed(os.path.join(HERE, "frame_f32.npz"), **out)
 
 
+# emitter cases: shape, spacing, jitter, initial velocity, max particles, bounds, srand seed
+EMIT_CASES = [
+    ({"type": "sphere", "radius": 0.1, "center": (0.01, 0.02, 0.03)}, 0.02, 0.0, (0.0, 0.0, 0.0), None, None, 1),
+    ({"type": "box", "size": (0.2, 0.1, 0.3), "center": (0.0, 0.0, 0.0)}, 0.02, 0.5, (1.0, 0.0, -0.5), None, None,
+     7),
+    ({"type": "sphere", "radius": 0.15, "center": (0.5, 0.4, 0.3)}, 0.013, 1.0, (0.0, 0.0, 0.0), None, None, 11),
+    ({"type": "box", "size": (0.4, 0.2, 0.3), "center": (0.1, 0.2, -0.3), "reverse": True}, 0.02, 0.3,
+     (0.0, 0.0, 0.0), None, ((-0.2, 0.0, -0.5), (0.3, 0.35, -0.1)), 3),
+    ({"type": "box", "size": (0.3, 0.3, 0.3), "center": (0.0, 0.0, 0.0)}, 0.015, 0.2, (0.0, 0.0, 0.0), 1000, None,
+     5),
+]
+
+
+def make_emit():
+    out = {"cases": np.array(json.dumps(EMIT_CASES))}
+    for i, (shape, sp, jit, vel, mx, bounds, seed) in enumerate(EMIT_CASES):
+        p, v = R.emit_volume(shape, sp, jitter=jit, velocity=vel, seed=seed, bounds=bounds,
+                             max_particles=mx if mx is not None else 2**31 - 1)
+        out["pos_%d" % i], out["vel_%d" % i] = p, v
+    np.savez_compressed(os.path.join(HERE, "emit_f32.npz"), **out)
+
+
 if __name__ == "__main__":
     if not R.available():
         sys.exit("the reference checkout is not available here; fixtures unchanged")
-    if sys.argv[1:] != ["frames"]:
+    what = sys.argv[1:]
+    if not what:
         for v in ("f32", "f64"):
             make(v)
-    make_frames()
+    if not what or what == ["frames"]:
+        make_frames()
+    if not what or what == ["emit"]:
+        make_emit()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
