@@ -2239,9 +2239,16 @@ bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *e, int append, 
         return fail(BBG_ERR_INVALID_ARGUMENT, "emitter needs spacing > 0, jitter >= 0, max_particles >= 0");
     if (append && s->n > 0 && s->nscenes > 0)
         return fail(BBG_ERR_STATE, "appending to a batch of scenes is not supported");
+    // the lattice's extent in spacings, before its loops are counted
+    for (int k = 0; k < 3; k++) {
+        const double lo = e->use_bounds ? e->bounds_min[k] : e->shape.center[k] - e->shape.size[0] - e->shape.size[k];
+        const double hi = e->use_bounds ? e->bounds_max[k] : e->shape.center[k] + e->shape.size[0] + e->shape.size[k];
+        if (!std::isfinite(lo) || !std::isfinite(hi) || !(std::fabs(hi - lo) / e->spacing < 4.0e6))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "the emitter's bounds are not finite or too many spacings wide");
+    }
     const Lattice L = emitter_lattice(*e);
-    if (L.total >= 0x7fffffffll)
-        return fail(BBG_ERR_CAPACITY, "the emitter's lattice has %lld points", L.total);
+    if (L.total > (1ll << 28))
+        return fail(BBG_ERR_CAPACITY, "the emitter's lattice has %lld points (at most 2^28)", L.total);
     const float sp = (float)e->spacing;
     const float max_jitter = (float)(0.5 * (double)(float)e->jitter * (double)sp);
     // the rand() sequence of the reference's loop: two values per lattice point, the
