@@ -187,6 +187,8 @@ SIGNATURES = {
                                ctypes.POINTER(ctypes.c_size_t)],
     "bbg_emitter_desc_default": [ctypes.POINTER(EmitterDesc)],
     "bbg_emit_volume": [_P, ctypes.POINTER(EmitterDesc), _I, _IP],
+    "bbg_map_grid": [_P, _IP],
+    "bbg_map_grid_emit": [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _IP],
     "bbg_checkpoint_save": [_P, ctypes.c_char_p],
     "bbg_checkpoint_load": [_P, ctypes.c_char_p],
     "bbg_checkpoint_write": [_P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],

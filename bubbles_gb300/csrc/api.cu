@@ -9,6 +9,7 @@
 #include "host_math.h"
 #include "mlp.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -111,6 +112,11 @@ struct bbg_solver_s {
     FrameBufs frame;             // particle-frame writer buffers (allocated on first use)
     FrameReadBufs fread;         // frame reader buffers (grown on use)
     EmitBufs emit;               // emitter buffers (grown on use)
+    MapBufs map;                 // MapGrid's remembered cells
+    BucketBufs bucket;           // cell lists of particles added since the last distribution
+    int grid_n = 0;              // particles in the last grid distribution's sorted ranges
+    bool members_ok = false;     // sorted ranges [0, grid_n) are the last distribution's cells
+    bool map_full = false;       // MapGridEmit reached the capacity once (it stops emitting)
 };
 
 namespace {
@@ -197,6 +203,16 @@ void free_frame(bbg_solver s) {
     for (void *p : eptrs)
         if (p) cudaFree(p);
     E = EmitBufs();
+    MapBufs &M = s->map;
+    void *mptrs[] = {M.pos, M.cell, M.rank, M.flag, M.flag_copy, M.index, M.part};
+    for (void *p : mptrs)
+        if (p) cudaFree(p);
+    M = MapBufs();
+    BucketBufs &K = s->bucket;
+    void *kptrs[] = {K.count, K.start, K.part, K.cell, K.sub, K.list};
+    for (void *p : kptrs)
+        if (p) cudaFree(p);
+    K = BucketBufs();
 }
 
 bbg_status free_all(bbg_solver s) {
@@ -340,6 +356,8 @@ bbg_status grid_update(bbg_solver s) {
     s->state = 1 - s->state;
     s->pid_cur = 1 - s->pid_cur;
     s->grid_valid = true;
+    s->grid_n = s->n;
+    s->members_ok = true;
     s->valid = kPosVel | bit(BBG_FIELD_INTERACTION);
     return BBG_OK;
 }
@@ -597,6 +615,8 @@ void after_substep(bbg_solver s, float dt) {
     (void)dt;
     s->pid_cur = 1 - s->pid_cur;
     s->grid_valid = true;
+    s->grid_n = s->n;
+    s->members_ok = true;
     s->valid = kPosVel | bit(BBG_FIELD_INTERACTION) | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE) |
                bit(BBG_FIELD_PRESSURE);
     if (s->desc.solver_kind == BBG_SOLVER_PCISPH)
@@ -950,6 +970,7 @@ static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d
     s->n = n;
     s->P.n = n;
     s->grid_valid = false;
+    s->members_ok = false;
     s->valid = kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) |
                bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
     return BBG_OK;
@@ -2228,6 +2249,23 @@ Lattice emitter_lattice(const bbg_emitter_desc &e) {
     return L;
 }
 
+// ContinuousParticleSetBuilder3::AddParticle + Commit (grid.h:1404-1437): `count` staged
+// particles (positions at stage, velocities at stage + 3 capacity) follow the existing ones
+// (ids n .. n + count - 1); the next substep's grid update sorts them in.
+bbg_status append_staged(bbg_solver s, int count) {
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    launch_append(s->B, s->state, s->pid_cur, dp, dv, s->n, count, s->stream);
+    CK_LAUNCH();
+    if (s->mlp_alloc) CK(cudaMemsetAsync(s->mlp.divsum + s->n, 0, sizeof(float) * (size_t)count, s->stream));
+    s->n += count;
+    s->P.n = s->n;
+    s->grid_valid = false;
+    s->valid &= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_DENSITY) |
+                bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
+    s->epoch++;
+    return BBG_OK;
+}
+
 }  // namespace
 
 bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *e, int append, int *emitted) {
@@ -2302,21 +2340,94 @@ bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *e, int append, 
     CK_LAUNCH();
     if (!append || s->n == 0) {
         if (bbg_status r = upload_common(s, dp, dv, count)) return r;
-    } else {
-        // ContinuousParticleSetBuilder3::AddParticle + Commit: the new particles follow the
-        // existing ones (ids n .. n + count - 1); the next substep re-sorts them
-        launch_append(s->B, s->state, s->pid_cur, dp, dv, s->n, count, s->stream);
-        CK_LAUNCH();
-        if (s->mlp_alloc)
-            CK(cudaMemsetAsync(s->mlp.divsum + s->n, 0, sizeof(float) * (size_t)count, s->stream));
-        s->n += count;
-        s->P.n = s->n;
-        s->grid_valid = false;
-        s->valid &= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_DENSITY) |
-                    bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
-        s->epoch++;
+    } else if (bbg_status r = append_staged(s, count)) {
+        return r;
     }
     CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// continuous emission: ContinuousParticleSetBuilder3::MapGrid / MapGridEmit
+// ----------------------------------------------------------------------------
+bbg_status bbg_map_grid(bbg_solver s, int *mapped) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    if (s->nscenes > 0) return fail(BBG_ERR_STATE, "continuous emission into a batch of scenes is not supported");
+    // the reference maps the cells of the grid's last distribution (its Setup distributes)
+    if (!s->grid_valid)
+        if (bbg_status r = grid_update(s)) return r;
+    MapBufs &M = s->map;
+    if (M.cap < s->n + 1) {
+        const size_t need = (size_t)s->n + 1;
+        M.cap = 0;
+        bbg_status r = reserve(&M.pos, need);
+        if (!r) r = reserve(&M.cell, need);
+        if (!r) r = reserve(&M.rank, need);
+        if (!r) r = reserve(&M.flag, need);
+        if (!r) r = reserve(&M.flag_copy, need);
+        if (!r) r = reserve(&M.index, need);
+        if (!r) r = reserve(&M.part, scan_partials_needed((unsigned)need));
+        if (r) return r;
+        M.cap = (int)need;
+    }
+    launch_map(s->n, s->B.pos[s->state], s->B.cell, s->B.start, M, s->stream);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->stream));
+    s->map_full = false;
+    if (mapped) *mapped = M.count;
+    return BBG_OK;
+}
+
+bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocity[3], int *emitted) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!velocity) return fail(BBG_ERR_INVALID_ARGUMENT, "null velocity");
+    MapBufs &M = s->map;
+    if (M.count <= 0) return fail(BBG_ERR_STATE, "bbg_map_grid has not been called");
+    if (emitted) *emitted = 0;
+    if (s->map_full) return BBG_OK;   // the reference's builder stops once it hit its capacity
+    // the cells' particles now: the last distribution's sorted ranges plus the particles
+    // added since (their cells as Commit's DistributeByParticleList would give them)
+    const bool sorted = s->members_ok;
+    const int first = sorted ? s->grid_n : 0;
+    const bool bucketed = s->n > first;
+    BucketBufs &K = s->bucket;
+    if (bucketed) {
+        const size_t cells = s->P.g.total, m = (size_t)(s->n - first);
+        if (K.cells != cells || K.cap < m) {
+            K.cells = 0;
+            K.cap = 0;
+            const size_t mm = std::max(m, (size_t)s->capacity);
+            bbg_status r = reserve(&K.count, cells + 1);
+            if (!r) r = reserve(&K.start, cells + 1);
+            if (!r) r = reserve(&K.part, scan_partials_needed((unsigned)(cells + 1)));
+            if (!r) r = reserve(&K.cell, mm);
+            if (!r) r = reserve(&K.sub, mm);
+            if (!r) r = reserve(&K.list, mm);
+            if (r) return r;
+            CK(cudaMemsetAsync(K.count, 0, sizeof(unsigned) * (cells + 1), s->stream));
+            K.cells = cells;
+            K.cap = mm;
+        }
+        launch_buckets(s->P, s->B.pos[s->state], first, s->n, K, s->stream);
+        CK_LAUNCH();
+    }
+    unsigned passed = 0;
+    CK(map_emit_test(M, sorted, s->B.start, bucketed, K, s->B.pos[s->state], (float)distance, &passed, s->h_u,
+                     s->stream));
+    CK_LAUNCH();
+    const unsigned room = (unsigned)(s->capacity - s->n);
+    const int count = (int)(passed < room ? passed : room);
+    if (passed > room) s->map_full = true;
+    if (count > 0) {
+        const float3 v = make_float3((float)velocity[0], (float)velocity[1], (float)velocity[2]);
+        launch_map_scatter(M, count, v, s->B.stage, s->B.stage + 3 * (size_t)s->capacity, s->stream);
+        CK_LAUNCH();
+        if (bbg_status r = append_staged(s, count)) return r;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    if (emitted) *emitted = count;
     return BBG_OK;
 }
 

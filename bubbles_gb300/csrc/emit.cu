@@ -111,4 +111,117 @@ void launch_append(DevBufs &B, int state, int pid_cur, const float *pos, const f
                                                 B.slot, B.force, B.pforce, B.rho, B.press);
 }
 
+// ----------------------------------------------------------------------------
+// continuous emission: MapGrid / MapGridEmit (src/core/grid.h:1289-1402)
+// ----------------------------------------------------------------------------
+__global__ void k_map(int n, const float4 *__restrict__ pos, const unsigned *__restrict__ cell,
+                      const unsigned *__restrict__ start, float4 *__restrict__ mpos, unsigned *__restrict__ mcell,
+                      uint2 *__restrict__ mrank) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const unsigned c = cell[q];
+    mpos[q] = pos[q];
+    mcell[q] = c;
+    mrank[q] = make_uint2((unsigned)q - start[c], start[c + 1] - start[c]);
+}
+
+__global__ void k_bucket_count(Params P, const float4 *__restrict__ pos, int first, int n,
+                               unsigned *__restrict__ cellof, unsigned *__restrict__ sub,
+                               unsigned *__restrict__ count) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (first + k >= n) return;
+    unsigned bad = 0;
+    const unsigned c = grid_hash(P.g, pos[first + k], P.iz, &bad);
+    cellof[k] = c;
+    sub[k] = atomicAdd(&count[c], 1u);
+}
+
+__global__ void k_bucket_place(int first, int n, const unsigned *__restrict__ cellof,
+                               const unsigned *__restrict__ sub, const unsigned *__restrict__ start,
+                               unsigned *__restrict__ list) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (first + k >= n) return;
+    list[start[cellof[k]] + sub[k]] = (unsigned)(first + k);
+}
+
+// Distance(pj, pi) < d (geometry.h:798-800): sqrt of x*x + y*y + z*z, unfused
+__device__ __forceinline__ bool closer_than(float4 a, float4 b, float d) {
+    const float x = __fsub_rn(a.x, b.x), y = __fsub_rn(a.y, b.y), z = __fsub_rn(a.z, b.z);
+    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+    return __fsqrt_rn(l2) < d;
+}
+
+// One mapped position: skipped when its cell holds kMaxPerCell particles or more, or when
+// it is past the first (kMaxPerCell - size) positions of its cell, or when a particle of the
+// cell is closer than d.
+__global__ void k_map_emit(int count, const float4 *__restrict__ mpos, const unsigned *__restrict__ mcell,
+                           const uint2 *__restrict__ mrank, bool sorted, const unsigned *__restrict__ start,
+                           bool bucketed, const unsigned *__restrict__ bstart, const unsigned *__restrict__ blist,
+                           const float4 *__restrict__ pos, float d, unsigned *__restrict__ flag) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const unsigned c = mcell[q];
+    const uint2 r = mrank[q];
+    const unsigned a0 = sorted ? start[c] : 0u, a1 = sorted ? start[c + 1] : 0u;
+    const unsigned b0 = bucketed ? bstart[c] : 0u, b1 = bucketed ? bstart[c + 1] : 0u;
+    const unsigned size = (a1 - a0) + (b1 - b0);
+    bool ok = size < (unsigned)kMaxPerCell;
+    if (ok) {
+        const unsigned room = (unsigned)kMaxPerCell - size;
+        ok = r.x < (room < r.y ? room : r.y);
+    }
+    if (ok) {
+        const float4 p = mpos[q];
+        for (unsigned j = a0; j < a1 && ok; j++) ok = !closer_than(pos[j], p, d);
+        for (unsigned j = b0; j < b1 && ok; j++) ok = !closer_than(pos[blist[j]], p, d);
+    }
+    flag[q] = ok ? 1u : 0u;
+}
+
+__global__ void k_map_scatter(int count, int n, const unsigned *__restrict__ flag, const unsigned *__restrict__ index,
+                              const float4 *__restrict__ mpos, float3 v, float *__restrict__ pos,
+                              float *__restrict__ vel) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count || !flag[q]) return;
+    const unsigned k = index[q];
+    if ((int)k >= n) return;
+    const float4 p = mpos[q];
+    pos[3 * (size_t)k] = p.x;
+    pos[3 * (size_t)k + 1] = p.y;
+    pos[3 * (size_t)k + 2] = p.z;
+    vel[3 * (size_t)k] = v.x;
+    vel[3 * (size_t)k + 1] = v.y;
+    vel[3 * (size_t)k + 2] = v.z;
+}
+
+void launch_map(int n, const float4 *pos, const unsigned *cell, const unsigned *start, MapBufs &M,
+                cudaStream_t s) {
+    k_map<<<blocks_for(n, 256), 256, 0, s>>>(n, pos, cell, start, M.pos, M.cell, M.rank);
+    M.count = n;
+}
+
+void launch_buckets(const Params &P, const float4 *pos, int first, int n, BucketBufs &K, cudaStream_t s) {
+    const int m = n - first;
+    if (m > 0) k_bucket_count<<<blocks_for(m, 256), 256, 0, s>>>(P, pos, first, n, K.cell, K.sub, K.count);
+    launch_cell_scan(K.count, (unsigned)K.cells, K.part, K.start, s);   // leaves count zeroed
+    if (m > 0) k_bucket_place<<<blocks_for(m, 256), 256, 0, s>>>(first, n, K.cell, K.sub, K.start, K.list);
+}
+
+cudaError_t map_emit_test(const MapBufs &M, bool sorted, const unsigned *start, bool bucketed,
+                          const BucketBufs &K, const float4 *pos, float d, unsigned *passed,
+                          unsigned *h_scratch, cudaStream_t s) {
+    k_map_emit<<<blocks_for(M.count, 128), 128, 0, s>>>(M.count, M.pos, M.cell, M.rank, sorted, start, bucketed,
+                                                        K.start, K.list, pos, d, M.flag);
+    cudaMemcpyAsync(M.flag_copy, M.flag, sizeof(unsigned) * (size_t)M.count, cudaMemcpyDeviceToDevice, s);
+    launch_cell_scan(M.flag_copy, (unsigned)M.count, M.part, M.index, s);
+    cudaMemcpyAsync(h_scratch, M.index + M.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    *passed = *h_scratch;
+    return e;
+}
+
+void launch_map_scatter(const MapBufs &M, int n, float3 v, float *pos, float *vel, cudaStream_t s) {
+    k_map_scatter<<<blocks_for(M.count, 256), 256, 0, s>>>(M.count, n, M.flag, M.index, M.pos, v, pos, vel);
+}
+
 }  // namespace bbg

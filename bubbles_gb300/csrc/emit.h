@@ -37,4 +37,38 @@ void launch_emit_scatter(const Lattice &L, int n, const EmitBufs &E, float3 v, f
 void launch_append(DevBufs &B, int state, int pid_cur, const float *pos, const float *vel, int first, int n,
                    cudaStream_t s);
 
+// ---- continuous emission (ContinuousParticleSetBuilder3, src/core/grid.h:1246-1450) ----
+constexpr int kMaxPerCell = 100;   // MaximumParticlesPerBucket (src/core/particle.h:10)
+
+// MapGrid: the particles of every occupied cell, positions in chain (sorted) order.
+struct MapBufs {
+    int count = 0, cap = 0;
+    float4 *pos = nullptr;       // mapped positions
+    unsigned *cell = nullptr;    // their cells
+    uint2 *rank = nullptr;       // (index within the cell, the cell's mapped count)
+    unsigned *flag = nullptr, *flag_copy = nullptr, *index = nullptr, *part = nullptr;
+};
+
+// Cell lists of the particles in sorted slots [first, n) (those not in the last grid
+// distribution's ranges): count, start (cells + 1), list of slots grouped by cell.
+struct BucketBufs {
+    size_t cells = 0, cap = 0;
+    unsigned *count = nullptr, *start = nullptr, *part = nullptr;
+    unsigned *cell = nullptr, *sub = nullptr, *list = nullptr;
+};
+
+// MapGrid from the last grid distribution: n sorted slots with their cells and cell starts.
+void launch_map(int n, const float4 *pos, const unsigned *cell, const unsigned *start, MapBufs &M,
+                cudaStream_t s);
+// Cell lists of slots [first, n) of pos.
+void launch_buckets(const Params &P, const float4 *pos, int first, int n, BucketBufs &K, cudaStream_t s);
+// MapGridEmit's test of each mapped position against the particles of its cell now (the
+// sorted ranges of the last distribution when `sorted`, plus the bucketed slots when
+// `bucketed`); returns how many pass (synchronises).
+cudaError_t map_emit_test(const MapBufs &M, bool sorted, const unsigned *start, bool bucketed,
+                          const BucketBufs &K, const float4 *pos, float d, unsigned *passed,
+                          unsigned *h_scratch, cudaStream_t s);
+// The first n passing positions, in map order, to pos (xyz); vel = v.
+void launch_map_scatter(const MapBufs &M, int n, float3 v, float *pos, float *vel, cudaStream_t s);
+
 }  // namespace bbg

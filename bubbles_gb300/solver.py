@@ -150,6 +150,21 @@ class Solver:
         self.n = self.particle_count()
         return out.value
 
+    def map_grid(self):
+        """ContinuousParticleSetBuilder3::MapGrid: remember the occupied cells' positions."""
+        out = ctypes.c_int()
+        N.call("bbg_map_grid", self.h, ctypes.byref(out))
+        return out.value
+
+    def map_grid_emit(self, distance, velocity=(0.0, 0.0, 0.0)):
+        """ContinuousParticleSetBuilder3::MapGridEmit: refill the mapped cells; returns how
+        many particles were added."""
+        v = (ctypes.c_double * 3)(*[float(x) for x in velocity])
+        out = ctypes.c_int()
+        N.call("bbg_map_grid_emit", self.h, float(distance), v, ctypes.byref(out))
+        self.n = self.particle_count()
+        return out.value
+
     def particle_count(self):
         n = ctypes.c_int()
         N.call("bbg_particle_count", self.h, ctypes.byref(n))

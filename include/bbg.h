@@ -303,6 +303,21 @@ bbg_status bbg_emitter_desc_default(bbg_emitter_desc *desc);
  * (ContinuousParticleSetBuilder3::AddParticle and Commit), ids n .. n + emitted - 1. */
 bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *desc, int append, int *emitted);
 
+/* Continuous emission (ContinuousParticleSetBuilder3, src/core/grid.h:1246-1450).
+ * bbg_map_grid = MapGrid (:1289-1321): remembers, for every occupied cell of the grid's last
+ * distribution (one is made first when the particles were uploaded since), its particles'
+ * positions in chain order; *mapped = how many.  bbg_map_grid_emit = MapGridEmit
+ * (:1359-1402) with a constant velocity field: in every mapped cell holding fewer than 100
+ * particles now (MaximumParticlesPerBucket), each of the first (100 - held) remembered
+ * positions that no particle of the cell is closer to than `distance` becomes a new
+ * particle after the existing ones, cells in ascending order, positions in chain order.
+ * The cell's particles are those of the last distribution (at their current positions)
+ * plus the ones added since, as Commit's DistributeByParticleList places them.  At the
+ * capacity the call adds what fits and, like the reference's builder, later calls add
+ * nothing.  One thread per remembered position on the device. */
+bbg_status bbg_map_grid(bbg_solver s, int *mapped);
+bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocity[3], int *emitted);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

@@ -39,6 +39,7 @@ struct RefSim {
     SphParticleSet3 *sphSet = nullptr;
     ParticleSet3 *pSet = nullptr;
     Grid3 *grid = nullptr;
+    ContinuousParticleSetBuilder3 *cont = nullptr;   // ref_create_continuous only
 };
 
 static vec3f V3(const double *a) { return vec3f((Float)a[0], (Float)a[1], (Float)a[2]); }
@@ -47,17 +48,7 @@ extern "C" {
 
 int ref_float_bytes(void) { return (int)sizeof(Float); }
 
-RefSim *ref_create(const orc_params *p, int n, const double *pos, const double *vel, int kind) {
-    SetCPUThreads(1);
-    SetSystemUseCPU();
-    RefSim *s = new RefSim();
-    s->n = n;
-    s->kind = kind;
-    ParticleSetBuilder3 builder;
-    for (int i = 0; i < n; i++) {
-        vec3f v = vel ? V3(&vel[3 * i]) : vec3f(0);
-        builder.AddParticle(V3(&pos[3 * i]), v);
-    }
+static RefSim *finish_sim(RefSim *s, const orc_params *p, SphParticleSet3 *set, int kind) {
     SphSolverData3 *data = DefaultSphSolverData3(false);
     data->eosExponent = p->eos_exponent;
     data->negativePressureScale = p->negative_pressure_scale;
@@ -69,7 +60,7 @@ RefSim *ref_create(const orc_params *p, int n, const double *pos, const double *
     AddConstantInteraction(ib, V3(p->gravity));
     data->cInteractions = ib.MakeConstantInteractions(data->cInteractionsCount);
     s->data = data;
-    s->sphSet = SphParticleSet3FromBuilder(&builder);
+    s->sphSet = set;
     Bounds3f domain(V3(p->domain_min), V3(p->domain_max));
     s->grid = UtilBuildGridForDomain(domain, p->target_spacing, p->grid_spacing_scale);
     if (kind == 0) {
@@ -100,6 +91,51 @@ RefSim *ref_create(const orc_params *p, int n, const double *pos, const double *
         else s->sph.SetColliders(cs);
     }
     return s;
+}
+
+RefSim *ref_create(const orc_params *p, int n, const double *pos, const double *vel, int kind) {
+    SetCPUThreads(1);
+    SetSystemUseCPU();
+    RefSim *s = new RefSim();
+    s->n = n;
+    s->kind = kind;
+    ParticleSetBuilder3 builder;
+    for (int i = 0; i < n; i++) {
+        vec3f v = vel ? V3(&vel[3 * i]) : vec3f(0);
+        builder.AddParticle(V3(&pos[3 * i]), v);
+    }
+    return finish_sim(s, p, SphParticleSet3FromBuilder(&builder), kind);
+}
+
+/* The same scene on a ContinuousParticleSetBuilder3 of `capacity` particles (the builder's
+ * own particle set, so MapGrid / MapGridEmit can add to it). */
+RefSim *ref_create_continuous(const orc_params *p, int n, const double *pos, const double *vel, int kind,
+                              int capacity) {
+    SetCPUThreads(1);
+    SetSystemUseCPU();
+    RefSim *s = new RefSim();
+    s->n = n;
+    s->kind = kind;
+    s->cont = new ContinuousParticleSetBuilder3(capacity);
+    s->cont->SetKernelRadius((Float)(p->relative_kernel_radius * p->target_spacing));
+    for (int i = 0; i < n; i++) {
+        vec3f v = vel ? V3(&vel[3 * i]) : vec3f(0);
+        s->cont->AddParticle(V3(&pos[3 * i]), v);
+    }
+    s->cont->Commit();
+    return finish_sim(s, p, SphParticleSet3FromContinuousBuilder(s->cont), kind);
+}
+
+/* ContinuousParticleSetBuilder3::MapGrid on the simulation grid. */
+void ref_map_grid(RefSim *s) { s->cont->MapGrid(s->grid); }
+
+/* ContinuousParticleSetBuilder3::MapGridEmit with a constant velocity field; returns the
+ * particle count afterwards. */
+int ref_map_grid_emit(RefSim *s, double d, const double *vel) {
+    const vec3f v = V3(vel);
+    s->cont->MapGridEmit([v](const vec3f &) -> vec3f { return v; }, (Float)d);
+    s->n = s->pSet->GetParticleCount();
+    return s->n;
 }
 
 void ref_destroy(RefSim *s) { delete s; /* reference buffers live in its memory regions */ }

@@ -44,6 +44,10 @@ def load(variant):
     sig = {
         "ref_float_bytes": (ctypes.c_int, []),
         "ref_create": (_P, [ctypes.POINTER(O.Params), ctypes.c_int, _D, _D, ctypes.c_int]),
+        "ref_create_continuous": (_P, [ctypes.POINTER(O.Params), ctypes.c_int, _D, _D, ctypes.c_int,
+                                       ctypes.c_int]),
+        "ref_map_grid": (None, [_P]),
+        "ref_map_grid_emit": (ctypes.c_int, [_P, ctypes.c_double, _D]),
         "ref_destroy": (None, [_P]),
         "ref_scalars": (None, [_P, _D]),
         "ref_grid_info": (None, [_P, _I32, _D]),
@@ -87,7 +91,9 @@ def load(variant):
 class RefSim:
     """One scene built and stepped by the reference's own classes (single thread)."""
 
-    def __init__(self, scene, pos, vel=None, variant="f32", kind=None):
+    def __init__(self, scene, pos, vel=None, variant="f32", kind=None, continuous=None):
+        """continuous: capacity of a ContinuousParticleSetBuilder3 holding the particles
+        (MapGrid / MapGridEmit), else a ParticleSetBuilder3 builds the set."""
         self.lib = load(variant)
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         self.n = len(pos)
@@ -95,9 +101,17 @@ class RefSim:
         if kind is None:
             kind = 1 if scene.get("solver", "pcisph") == "sph" else 0
         self._params = O.make_params(scene)
-        self.h = self.lib.ref_create(ctypes.byref(self._params), self.n,
-                                     pos.ctypes.data_as(_D), v.ctypes.data_as(_D) if v is not None else None,
-                                     kind)
+        vp = v.ctypes.data_as(_D) if v is not None else None
+        if continuous:
+            self.h = self.lib.ref_create_continuous(ctypes.byref(self._params), self.n, pos.ctypes.data_as(_D),
+                                                    vp, kind, int(continuous))
+        else:
+            self.h = self.lib.ref_create(ctypes.byref(self._params), self.n, pos.ctypes.data_as(_D), vp, kind)
+
+    def map_grid_emit(self, d, velocity=(0.0, 0.0, 0.0)):
+        v = np.array(velocity, np.float64)
+        self.n = self.lib.ref_map_grid_emit(self.h, float(d), v.ctypes.data_as(_D))
+        return self.n
 
     def __getattr__(self, name):
         fn = getattr(self.lib, "ref_" + name)

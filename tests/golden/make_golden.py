@@ -20,6 +20,10 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   CR and CRLF ends, tabs, malformed and out-of-range numbers) with what the
                   reference reads from it.
 
+  continuous_f32.npz  ContinuousParticleSetBuilder3 on the 1,440-particle scene: MapGrid
+                  after Setup, positions moved by hand, then two MapGridEmit calls; the
+                  particle arrays after each, for a capacity that holds them and one that
+                  stops the first call (CONTINUOUS_CASES).
   emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
                   srand(seed) for boxes and spheres, with and without jitter, explicit
                   bounds, a reversed box and a binding max_particles (EMIT_CASES).
@@ -27,6 +31,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py           # every fixture
     python tests/golden/make_golden.py frames    # frame_f32.npz only
     python tests/golden/make_golden.py emit      # emit_f32.npz only
+    python tests/golden/make_golden.py continuous    # continuous_f32.npz only
 """
 import json
 import os
@@ -173,6 +178,32 @@ def make_emit():
     np.savez_compressed(os.path.join(HERE, "emit_f32.npz"), **out)
 
 
+# continuous emission cases: builder capacity, MapGridEmit distance, velocity
+CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
+
+
+def moved_positions(pos):
+    """The hand-moved positions of the continuous-emission fixture."""
+    rng = np.random.default_rng(1)
+    return pos + np.array([0.012, 0.0, 0.009]) + rng.normal(0.0, 0.002, pos.shape)
+
+
+def make_continuous():
+    sc, p0 = pcisph_scene()
+    p1 = moved_positions(p0)
+    out = {"scene": np.array(json.dumps(clean(sc))), "pos0": p0, "pos1": p1,
+           "cases": np.array(json.dumps(CONTINUOUS_CASES))}
+    for i, (cap, d, vel) in enumerate(CONTINUOUS_CASES):
+        r = R.RefSim(sc, p0, continuous=cap)
+        r.map_grid()
+        r.set(O.POSITION, p1)
+        for k in range(2):
+            r.map_grid_emit(d, vel)
+            out["pos_%d_%d" % (i, k)] = r.get(O.POSITION)
+            out["vel_%d_%d" % (i, k)] = r.get(O.VELOCITY)
+    np.savez_compressed(os.path.join(HERE, "continuous_f32.npz"), **out)
+
+
 if __name__ == "__main__":
     if not R.available():
         sys.exit("the reference checkout is not available here; fixtures unchanged")
@@ -184,4 +215,6 @@ if __name__ == "__main__":
         make_frames()
     if not what or what == ["emit"]:
         make_emit()
+    if not what or what == ["continuous"]:
+        make_continuous()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
