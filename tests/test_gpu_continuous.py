@@ -44,7 +44,7 @@ def map_emit_numpy(cell_of, counts, ids, p0, p1, dist, limit=100):
     """MapGridEmit restated: cells ascending, the first min(limit - held, remembered) chain
     positions of each cell with no current particle of the cell closer than dist."""
     chain = ids   # the cells' chains, concatenated in cell order
-    starts = np.concatenate([[0], np.cumsum(counts)])
+    starts = np.concatenate([[0], np.cumsum(counts.astype(np.int64))]).astype(np.int64)
     d32 = np.float32(dist)
     out = []
     for c in np.nonzero(counts)[0]:
