@@ -16,7 +16,7 @@ SOLVER_PCISPH, SOLVER_SPH = 0, 1
 PCISPH_AS_SHIPPED, PCISPH_TOLERANCE = 0, 1
 PRESSURE_INIT_ZERO, PRESSURE_INIT_PREVIOUS, PRESSURE_INIT_LEARNED = 0, 1, 2
 WARM_CLAMP_TOTAL, WARM_MONOTONE = 0, 1
-SHAPE_BOX, SHAPE_SPHERE = 1, 2
+SHAPE_BOX, SHAPE_SPHERE, SHAPE_SDF = 1, 2, 3
 MAX_COLLIDERS = 16
 
 FIELD_POSITION, FIELD_VELOCITY, FIELD_FORCE, FIELD_INTERACTION = 0, 1, 2, 3
@@ -86,6 +86,12 @@ class Shape(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("reverse", ctypes.c_int),
                 ("center", ctypes.c_double * 3), ("size", ctypes.c_double * 3),
                 ("friction", ctypes.c_double)]
+
+
+class SdfGrid(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_int * 3), ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3),
+                ("bounded", ctypes.c_int), ("bounds_min", ctypes.c_double * 3),
+                ("bounds_max", ctypes.c_double * 3)]
 
 
 class EmitterDesc(ctypes.Structure):
@@ -188,6 +194,12 @@ SIGNATURES = {
     "bbg_emitter_desc_default": [ctypes.POINTER(EmitterDesc)],
     "bbg_emit_volume": [_P, ctypes.POINTER(EmitterDesc), _I, _IP],
     "bbg_map_grid": [_P, _IP],
+    "bbg_collider_set_sdf": [_P, _I, ctypes.POINTER(SdfGrid), ctypes.c_void_p],
+    "bbg_collider_generate_sdf": [_P, _I, ctypes.c_double, ctypes.c_double],
+    "bbg_collider_get_sdf": [_P, _I, ctypes.POINTER(SdfGrid), ctypes.c_void_p, ctypes.c_size_t,
+                             ctypes.POINTER(ctypes.c_size_t)],
+    "bbg_collider_query": [_P, _I, _I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "bbg_map_grid_emit": [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _IP],
     "bbg_checkpoint_save": [_P, ctypes.c_char_p],
     "bbg_checkpoint_load": [_P, ctypes.c_char_p],

@@ -117,6 +117,10 @@ struct bbg_solver_s {
     int grid_n = 0;              // particles in the last grid distribution's sorted ranges
     bool members_ok = false;     // sorted ranges [0, grid_n) are the last distribution's cells
     bool map_full = false;       // MapGridEmit reached the capacity once (it stops emitting)
+    // signed-distance fields of colliders (Params::sdf holds their device descriptors)
+    float *sdf_values[kMaxSdf] = {};
+    bbg_sdf_grid sdf_grid[kMaxSdf] = {};
+    int nsdf = 0;
 };
 
 namespace {
@@ -186,6 +190,18 @@ void drop_graphs(bbg_solver s) {
 
 void free_mlp(bbg_solver s);
 
+// Detaches and frees the colliders' signed-distance fields.
+void free_fields(bbg_solver s) {
+    for (int k = 0; k < kMaxSdf; k++) {
+        if (s->sdf_values[k]) cudaFree(s->sdf_values[k]);
+        s->sdf_values[k] = nullptr;
+        s->P.sdf[k] = SdfDev();
+    }
+    for (int i = 0; i < kMaxColliders; i++) s->P.shapes[i].sdf = -1;
+    s->nsdf = 0;
+    s->P.has_sdf = 0;
+}
+
 void free_frame(bbg_solver s) {
     FrameBufs &F = s->frame;
     void *ptrs[] = {F.lines, F.lens, F.scan_in, F.offset, F.partials, F.out};
@@ -213,6 +229,7 @@ void free_frame(bbg_solver s) {
     for (void *p : kptrs)
         if (p) cudaFree(p);
     K = BucketBufs();
+    free_fields(s);
 }
 
 bbg_status free_all(bbg_solver s) {
@@ -332,6 +349,7 @@ ShapeDev shape_dev(const bbg_shape &sh) {
     d.hz = (float)((double)(float)sh.size[2] / 2.0);
     d.radius = (float)sh.size[0];
     d.friction = (float)sh.friction;
+    d.sdf = -1;
     return d;
 }
 
@@ -625,6 +643,9 @@ void after_substep(bbg_solver s, float dt) {
 }
 
 bbg_status substep(bbg_solver s, float dt) {
+    for (int i = 0; i < s->P.nshapes; i++)
+        if (s->P.shapes[i].type == BBG_SHAPE_SDF && s->P.shapes[i].sdf < 0)
+            return fail(BBG_ERR_STATE, "collider %d is a field-only shape without a field", i);
     s->prof.substep++;
     const bool shipped = s->desc.pcisph_mode == BBG_PCISPH_AS_SHIPPED;
     int max_it = shipped ? 1 : s->desc.max_iterations;
@@ -952,9 +973,14 @@ bbg_status bbg_set_colliders(bbg_solver s, const bbg_shape *shapes, int count) {
         return fail(BBG_ERR_INVALID_ARGUMENT, "collider count must be in [0, %d]", kMaxColliders);
     for (int i = 0; i < count; i++) {
         const bbg_shape &sh = shapes[i];
-        if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE)
+        if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE && sh.type != BBG_SHAPE_SDF)
             return fail(BBG_ERR_INVALID_ARGUMENT, "collider %d: unknown shape type", i);
-        s->P.shapes[i] = shape_dev(sh);
+    }
+    free_fields(s);   // fields belong to the previous colliders
+    for (int i = 0; i < count; i++) {
+        s->P.shapes[i] = shape_dev(shapes[i]);
+        if (shapes[i].type == BBG_SHAPE_SDF)   // defined by its field alone: identity transform
+            for (int k = 0; k < 3; k++) s->P.shapes[i].t[k] = 0.f;
     }
     s->P.nshapes = count;
     s->epoch++;
@@ -2428,6 +2454,177 @@ bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocit
     }
     CK(cudaStreamSynchronize(s->stream));
     if (emitted) *emitted = count;
+    return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// colliders with signed-distance fields (FieldGrid3f; GenerateShapeSDF)
+// ----------------------------------------------------------------------------
+namespace {
+
+// Attaches device node values (owned by the solver from here on) to collider `index`.
+bbg_status attach_field(bbg_solver s, int index, const bbg_sdf_grid &g, float *values) {
+    int slot = s->P.shapes[index].sdf;
+    if (slot < 0) {
+        if (s->nsdf >= kMaxSdf) {
+            cudaFree(values);
+            return fail(BBG_ERR_CAPACITY, "at most %d colliders can have fields", kMaxSdf);
+        }
+        slot = s->nsdf++;
+    } else if (s->sdf_values[slot]) {
+        cudaFree(s->sdf_values[slot]);
+    }
+    s->sdf_values[slot] = values;
+    s->sdf_grid[slot] = g;
+    SdfDev &d = s->P.sdf[slot];
+    d.v = values;
+    d.nx = g.nodes[0];
+    d.ny = g.nodes[1];
+    d.nz = g.nodes[2];
+    for (int k = 0; k < 3; k++) {
+        d.org[k] = (float)g.origin[k];
+        d.sp[k] = (float)g.spacing[k];
+        d.inv2[k] = (float)(1.0 / (2.0 * (double)d.sp[k]));   // Gradient's Float inv
+        d.lo[k] = (float)g.bounds_min[k];
+        d.hi[k] = (float)g.bounds_max[k];
+    }
+    d.bounded = g.bounded ? 1 : 0;
+    s->P.shapes[index].sdf = slot;
+    s->P.has_sdf = 1;
+    s->epoch++;   // captured launches hold the collider parameters
+    return BBG_OK;
+}
+
+bbg_status check_field_target(bbg_solver s, int index) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (s->nscenes > 0) return fail(BBG_ERR_STATE, "fields are not supported on a batch of scenes");
+    if (index < 0 || index >= s->P.nshapes) return fail(BBG_ERR_INVALID_ARGUMENT, "no collider %d", index);
+    return BBG_OK;
+}
+
+}  // namespace
+
+bbg_status bbg_collider_set_sdf(bbg_solver s, int index, const bbg_sdf_grid *grid, const float *values) {
+    if (bbg_status r = check_field_target(s, index)) return r;
+    if (!grid || !values) return fail(BBG_ERR_INVALID_ARGUMENT, "null grid or values");
+    size_t total = 1;
+    for (int k = 0; k < 3; k++) {
+        if (grid->nodes[k] < 1 || !(grid->spacing[k] > 0) || !std::isfinite(grid->origin[k]))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "a field needs >= 1 node, spacing > 0 and a finite origin per axis");
+        total *= (size_t)grid->nodes[k];
+    }
+    if (total >= 0xffffffffull) return fail(BBG_ERR_CAPACITY, "the field has %zu nodes", total);
+    float *d = nullptr;
+    CK(cudaMalloc((void **)&d, sizeof(float) * total));
+    cudaError_t e = cudaMemcpy(d, values, sizeof(float) * total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return fail(BBG_ERR_CUDA, "field upload: %s", cudaGetErrorString(e));
+    }
+    return attach_field(s, index, *grid, d);
+}
+
+bbg_status bbg_collider_generate_sdf(bbg_solver s, int index, double dx, double margin) {
+    if (bbg_status r = check_field_target(s, index)) return r;
+    const ShapeDev &sh = s->P.shapes[index];
+    if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "collider %d is not a box or a sphere", index);
+    if (!(dx > 0) || !(margin >= 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need dx > 0 and margin >= 0");
+    // GetBounds of the translated object box, widened by margin x extent; the grid's
+    // resolution and spacing in the reference's float operations
+    const float h[3] = {sh.type == BBG_SHAPE_BOX ? sh.hx : sh.radius, sh.type == BBG_SHAPE_BOX ? sh.hy : sh.radius,
+                        sh.type == BBG_SHAPE_BOX ? sh.hz : sh.radius};
+    const float mg = (float)margin;
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        lo[k] = -h[k] + sh.t[k];
+        hi[k] = h[k] + sh.t[k];
+        const float scale = hi[k] - lo[k];
+        lo[k] -= scale * mg;
+        hi[k] += scale * mg;
+    }
+    const float width = hi[0] - lo[0], height = hi[1] - lo[1], depth = hi[2] - lo[2];
+    const int res = (int)std::ceil(width / (float)dx);
+    if (res < 1 || res > 4096) return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d cells across", res);
+    const float cell = width / (float)res;
+    const int res_y = (int)std::ceil((float)res * height / width);
+    const int res_z = (int)std::ceil((float)res * depth / width);
+    if (res_y < 0 || res_z < 0 || res_y > 4096 || res_z > 4096)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d x %d x %d cells", res, res_y, res_z);
+    bbg_sdf_grid g;
+    memset(&g, 0, sizeof(g));
+    g.nodes[0] = res + 1;
+    g.nodes[1] = res_y + 1;
+    g.nodes[2] = res_z + 1;
+    for (int k = 0; k < 3; k++) {
+        g.origin[k] = lo[k];
+        g.spacing[k] = cell;
+    }
+    const size_t total = (size_t)g.nodes[0] * g.nodes[1] * g.nodes[2];
+    float *d = nullptr;
+    CK(cudaMalloc((void **)&d, sizeof(float) * total));
+    SdfDev gd;
+    gd.v = d;
+    gd.nx = g.nodes[0];
+    gd.ny = g.nodes[1];
+    gd.nz = g.nodes[2];
+    for (int k = 0; k < 3; k++) {
+        gd.org[k] = lo[k];
+        gd.sp[k] = cell;
+    }
+    launch_sdf_generate(sh, gd, float_above(1e-8), float_above(1e-6), d, s->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return fail(BBG_ERR_CUDA, "field generation: %s", cudaGetErrorString(e));
+    }
+    return attach_field(s, index, g, d);
+}
+
+bbg_status bbg_collider_get_sdf(bbg_solver s, int index, bbg_sdf_grid *grid, float *values, size_t capacity,
+                                size_t *count) {
+    if (bbg_status r = check_field_target(s, index)) return r;
+    const int slot = s->P.shapes[index].sdf;
+    if (slot < 0) return fail(BBG_ERR_NOT_FOUND, "collider %d has no field", index);
+    const bbg_sdf_grid &g = s->sdf_grid[slot];
+    const size_t total = (size_t)g.nodes[0] * g.nodes[1] * g.nodes[2];
+    if (grid) *grid = g;
+    if (count) *count = total;
+    if (values) {
+        if (capacity < total) return fail(BBG_ERR_CAPACITY, "the field has %zu nodes", total);
+        CK(cudaMemcpy(values, s->sdf_values[slot], sizeof(float) * total, cudaMemcpyDeviceToHost));
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_collider_query(bbg_solver s, int index, int n, const float *points, float *sample, float *gradient,
+                              float *closest, float *normal, float *distance, int *inside) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (index < 0 || index >= s->P.nshapes) return fail(BBG_ERR_INVALID_ARGUMENT, "no collider %d", index);
+    if (s->P.shapes[index].type == BBG_SHAPE_SDF && s->P.shapes[index].sdf < 0)
+        return fail(BBG_ERR_STATE, "collider %d is a field-only shape without a field", index);
+    if (n <= 0 || !points) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 points");
+    if ((size_t)n * 17 > 6 * (size_t)s->capacity)
+        return fail(BBG_ERR_CAPACITY, "%d points exceed the staging of capacity %d", n, s->capacity);
+    float *dp = s->B.stage, *dout = s->B.stage + 3 * (size_t)n;
+    CK(cudaMemcpyAsync(dp, points, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    launch_shape_query(s->P, index, n, dp, dout, s->stream);
+    CK_LAUNCH();
+    std::vector<float> o(14 * (size_t)n);
+    CK(cudaMemcpyAsync(o.data(), dout, sizeof(float) * o.size(), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (int q = 0; q < n; q++) {
+        const float *r = &o[14 * (size_t)q];
+        if (sample) sample[q] = r[0];
+        for (int k = 0; k < 3; k++) {
+            if (gradient) gradient[3 * q + k] = r[1 + k];
+            if (closest) closest[3 * q + k] = r[4 + k];
+            if (normal) normal[3 * q + k] = r[7 + k];
+        }
+        if (distance) distance[q] = r[10];
+        if (inside) inside[q] = r[11] != 0.f;
+    }
     return BBG_OK;
 }
 

@@ -30,11 +30,25 @@ struct GridDev {
 };
 
 struct ShapeDev {
-    int type, reverse;
+    int type, reverse;   // type 1: box, 2: sphere, 3: a shape given by its field alone
     float t[3];          // translation
     float hx, hy, hz;    // box half sizes, sizex / 2.0 rounded to float
     float radius;        // sphere radius
     float friction;
+    int sdf;             // index of the shape's signed-distance field in Params::sdf, or -1
+};
+
+// A signed-distance field on a vertex-centred grid (FieldGrid3f, src/core/grid.h:950-1240,
+// built by GenerateShapeSDF or given), sampled trilinearly.
+constexpr int kMaxSdf = 4;
+struct SdfDev {
+    const float *v;      // nodes, x fastest (LinearIndex)
+    int nx, ny, nz;      // nodes per axis (resolution + 1)
+    float org[3];        // minPoint
+    float sp[3];         // spacing
+    float inv2[3];       // (float)(1.0 / (2.0 * spacing)): Gradient's central difference
+    int bounded;         // a mesh's field: positions outside [lo, hi] never collide
+    float lo[3], hi[3];  // (Collider3::OptmizedClosestPointCheck, IsPenetrating)
 };
 
 // Corrector state of one scene of a batch.
@@ -73,6 +87,8 @@ struct Params {
     const ShapeDev *scene_box;      // container box of each scene
     SceneState *scene_st;           // per-scene corrector state (reset each substep)
     unsigned short *scene;          // scene of each sorted slot (density pass)
+    int has_sdf;                    // some collider has a signed-distance field
+    SdfDev sdf[kMaxSdf];
 };
 
 // Per-substep device scalars (reset each substep).
@@ -374,9 +390,170 @@ __device__ __forceinline__ int scene_of(const Params &P, float z) {
     return lo;
 }
 
+// ---- colliders with signed-distance fields ----
+// GetBarycentric (src/core/sampling.h:7-31) of x over nodes [0, high]; a float outside
+// the int range converts as on the host (the lowest int).
+__device__ __forceinline__ void barycentric(float x, int high, int *i, float *f) {
+    const float s = floorf(x);
+    int k = (s >= -2147483648.f && s < 2147483648.f) ? (int)s : (int)0x80000000;
+    if (high == 0) {
+        *i = 0;
+        *f = 0.f;
+    } else if (k < 0) {
+        *i = 0;
+        *f = 0.f;
+    } else if (k > high - 1) {
+        *i = high - 1;
+        *f = 1.f;
+    } else {
+        *i = k;
+        *f = fs(x, s);
+    }
+}
+
+// Lerp (src/core/geometry.h:1087-1089): (1 - t) p0 + t p1
+__device__ __forceinline__ float rlerp(float p0, float p1, float t) { return fa(fm(fs(1.f, t), p0), fm(t, p1)); }
+
+// FieldGrid3f::Sample (src/core/grid.h:1093-1133) of a vertex-centred grid
+__device__ __forceinline__ float sdf_sample(const SdfDev &g, v3 p) {
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const float pc[3] = {p.x, p.y, p.z};
+    int ii[3], jj[3];
+    float w[3];
+    for (int k = 0; k < 3; k++) {
+        const float origin = fa(g.org[k], fm(g.sp[k], 0.f));   // GetDataPosition(0)
+        const float x = fdv(fs(pc[k], origin), g.sp[k]);
+        barycentric(x, n[k] - 1, &ii[k], &w[k]);
+        jj[k] = ii[k] + 1 < n[k] - 1 ? ii[k] + 1 : n[k] - 1;
+    }
+    const unsigned sx = (unsigned)g.nx, sxy = (unsigned)g.nx * (unsigned)g.ny;
+    auto at = [&](int a, int b, int c) {
+        return __ldg(&g.v[(unsigned)a + (unsigned)b * sx + (unsigned)c * sxy]);
+    };
+    const float f000 = at(ii[0], ii[1], ii[2]), f100 = at(jj[0], ii[1], ii[2]);
+    const float f010 = at(ii[0], jj[1], ii[2]), f110 = at(jj[0], jj[1], ii[2]);
+    const float f001 = at(ii[0], ii[1], jj[2]), f101 = at(jj[0], ii[1], jj[2]);
+    const float f011 = at(ii[0], jj[1], jj[2]), f111 = at(jj[0], jj[1], jj[2]);
+    const float b0 = rlerp(rlerp(f000, f100, w[0]), rlerp(f010, f110, w[0]), w[1]);
+    const float b1 = rlerp(rlerp(f001, f101, w[0]), rlerp(f011, f111, w[0]), w[1]);
+    return rlerp(b0, b1, w[2]);
+}
+
+// FieldGrid3f::Gradient (grid.h:1153-1169): central differences one spacing apart
+__device__ __forceinline__ v3 sdf_gradient(const SdfDev &g, v3 p) {
+    float d[3];
+    for (int k = 0; k < 3; k++) {
+        const v3 s = V(k == 0 ? g.sp[0] : 0.f, k == 1 ? g.sp[1] : 0.f, k == 2 ? g.sp[2] : 0.f);
+        d[k] = fm(fs(sdf_sample(g, vadd(p, s)), sdf_sample(g, vsub(p, s))), g.inv2[k]);
+    }
+    return V(d[0], d[1], d[2]);
+}
+
+// Transform::Point of a translation ((1 x + 0 y) + 0 z) + t, in the host's operation order
+__device__ __forceinline__ v3 translate_point(v3 p, float tx, float ty, float tz) {
+    return V(fa(fa(fa(fm(1.f, p.x), fm(0.f, p.y)), fm(0.f, p.z)), tx),
+             fa(fa(fa(fm(0.f, p.x), fm(1.f, p.y)), fm(0.f, p.z)), ty),
+             fa(fa(fa(fm(0.f, p.x), fm(0.f, p.y)), fm(1.f, p.z)), tz));
+}
+
+// Shape::ClosestPointBySDF (src/shapes/bvh.cpp:666-707): the object-space point marched
+// onto the zero level along the normalised gradient (at most 5 steps, stop at |sdf| <
+// 0.001); the distance is unsigned.
+__device__ __forceinline__ Cpq sdf_closest_point(const ShapeDev &s, const SdfDev &g, v3 pw) {
+    const v3 point = translate_point(pw, -s.t[0], -s.t[1], -s.t[2]);   // WorldToObject
+    v3 tn = V(0.f, 1.f, 0.f), tp = point;
+    bool has_gradient = false;
+    for (int i = 0; i < 5; i++) {
+        const float sdf = sdf_sample(g, tp);
+        if ((double)fabsf(sdf) < 0.001) break;
+        tn = sdf_gradient(g, tp);
+        const float len = vlen(tn);
+        if (len > 0.f) tn = vdiv(tn, len);
+        tp = vsub(tp, vmul(tn, sdf));
+        has_gradient = true;
+    }
+    if (!has_gradient) {
+        tn = sdf_gradient(g, tp);
+        const float len = vlen(tn);
+        if (len > 0.f) tn = vdiv(tn, len);
+    }
+    Cpq q;
+    q.sd = vlen(vsub(point, tp));
+    q.point = translate_point(tp, s.t[0], s.t[1], s.t[2]);   // ObjectToWorld
+    // ObjectToWorld.Normal: the inverse's transpose, identity for a translation
+    q.normal = V(fa(fa(fm(1.f, tn.x), fm(0.f, tn.y)), fm(0.f, tn.z)),
+                 fa(fa(fm(0.f, tn.x), fm(1.f, tn.y)), fm(0.f, tn.z)),
+                 fa(fa(fm(0.f, tn.x), fm(0.f, tn.y)), fm(1.f, tn.z)));
+    return q;
+}
+
+// ColliderSet3::ResolveCollision + CollisionHandle (src/core/collider.cpp:3-44, 238-264)
+// when a collider has a field: the target is the least |ClosestDistance| (the analytic
+// distance, or the field's sample for a field-only shape), its closest point comes from
+// ClosestPointBySDF and IsInside from the field's sample; a mesh's field skips positions
+// outside the mesh bounds.  Kept out of line: the fast path above serves analytic shapes.
+struct Contact { v3 pos, vel; };
+static __device__ __noinline__ Contact resolve_with_fields(const Params &P, float r, float rc1, v3 p, v3 v) {
+    Contact out;
+    out.pos = p;
+    out.vel = v;
+    v3 *pos = &out.pos, *vel = &out.vel;
+    int target = -1;
+    float minD = 3.402823466e+38f;
+    for (int i = 0; i < P.nshapes; i++) {
+        const ShapeDev &s = P.shapes[i];
+        if (s.sdf >= 0 && P.sdf[s.sdf].bounded &&
+            !inside3(p, V(P.sdf[s.sdf].lo[0], P.sdf[s.sdf].lo[1], P.sdf[s.sdf].lo[2]),
+                     V(P.sdf[s.sdf].hi[0], P.sdf[s.sdf].hi[1], P.sdf[s.sdf].hi[2]), P.iz6))
+            continue;
+        const float d = s.type == 3 ? sdf_sample(P.sdf[s.sdf], p) : shape_closest_point(s, p, P.iz, P.iz6).sd;
+        if (fabsf(d) < minD) {
+            target = i;
+            minD = fabsf(d);
+        }
+    }
+    if (target < 0) return out;
+    const ShapeDev &s = P.shapes[target];
+    Cpq q;
+    bool inside;
+    if (s.sdf >= 0) {
+        q = sdf_closest_point(s, P.sdf[s.sdf], p);
+        inside = sdf_sample(P.sdf[s.sdf], p) < 0.f;   // Shape::IsInside of a filled field
+    } else {
+        q = shape_closest_point(s, p, P.iz, P.iz6);
+        inside = (s.reverse != 0) == !(q.sd < 0.f);
+    }
+    if (!(inside || fabsf(q.sd) < P.radius)) return out;
+    v3 n = q.normal;
+    v3 targetPoint = vadd(q.point, vmul(n, P.radius));
+    v3 rel = *vel;
+    float ndr = vdot(n, rel);
+    v3 relN = vmul(n, ndr);
+    v3 relT = vsub(rel, relN);
+    if (ndr < 0.f) {
+        v3 dRelN = vmul(relN, rc1);
+        relN = vmul(relN, -r);
+        if (vlen2(relT) > 0.f) {
+            float scale = fdv(vlen(dRelN), vlen(relT));
+            float fScale = fs(1.0f, fm(s.friction, scale));
+            float frictionScale = rmax(0.f, fScale);
+            relT = vmul(relT, frictionScale);
+        }
+        *vel = vadd(vadd(relN, relT), V(0.f, 0.f, 0.f));
+    }
+    *pos = targetPoint;
+    return out;
+}
+
 // ColliderSet3::ResolveCollision over the scene's colliders: the global shapes of a
 // single scene, or the container box of the particle's scene in a batch.
 __device__ __forceinline__ void resolve_collision(const Params &P, float r, float rc1, v3 *pos, v3 *vel) {
+    if (P.has_sdf) {
+        const Contact c = resolve_with_fields(P, r, rc1, *pos, *vel);
+        *pos = c.pos;
+        *vel = c.vel;
+        return;
+    }
     if (P.nscenes > 0) {
         const ShapeDev box = P.scene_box[scene_of(P, pos->z)];
         resolve_against(P, &box, 1, r, rc1, pos, vel);

@@ -98,4 +98,10 @@ void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cuda
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
                              cudaStream_t s);
 
+// GenerateShapeSDF of an analytic shape into the node values of grid g (sdf.cu)
+void launch_sdf_generate(const ShapeDev &shape, const SdfDev &g, float iz, float iz6, float *out, cudaStream_t s);
+
+// Shape queries of collider `index` at n points (xyz); 14 floats per point out (sdf.cu)
+void launch_shape_query(const Params &P, int index, int n, const float *pts, float *out, cudaStream_t s);
+
 }  // namespace bbg

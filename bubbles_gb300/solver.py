@@ -48,14 +48,14 @@ def desc_from_scene(scene, device=0):
 def fill_shape(dst, c):
     """A bbg_shape from a shape dict ({"type": "box", "size", "center", "reverse"} or
     {"type": "sphere", "radius", ...})."""
-    dst.type = N.SHAPE_BOX if c["type"] == "box" else N.SHAPE_SPHERE
+    dst.type = {"box": N.SHAPE_BOX, "sphere": N.SHAPE_SPHERE, "sdf": N.SHAPE_SDF}[c["type"]]
     dst.reverse = 1 if c.get("reverse", False) else 0
     for k in range(3):
         dst.center[k] = float(c.get("center", (0.0, 0.0, 0.0))[k])
     if c["type"] == "box":
         for k in range(3):
             dst.size[k] = float(c["size"][k])
-    else:
+    elif c["type"] == "sphere":
         dst.size[0] = float(c["radius"])
     dst.friction = float(c.get("friction", 0.0))
 
@@ -149,6 +149,52 @@ class Solver:
         N.call("bbg_emit_volume", self.h, ctypes.byref(e), int(bool(append)), ctypes.byref(out))
         self.n = self.particle_count()
         return out.value
+
+    # --- colliders with signed-distance fields -------------------------------------
+    def set_sdf(self, index, nodes, origin, spacing, values, bounds=None):
+        """Attach a vertex-centred field (nodes per axis, x fastest values) to collider
+        `index`; bounds=(lo, hi) marks a mesh's field."""
+        g = N.SdfGrid()
+        for k in range(3):
+            g.nodes[k] = int(nodes[k])
+            g.origin[k] = float(origin[k])
+            g.spacing[k] = float(spacing[k] if np.ndim(spacing) else spacing)
+        if bounds is not None:
+            g.bounded = 1
+            for k in range(3):
+                g.bounds_min[k] = float(bounds[0][k])
+                g.bounds_max[k] = float(bounds[1][k])
+        v = np.ascontiguousarray(values, dtype=np.float32).reshape(-1)
+        if v.size != int(np.prod([int(x) for x in nodes])):
+            raise ValueError("values must hold one float per node")
+        N.call("bbg_collider_set_sdf", self.h, int(index), ctypes.byref(g), v.ctypes.data)
+
+    def generate_sdf(self, index, dx=0.01, margin=0.1):
+        """GenerateShapeSDF of a box or sphere collider on the device (attached to it)."""
+        N.call("bbg_collider_generate_sdf", self.h, int(index), float(dx), float(margin))
+
+    def get_sdf(self, index):
+        """(nodes, origin, spacing, values) of collider `index`'s field."""
+        g = N.SdfGrid()
+        cnt = ctypes.c_size_t()
+        N.call("bbg_collider_get_sdf", self.h, int(index), ctypes.byref(g), None, 0, ctypes.byref(cnt))
+        vals = np.empty(cnt.value, np.float32)
+        N.call("bbg_collider_get_sdf", self.h, int(index), ctypes.byref(g), vals.ctypes.data, vals.size,
+               ctypes.byref(cnt))
+        return np.array(g.nodes[:]), np.array(g.origin[:]), np.array(g.spacing[:]), vals
+
+    def collider_query(self, index, points):
+        """Collider `index` at the points as the collision code sees it: dict of sample,
+        gradient, point, normal, distance, inside."""
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        n = len(p)
+        out = {"sample": np.zeros(n, np.float32), "gradient": np.zeros((n, 3), np.float32),
+               "point": np.zeros((n, 3), np.float32), "normal": np.zeros((n, 3), np.float32),
+               "distance": np.zeros(n, np.float32), "inside": np.zeros(n, np.int32)}
+        N.call("bbg_collider_query", self.h, int(index), n, p.ctypes.data, out["sample"].ctypes.data,
+               out["gradient"].ctypes.data, out["point"].ctypes.data, out["normal"].ctypes.data,
+               out["distance"].ctypes.data, out["inside"].ctypes.data)
+        return out
 
     def map_grid(self):
         """ContinuousParticleSetBuilder3::MapGrid: remember the occupied cells' positions."""

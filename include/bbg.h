@@ -69,6 +69,7 @@ typedef int bbg_status;
 
 #define BBG_SHAPE_BOX 1
 #define BBG_SHAPE_SPHERE 2
+#define BBG_SHAPE_SDF 3      /* defined by a signed-distance field alone (MakeSDFShape) */
 #define BBG_MAX_COLLIDERS 16
 
 /* Field ids for bbg_get_field / bbg_set_field (ParticleSet3 accessors,
@@ -275,6 +276,44 @@ bbg_status bbg_checkpoint_load(bbg_solver s, const char *path);
  * (BBG_ERR_CAPACITY). */
 bbg_status bbg_checkpoint_write(bbg_solver s, void *buf, size_t capacity, size_t *length);
 bbg_status bbg_checkpoint_read(bbg_solver s, const void *buf, size_t length);
+
+/* ----- colliders with signed-distance fields ---------------------------------------- */
+/* A vertex-centred FieldGrid3f (src/core/grid.h:950-1240): nodes[k] = cells + 1 per axis,
+ * node (i, j, k) at origin + spacing * (i, j, k), values x fastest.  A collider with a
+ * field resolves collisions as the reference's shapes with a filled grid do
+ * (ColliderSet3::ResolveCollision, src/core/collider.cpp:238-264): the target is the least
+ * |ClosestDistance| (analytic for a box or sphere, the field's trilinear sample for a
+ * BBG_SHAPE_SDF collider), the closest point is Shape::ClosestPointBySDF
+ * (src/shapes/bvh.cpp:666-707: five gradient steps at most), IsInside is sample < 0.  A
+ * field with `bounded` set is a mesh's: positions outside [bounds_min, bounds_max] never
+ * collide with it (Collider3::OptmizedClosestPointCheck); its target distance is the
+ * field's sample where the reference measures the mesh itself.  At most 4 fields; setting
+ * the colliders again drops them. */
+typedef struct {
+    int nodes[3];
+    double origin[3];
+    double spacing[3];
+    int bounded;
+    double bounds_min[3], bounds_max[3];
+} bbg_sdf_grid;
+bbg_status bbg_collider_set_sdf(bbg_solver s, int index, const bbg_sdf_grid *grid, const float *values);
+/* GenerateShapeSDF (src/core/shape.cpp:479-510) of a box or sphere collider on the device:
+ * the shape's bounds widened by margin x extent, ceil(width / dx) cells across, nodes set
+ * to max(|ClosestDistance|, 1e-5) signed by IsInside; the field is attached to the
+ * collider.  Reference defaults: dx 0.01, margin 0.1. */
+bbg_status bbg_collider_generate_sdf(bbg_solver s, int index, double dx, double margin);
+/* A collider's field: its grid, and its values when capacity (in floats) suffices;
+ * *count = node count. */
+bbg_status bbg_collider_get_sdf(bbg_solver s, int index, bbg_sdf_grid *grid, float *values, size_t capacity,
+                                size_t *count);
+
+/* Collider `index` queried at n points as the collision code sees it: its field's Sample
+ * and Gradient (zeros without a field), Shape::ClosestPoint (point, normal, distance: signed
+ * for an analytic shape, the marched distance with a field) and IsInside.  Any output may
+ * be NULL.  Needs 17 n <= 6 capacity. */
+bbg_status bbg_collider_query(bbg_solver s, int index, int n, const float *points, float *sample,
+                              float *gradient, float *closest, float *normal, float *distance,
+                              int *inside);
 
 /* ----- particle seeding (VolumeParticleEmitter3) --------------------------------- */
 /* VolumeParticleEmitter3 (src/core/emitter.h:39-69, emitter.cpp:241-330) with a box or

@@ -114,6 +114,7 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_shape_distance": (None, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, _I32]),
         "orc_emit_volume": (ctypes.c_long, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, ctypes.c_double,
                                             ctypes.c_double, _D, ctypes.c_long, _D, _D, ctypes.c_long]),
         "orc_frame_parse": (ctypes.c_long, [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
@@ -399,4 +400,21 @@ def emit_volume(shape, spacing, jitter=0.0, velocity=(0.0, 0.0, 0.0), max_partic
     n = lib.orc_emit_volume(ctypes.byref(sh), int(bounds is not None), _ptr(bmin), _ptr(bmax), float(spacing),
                             float(jitter), _ptr(v), int(max_particles), _ptr(pos), _ptr(vel), capacity)
     return pos[:min(n, capacity)], vel[:min(n, capacity)]
+
+
+def shape_distance(shape, points, variant="f32"):
+    """Shape::ClosestDistance and IsInside of a box or sphere shape dict at the points."""
+    lib = load(variant)
+    sh = Shape()
+    box = shape["type"] == "box"
+    sh.type = SHAPE_BOX if box else SHAPE_SPHERE
+    sh.reverse = int(bool(shape.get("reverse", False)))
+    for k in range(3):
+        sh.center[k] = shape.get("center", (0.0, 0.0, 0.0))[k]
+        sh.size[k] = shape["size"][k] if box else (shape["radius"] if k == 0 else 0.0)
+    p = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    d = np.zeros(len(p))
+    ins = np.zeros(len(p), np.int32)
+    lib.orc_shape_distance(ctypes.byref(sh), len(p), _ptr(p), _ptr(d), _ptr(ins, _I32))
+    return d, ins
 

@@ -40,6 +40,7 @@ struct RefSim {
     ParticleSet3 *pSet = nullptr;
     Grid3 *grid = nullptr;
     ContinuousParticleSetBuilder3 *cont = nullptr;   // ref_create_continuous only
+    ColliderSet3 *cs = nullptr;
 };
 
 static vec3f V3(const double *a) { return vec3f((Float)a[0], (Float)a[1], (Float)a[2]); }
@@ -87,6 +88,7 @@ static RefSim *finish_sim(RefSim *s, const orc_params *p, SphParticleSet3 *set, 
             cb.AddCollider3(shape, c.friction);
         }
         ColliderSet3 *cs = cb.GetColliderSet();
+        s->cs = cs;
         if (kind == 0) s->pci.SetColliders(cs);
         else s->sph.SetColliders(cs);
     }
@@ -286,6 +288,58 @@ int ref_emit_volume(int type, int reverse, const double *center, const double *s
     }
     delete em;
     return n;
+}
+
+/* GenerateShapeSDF(shape, dx, margin) of collider i's shape. */
+void ref_generate_collider_sdf(RefSim *s, int i, double dx, double margin) {
+    GenerateShapeSDF(s->cs->colliders[i]->shape, (Float)dx, (Float)margin);
+}
+
+/* Collider i's shape becomes MakeSDFShape over the sphere's bounds: a field-only shape
+ * whose nodes hold Distance(p, center) - radius. */
+void ref_make_sdf_sphere_collider(RefSim *s, int i, const double *center, double radius, double dx,
+                                  double margin) {
+    const vec3f c = V3(center);
+    const Float r = (Float)radius;
+    Bounds3f b(c - vec3f(r), c + vec3f(r));
+    s->cs->colliders[i]->shape = MakeSDFShape(b, [c, r](const vec3f &p, Shape *, int) -> Float {
+        return Distance(p, c) - r;
+    }, (Float)dx, (Float)margin);
+}
+
+/* Collider i's field: nodes, origin, spacing; up to `capacity` values (x fastest). */
+int ref_collider_sdf(RefSim *s, int i, int *nodes, double *origin, double *spacing, float *values, int capacity) {
+    FieldGrid3f *g = s->cs->colliders[i]->shape->grid;
+    if (!g) return 0;
+    for (int k = 0; k < 3; k++) {
+        nodes[k] = (int)g->resolution[k];
+        origin[k] = g->minPoint[k];
+        spacing[k] = g->spacing[k];
+    }
+    const int total = (int)g->total;
+    for (int q = 0; q < total && q < capacity; q++) values[q] = (float)g->field[q];
+    return total;
+}
+
+/* Collider i's field and shape queries at n points: FieldGrid3f::Sample, Gradient,
+ * Shape::ClosestPoint (point, normal, signed distance) and IsInside. */
+void ref_sdf_probe(RefSim *s, int i, int n, const double *pts, double *sample, double *grad, double *cp,
+                   double *cn, double *cd, int *inside) {
+    Shape *shape = s->cs->colliders[i]->shape;
+    for (int q = 0; q < n; q++) {
+        const vec3f p = V3(&pts[3 * q]);
+        sample[q] = shape->grid->Sample(p);
+        const vec3f gr = shape->grid->Gradient(p);
+        ClosestPointQuery cq;
+        shape->ClosestPoint(p, &cq);
+        for (int k = 0; k < 3; k++) {
+            grad[3 * q + k] = gr[k];
+            cp[3 * q + k] = cq.point[k];
+            cn[3 * q + k] = cq.normal[k];
+        }
+        cd[q] = cq.signedDistance;
+        inside[q] = shape->IsInside(p) ? 1 : 0;
+    }
 }
 
 /* SerializerLoadParticles3 on a frame file: the first fluid section's particles (at most

@@ -47,6 +47,12 @@ def load(variant):
         "ref_create_continuous": (_P, [ctypes.POINTER(O.Params), ctypes.c_int, _D, _D, ctypes.c_int,
                                        ctypes.c_int]),
         "ref_map_grid": (None, [_P]),
+        "ref_generate_collider_sdf": (None, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+        "ref_make_sdf_sphere_collider": (None, [_P, ctypes.c_int, _D, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double]),
+        "ref_collider_sdf": (ctypes.c_int, [_P, ctypes.c_int, _I32, _D, _D, ctypes.POINTER(ctypes.c_float),
+                                            ctypes.c_int]),
+        "ref_sdf_probe": (None, [_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, _I32]),
         "ref_map_grid_emit": (ctypes.c_int, [_P, ctypes.c_double, _D]),
         "ref_destroy": (None, [_P]),
         "ref_scalars": (None, [_P, _D]),
@@ -107,6 +113,29 @@ class RefSim:
                                                     vp, kind, int(continuous))
         else:
             self.h = self.lib.ref_create(ctypes.byref(self._params), self.n, pos.ctypes.data_as(_D), vp, kind)
+
+    def collider_sdf(self, i):
+        """Collider i's field: (nodes, origin, spacing, values float32 x fastest)."""
+        nodes = np.zeros(3, np.int32)
+        org = np.zeros(3)
+        sp = np.zeros(3)
+        n = self.lib.ref_collider_sdf(self.h, i, nodes.ctypes.data_as(_I32), org.ctypes.data_as(_D),
+                                      sp.ctypes.data_as(_D), None, 0)
+        vals = np.zeros(n, np.float32)
+        self.lib.ref_collider_sdf(self.h, i, nodes.ctypes.data_as(_I32), org.ctypes.data_as(_D),
+                                  sp.ctypes.data_as(_D), vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n)
+        return nodes, org, sp, vals
+
+    def sdf_probe(self, i, pts):
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        n = len(pts)
+        out = {"sample": np.zeros(n), "gradient": np.zeros((n, 3)), "point": np.zeros((n, 3)),
+               "normal": np.zeros((n, 3)), "distance": np.zeros(n), "inside": np.zeros(n, np.int32)}
+        self.lib.ref_sdf_probe(self.h, i, n, pts.ctypes.data_as(_D), out["sample"].ctypes.data_as(_D),
+                               out["gradient"].ctypes.data_as(_D), out["point"].ctypes.data_as(_D),
+                               out["normal"].ctypes.data_as(_D), out["distance"].ctypes.data_as(_D),
+                               out["inside"].ctypes.data_as(_I32))
+        return out
 
     def map_grid_emit(self, d, velocity=(0.0, 0.0, 0.0)):
         v = np.array(velocity, np.float64)

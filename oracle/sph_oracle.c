@@ -1655,3 +1655,18 @@ long orc_emit_volume(const orc_shape *shape, int use_bounds, const double bmin[3
     }
     return emitted;
 }
+
+void orc_shape_distance(const orc_shape *shape, int n, const double *pts, double *distance, int *inside) {
+    oshape s;
+    s.type = shape->type;
+    s.reverse = shape->reverse ? 1 : 0;
+    s.t = V((Float)shape->center[0], (Float)shape->center[1], (Float)shape->center[2]);
+    s.sx = (Float)shape->size[0]; s.sy = (Float)shape->size[1]; s.sz = (Float)shape->size[2];
+    s.radius = (Float)shape->size[0];
+    s.friction = 0;
+    for (int i = 0; i < n; i++) {
+        const v3 p = V((Float)pts[3 * i], (Float)pts[3 * i + 1], (Float)pts[3 * i + 2]);
+        distance[i] = shape_closest_distance(&s, p);
+        inside[i] = shape_is_inside(&s, p);
+    }
+}

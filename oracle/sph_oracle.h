@@ -169,6 +169,10 @@ int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
 size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
                         double mass, double spacing, char *buf, size_t capacity);
 
+/* Shape::ClosestDistance and IsInside of a box or sphere at n points (src/core/shape.cpp:
+ * 206-232, 275-282): the values SetNodeSDFKernel (shape.cpp:409-424) signs into a field. */
+void     orc_shape_distance(const orc_shape *shape, int n, const double *pts, double *distance, int *inside);
+
 /* VolumeParticleEmitter3::Emit into a ParticleSetBuilder3 (src/core/emitter.cpp:8-12,
  * 241-330) for a box or sphere: the BCC lattice of BccLatticePointGenerator::ForEach
  * (src/generator/bcclattice.cpp:6-36) over the shape's bounds (or [bmin, bmax] when

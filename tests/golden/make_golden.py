@@ -24,6 +24,10 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   after Setup, positions moved by hand, then two MapGridEmit calls; the
                   particle arrays after each, for a capacity that holds them and one that
                   stops the first call (CONTINUOUS_CASES).
+  sdf_f32.npz     a field-only collider (MakeSDFShape of the scene's sphere, core/shape.h):
+                  its grid, FieldGrid3f::Sample / Gradient, Shape::ClosestPoint and IsInside
+                  at probe points, and TimeIntegrationCPU's collision response of 4,000
+                  particles driven into the walls and the field.
   emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
                   srand(seed) for boxes and spheres, with and without jitter, explicit
                   bounds, a reversed box and a binding max_particles (EMIT_CASES).
@@ -32,6 +36,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py frames    # frame_f32.npz only
     python tests/golden/make_golden.py emit      # emit_f32.npz only
     python tests/golden/make_golden.py continuous    # continuous_f32.npz only
+    python tests/golden/make_golden.py sdf       # sdf_f32.npz only
 """
 import json
 import os
@@ -178,6 +183,41 @@ def make_emit():
     np.savez_compressed(os.path.join(HERE, "emit_f32.npz"), **out)
 
 
+def sdf_collision_inputs(sc, rng):
+    """Positions and velocities driving particles into the container and the sphere."""
+    lo, hi = np.array(sc["domain_min"]), np.array(sc["domain_max"])
+    p = rng.uniform(lo - 0.01, hi + 0.01, size=(4000, 3))
+    sph = sc["colliders"][1]
+    p[:1500] = np.array(sph["center"]) + rng.normal(size=(1500, 3)) * sph["radius"] * 0.7
+    v = rng.normal(size=p.shape) * 2.0
+    return p.astype(np.float32), v.astype(np.float32)
+
+
+def make_sdf():
+    import ctypes
+    sc, _ = pcisph_scene()
+    sph = sc["colliders"][1]
+    center = np.array(sph["center"], np.float64)
+    rng = np.random.default_rng(21)
+    p, v = sdf_collision_inputs(sc, rng)
+    r = R.RefSim(sc, p, v)
+    r.make_sdf_sphere_collider(1, center.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sph["radius"], 0.01,
+                               0.2)
+    nodes, org, sp, vals = r.collider_sdf(1)
+    out = {"scene": np.array(json.dumps(clean(sc))), "nodes": nodes, "origin": org, "spacing": sp,
+           "values": vals, "pos_in": p, "vel_in": v}
+    pts = (center + rng.normal(size=(800, 3)) * sph["radius"] * 0.9).astype(np.float32)
+    pts[:100] = (center + rng.uniform(-0.5, 0.5, size=(100, 3))).astype(np.float32)   # beyond the grid too
+    out["probe_points"] = pts
+    for k, a in r.sdf_probe(1, pts.astype(np.float64)).items():
+        out["probe_" + k] = a
+    r.set(O.FORCE, np.zeros_like(p, dtype=np.float64))
+    r.time_integration(1e-3)
+    out["pos_out"] = r.get(O.POSITION)
+    out["vel_out"] = r.get(O.VELOCITY)
+    np.savez_compressed(os.path.join(HERE, "sdf_f32.npz"), **out)
+
+
 # continuous emission cases: builder capacity, MapGridEmit distance, velocity
 CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
 
@@ -217,4 +257,6 @@ if __name__ == "__main__":
         make_emit()
     if not what or what == ["continuous"]:
         make_continuous()
+    if not what or what == ["sdf"]:
+        make_sdf()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
