@@ -2605,15 +2605,20 @@ bbg_status bbg_collider_query(bbg_solver s, int index, int n, const float *point
     if (s->P.shapes[index].type == BBG_SHAPE_SDF && s->P.shapes[index].sdf < 0)
         return fail(BBG_ERR_STATE, "collider %d is a field-only shape without a field", index);
     if (n <= 0 || !points) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 points");
-    if ((size_t)n * 17 > 6 * (size_t)s->capacity)
-        return fail(BBG_ERR_CAPACITY, "%d points exceed the staging of capacity %d", n, s->capacity);
-    float *dp = s->B.stage, *dout = s->B.stage + 3 * (size_t)n;
-    CK(cudaMemcpyAsync(dp, points, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-    launch_shape_query(s->P, index, n, dp, dout, s->stream);
-    CK_LAUNCH();
+    float *dp = nullptr;   // a query buffer of its own: 3 in + 14 out floats per point
+    CK(cudaMalloc((void **)&dp, sizeof(float) * 17 * (size_t)n));
+    float *dout = dp + 3 * (size_t)n;
     std::vector<float> o(14 * (size_t)n);
-    CK(cudaMemcpyAsync(o.data(), dout, sizeof(float) * o.size(), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    cudaError_t e = cudaMemcpyAsync(dp, points, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+        launch_shape_query(s->P, index, n, dp, dout, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(o.data(), dout, sizeof(float) * o.size(), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(dp);
+    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "collider query: %s", cudaGetErrorString(e));
     for (int q = 0; q < n; q++) {
         const float *r = &o[14 * (size_t)q];
         if (sample) sample[q] = r[0];

@@ -310,7 +310,7 @@ bbg_status bbg_collider_get_sdf(bbg_solver s, int index, bbg_sdf_grid *grid, flo
 /* Collider `index` queried at n points as the collision code sees it: its field's Sample
  * and Gradient (zeros without a field), Shape::ClosestPoint (point, normal, distance: signed
  * for an analytic shape, the marched distance with a field) and IsInside.  Any output may
- * be NULL.  Needs 17 n <= 6 capacity. */
+ * be NULL. */
 bbg_status bbg_collider_query(bbg_solver s, int index, int n, const float *points, float *sample,
                               float *gradient, float *closest, float *normal, float *distance,
                               int *inside);
