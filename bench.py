@@ -357,6 +357,58 @@ def frame_io(bb, g, scene, n, device, reps=5):
             "measured": "host wall clock around the C-ABI calls (frame bytes in pageable host memory)"}
 
 
+def seeding(bb, scene, final_pos, device, reps=3):
+    """Particle seeding on the device, end to end through the C ABI, beside the oracle's
+    restatement of the reference's CPU code (single thread, as the reference):
+    - VolumeParticleEmitter3: a jittered BCC sphere of about 0.7 M particles at the
+      scene's spacing (the rand() jitter sequence is drawn on the host, as in the reference);
+    - MapGridEmit: the final state mapped, every particle moved half a spacing, the mapped
+      cells refilled (capacity twice the particle count)."""
+    import ctypes
+    from oracle import oracle as O
+    libc = ctypes.CDLL(None)
+    sp = scene["spacing"]
+    n = len(final_pos)
+    out = {}
+    shape = {"type": "sphere", "radius": 0.35 * (sp / 0.008), "center": (0.0, 0.0, 0.0)}
+    s = bb.Solver(dict(scene), capacity=2 * n, device=device)
+    t = []
+    for _ in range(reps + 1):
+        libc.srand(42)
+        t0 = time.perf_counter()
+        k = s.emit_volume(shape, sp, jitter=0.2)
+        t.append(time.perf_counter() - t0)
+    libc.srand(42)
+    t0 = time.perf_counter()
+    want, _ = O.emit_volume(shape, sp, jitter=0.2, capacity=k + 1)
+    cpu = time.perf_counter() - t0
+    out["volume_emitter"] = {"particles": k, "ms": 1e3 * float(np.median(t[1:])),
+                             "cpu_ms": 1e3 * cpu, "cpu_kind": "port", "cpu_cores": 1,
+                             "same_as_oracle": bool(len(want) == k)}
+    # continuous emission on the final state
+    s.upload(final_pos)
+    s.setup()
+    s.map_grid()
+    moved = (final_pos + np.float32(0.5 * sp) * np.array([0.0, -1.0, 0.0], np.float32)).astype(np.float32)
+    s.set(bb.FIELD_POSITION, moved)
+    t0 = time.perf_counter()
+    added = s.map_grid_emit(0.5 * sp)
+    gpu = time.perf_counter() - t0
+    s.close()
+    o = O.OracleSim(scene, final_pos)
+    o.update_grid_distribution()
+    o.map_grid()
+    o.set(O.POSITION, moved)
+    t0 = time.perf_counter()
+    ref = o.map_grid_emit(0.5 * sp)
+    cpu = time.perf_counter() - t0
+    o.close()
+    out["map_grid_emit"] = {"particles": n, "added": added, "ms": 1e3 * gpu, "cpu_ms": 1e3 * cpu,
+                            "cpu_kind": "port", "cpu_cores": 1, "same_as_oracle": bool(len(ref) == added)}
+    out["measured"] = "host wall clock around the C-ABI calls (single call; emitter median of %d)" % reps
+    return out
+
+
 def run_ours(args, scene, pos):
     import torch
 
@@ -498,9 +550,10 @@ def run_ours(args, scene, pos):
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
         batch_offsets = g.layout() if scene.get("batch") else None
-        frames = None
+        frames = seeds = None
         if not scene.get("batch") and not args.no_frames and rank == 0:
             frames = frame_io(bb, g, scene, n, local)
+            seeds = seeding(bb, scene, final_pos, local)
         g.close()
 
     if rank != 0:
@@ -597,6 +650,8 @@ def run_ours(args, scene, pos):
     }
     if frames is not None:
         line["frame_io"] = frames
+    if seeds is not None:
+        line["seeding"] = seeds
     print(json.dumps(line), flush=True)
     barrier(dist)
 
@@ -616,7 +671,8 @@ def main():
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
-    ap.add_argument("--no-frames", action="store_true", help="skip the particle-frame writer / reader timing")
+    ap.add_argument("--no-frames", action="store_true",
+                    help="skip the particle-frame and seeding timings (frame writer / reader, emitters)")
     ap.add_argument("--no-tuning", action="store_true",
                     help="ignore bubbles_gb300/tuned/<config>.json (autotuner output)")
     ap.add_argument("--variant", default="learned", choices=["plain", "warm", "learned"],

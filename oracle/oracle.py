@@ -114,6 +114,8 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_map_grid": (None, [_P]),
+        "orc_map_grid_emit": (ctypes.c_long, [_P, ctypes.c_double, _D, ctypes.c_long]),
         "orc_shape_distance": (None, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, _I32]),
         "orc_emit_volume": (ctypes.c_long, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, ctypes.c_double,
                                             ctypes.c_double, _D, ctypes.c_long, _D, _D, ctypes.c_long]),
@@ -283,6 +285,17 @@ class OracleSim:
         return self.lib.orc_advance_sph(self.h, dt, int(inplace))
 
     # --- fields ---------------------------------------------------------------
+    def map_grid(self):
+        """ContinuousParticleSetBuilder3::MapGrid on the current chains."""
+        self.lib.orc_map_grid(self.h)
+
+    def map_grid_emit(self, distance):
+        """Positions MapGridEmit would add (cells ascending, chain order), float64 (k, 3)."""
+        k = self.lib.orc_map_grid_emit(self.h, float(distance), None, 0)
+        out = np.zeros((max(k, 0), 3))
+        self.lib.orc_map_grid_emit(self.h, float(distance), _ptr(out), k)
+        return out
+
     def get(self, field):
         if field in VECTOR_FIELDS:
             out = np.zeros((self.n, 3))

@@ -594,6 +594,9 @@ struct orc_sim {
     int frame_index;
     int tol_mode;   /* PredictPressure stores densityErrors (tolerance mode) */
     int clamp_total; /* warm start: negative total pressure scaled instead of the increment */
+    /* ContinuousParticleSetBuilder3::MapGrid: positions per cell in chain order */
+    v3 *map_pos;
+    int *map_start;
 };
 
 static v3 *alloc_v3(int n) { return (v3 *)calloc((size_t)(n > 0 ? n : 1), sizeof(v3)); }
@@ -706,6 +709,7 @@ void orc_destroy(orc_sim *s) {
     for (int b = 0; b < 2; b++) { free(s->head[b]); free(s->tail[b]); free(s->clen[b]); free(s->next[b]); }
     free(s->g.nbr); free(s->g.nbr_n); free(s->cell_of); free(s->bucket); free(s->bcount);
     free(s->bfull);
+    free(s->map_pos); free(s->map_start);
     free(s);
 }
 
@@ -1669,4 +1673,56 @@ void orc_shape_distance(const orc_shape *shape, int n, const double *pts, double
         distance[i] = shape_closest_distance(&s, p);
         inside[i] = shape_is_inside(&s, p);
     }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Continuous emission (src/core/grid.h:1289-1402)                                       */
+/* ------------------------------------------------------------------------------------ */
+void orc_map_grid(orc_sim *s) {
+    const int cur = s->active ? 1 : 0;
+    free(s->map_pos);
+    free(s->map_start);
+    s->map_pos = alloc_v3(s->n);
+    s->map_start = (int *)calloc((size_t)s->g.total + 1, sizeof(int));
+    int w = 0;
+    for (unsigned c = 0; c < s->g.total; c++) {
+        s->map_start[c] = w;
+        int node = s->head[cur][c];
+        for (int j = 0; j < s->clen[cur][c] && w < s->n; j++) {
+            s->map_pos[w++] = s->pos[node];
+            node = s->next[cur][node];
+        }
+    }
+    s->map_start[s->g.total] = w;
+}
+
+long orc_map_grid_emit(const orc_sim *s, double d, double *out, long capacity) {
+    if (!s->map_pos) return -1;
+    const int cur = s->active ? 1 : 0;
+    const Float dd = (Float)d;
+    long count = 0;
+    for (unsigned c = 0; c < s->g.total; c++) {
+        const int mapped = s->map_start[c + 1] - s->map_start[c];
+        if (mapped == 0) continue;
+        const int held = s->clen[cur][c];
+        if (held >= ORC_BUCKET) continue;
+        const int to_insert = ORC_BUCKET - held < mapped ? ORC_BUCKET - held : mapped;
+        for (int i = 0; i < to_insert; i++) {
+            const v3 pi = s->map_pos[s->map_start[c] + i];
+            int ok = 1;
+            int node = s->head[cur][c];
+            for (int j = 0; j < held && ok; j++) {
+                if (vlen(vsub(s->pos[node], pi)) < dd) ok = 0;
+                node = s->next[cur][node];
+            }
+            if (!ok) continue;
+            if (count < capacity) {
+                out[3 * count] = pi.x;
+                out[3 * count + 1] = pi.y;
+                out[3 * count + 2] = pi.z;
+            }
+            count++;
+        }
+    }
+    return count;
 }

@@ -169,6 +169,13 @@ int      orc_get_buckets(const orc_sim *s, int32_t *counts, int32_t *ids);
 size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, const double *rho,
                         double mass, double spacing, char *buf, size_t capacity);
 
+/* ContinuousParticleSetBuilder3::MapGrid (src/core/grid.h:1289-1321) on the simulation's
+ * current chains, and MapGridEmit (:1359-1402): the positions a refill would add, cells
+ * ascending, chain order (at most `capacity` stored; the count is returned, -1 without a
+ * map).  The oracle's particle arrays do not grow: the caller appends. */
+void     orc_map_grid(orc_sim *s);
+long     orc_map_grid_emit(const orc_sim *s, double distance, double *out, long capacity);
+
 /* Shape::ClosestDistance and IsInside of a box or sphere at n points (src/core/shape.cpp:
  * 206-232, 275-282): the values SetNodeSDFKernel (shape.cpp:409-424) signs into a field. */
 void     orc_shape_distance(const orc_shape *shape, int n, const double *pts, double *distance, int *inside);

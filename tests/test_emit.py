@@ -47,6 +47,21 @@ def test_oracle_emitter_is_the_reference():
         assert same_bits(p, g["pos_%d" % i]) and same_bits(v, g["vel_%d" % i]), i
 
 
+def test_oracle_map_grid_emit_is_the_reference():
+    """The oracle's MapGrid / MapGridEmit gives the positions the reference builder added."""
+    d = np.load(os.path.join(os.path.dirname(GOLDEN), "continuous_f32.npz"), allow_pickle=False)
+    sc = json.loads(str(d["scene"]))
+    for i, (cap, dist, _) in enumerate(json.loads(str(d["cases"]))):
+        o = O.OracleSim(sc, d["pos0"])
+        o.update_grid_distribution()
+        o.map_grid()
+        o.set(O.POSITION, d["pos1"])
+        new = o.map_grid_emit(dist)
+        k = min(len(new), cap - len(d["pos0"]))
+        assert same_bits(new[:k], d["pos_%d_0" % i][len(d["pos0"]):])
+        o.close()
+
+
 @pytest.mark.gpu
 def test_emit_matches_reference(gpu):
     g, cases = golden()
