@@ -17,6 +17,7 @@
 #include <new>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace bbg;
@@ -2321,15 +2322,37 @@ bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *e, int append, 
     const size_t P = (size_t)L.total;
     const bool jitter = max_jitter != 0.f;
     std::vector<float> off(jitter ? 3 * P : 0);
-    for (size_t t = 0; t < P; t++) {
-        const float u1 = rand_float();
-        const float u0 = rand_float();
-        if (!jitter) continue;
-        const float usqrt = 2 * std::sqrt(u1 * (1 - u1));
-        const float utheta = (float)(2 * 3.14159265358979323846 * (double)u0);
-        off[3 * t] = std::cos(utheta) * usqrt * max_jitter;
-        off[3 * t + 1] = std::sin(utheta) * usqrt * max_jitter;
-        off[3 * t + 2] = (1 - 2 * u1) * max_jitter;
+    if (!jitter) {
+        for (size_t t = 0; t < 2 * P; t++) (void)rand();   // the draws the reference makes anyway
+    } else {
+        // the draws are sequential; the offsets of disjoint point ranges are computed by
+        // the host's threads
+        for (size_t t = 0; t < P; t++) {
+            off[3 * t + 1] = rand_float();   // u[1]
+            off[3 * t] = rand_float();       // u[0]
+        }
+        auto sample_sphere = [&](size_t lo, size_t hi) {
+            for (size_t t = lo; t < hi; t++) {
+                const float u1 = off[3 * t + 1], u0 = off[3 * t];
+                const float usqrt = 2 * std::sqrt(u1 * (1 - u1));
+                const float utheta = (float)(2 * 3.14159265358979323846 * (double)u0);
+                off[3 * t] = std::cos(utheta) * usqrt * max_jitter;
+                off[3 * t + 1] = std::sin(utheta) * usqrt * max_jitter;
+                off[3 * t + 2] = (1 - 2 * u1) * max_jitter;
+            }
+        };
+        const size_t workers = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), 32));
+        if (workers == 1 || P < 65536) {
+            sample_sphere(0, P);
+        } else {
+            std::vector<std::thread> pool;
+            const size_t chunk = (P + workers - 1) / workers;
+            for (size_t w = 0; w < workers; w++) {
+                const size_t lo = w * chunk, hi = std::min(P, lo + chunk);
+                if (lo < hi) pool.emplace_back(sample_sphere, lo, hi);
+            }
+            for (auto &th : pool) th.join();
+        }
     }
     int count = 0;
     if (P > 0) {
