@@ -2518,6 +2518,49 @@ bbg_status attach_field(bbg_solver s, int index, const bbg_sdf_grid &g, float *v
     return BBG_OK;
 }
 
+// GenerateShapeSDF's grid over bounds [lo, hi] (shape.cpp:479-502): widened by margin x
+// extent, ceil(width / dx) cells across, cubic cells, in the reference's float operations.
+bbg_status field_grid_for(const float lo_in[3], const float hi_in[3], double dx, double margin, bbg_sdf_grid *g) {
+    const float mg = (float)margin;
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        const float scale = hi_in[k] - lo_in[k];
+        lo[k] = lo_in[k] - scale * mg;
+        hi[k] = hi_in[k] + scale * mg;
+    }
+    const float width = hi[0] - lo[0], height = hi[1] - lo[1], depth = hi[2] - lo[2];
+    const int res = (int)std::ceil(width / (float)dx);
+    if (!(width > 0) || res < 1 || res > 4096) return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d cells across", res);
+    const float cell = width / (float)res;
+    const int res_y = (int)std::ceil((float)res * height / width);
+    const int res_z = (int)std::ceil((float)res * depth / width);
+    if (res_y < 0 || res_z < 0 || res_y > 4096 || res_z > 4096)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d x %d x %d cells", res, res_y, res_z);
+    memset(g, 0, sizeof(*g));
+    g->nodes[0] = res + 1;
+    g->nodes[1] = res_y + 1;
+    g->nodes[2] = res_z + 1;
+    for (int k = 0; k < 3; k++) {
+        g->origin[k] = lo[k];
+        g->spacing[k] = cell;
+    }
+    return BBG_OK;
+}
+
+SdfDev field_dev(const bbg_sdf_grid &g, float *values) {
+    SdfDev d;
+    memset(&d, 0, sizeof(d));
+    d.v = values;
+    d.nx = g.nodes[0];
+    d.ny = g.nodes[1];
+    d.nz = g.nodes[2];
+    for (int k = 0; k < 3; k++) {
+        d.org[k] = (float)g.origin[k];
+        d.sp[k] = (float)g.spacing[k];
+    }
+    return d;
+}
+
 bbg_status check_field_target(bbg_solver s, int index) {
     if (bbg_status r = check_solver(s)) return r;
     if (s->nscenes > 0) return fail(BBG_ERR_STATE, "fields are not supported on a batch of scenes");
@@ -2553,48 +2596,20 @@ bbg_status bbg_collider_generate_sdf(bbg_solver s, int index, double dx, double 
     if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE)
         return fail(BBG_ERR_INVALID_ARGUMENT, "collider %d is not a box or a sphere", index);
     if (!(dx > 0) || !(margin >= 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need dx > 0 and margin >= 0");
-    // GetBounds of the translated object box, widened by margin x extent; the grid's
-    // resolution and spacing in the reference's float operations
+    // GetBounds of the translated object box
     const float h[3] = {sh.type == BBG_SHAPE_BOX ? sh.hx : sh.radius, sh.type == BBG_SHAPE_BOX ? sh.hy : sh.radius,
                         sh.type == BBG_SHAPE_BOX ? sh.hz : sh.radius};
-    const float mg = (float)margin;
     float lo[3], hi[3];
     for (int k = 0; k < 3; k++) {
         lo[k] = -h[k] + sh.t[k];
         hi[k] = h[k] + sh.t[k];
-        const float scale = hi[k] - lo[k];
-        lo[k] -= scale * mg;
-        hi[k] += scale * mg;
     }
-    const float width = hi[0] - lo[0], height = hi[1] - lo[1], depth = hi[2] - lo[2];
-    const int res = (int)std::ceil(width / (float)dx);
-    if (res < 1 || res > 4096) return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d cells across", res);
-    const float cell = width / (float)res;
-    const int res_y = (int)std::ceil((float)res * height / width);
-    const int res_z = (int)std::ceil((float)res * depth / width);
-    if (res_y < 0 || res_z < 0 || res_y > 4096 || res_z > 4096)
-        return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %d x %d x %d cells", res, res_y, res_z);
     bbg_sdf_grid g;
-    memset(&g, 0, sizeof(g));
-    g.nodes[0] = res + 1;
-    g.nodes[1] = res_y + 1;
-    g.nodes[2] = res_z + 1;
-    for (int k = 0; k < 3; k++) {
-        g.origin[k] = lo[k];
-        g.spacing[k] = cell;
-    }
+    if (bbg_status r = field_grid_for(lo, hi, dx, margin, &g)) return r;
     const size_t total = (size_t)g.nodes[0] * g.nodes[1] * g.nodes[2];
     float *d = nullptr;
     CK(cudaMalloc((void **)&d, sizeof(float) * total));
-    SdfDev gd;
-    gd.v = d;
-    gd.nx = g.nodes[0];
-    gd.ny = g.nodes[1];
-    gd.nz = g.nodes[2];
-    for (int k = 0; k < 3; k++) {
-        gd.org[k] = lo[k];
-        gd.sp[k] = cell;
-    }
+    const SdfDev gd = field_dev(g, d);
     launch_sdf_generate(sh, gd, float_above(1e-8), float_above(1e-6), d, s->stream);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -2654,5 +2669,105 @@ bbg_status bbg_collider_query(bbg_solver s, int index, int n, const float *point
         if (inside) inside[q] = r[11] != 0.f;
     }
     return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// the field of a triangle mesh (GenerateShapeSDF of a mesh shape)
+// ----------------------------------------------------------------------------
+namespace {
+
+// Node values of the mesh's field into device memory (*values, owned by the caller).
+bbg_status mesh_field(bbg_solver s, const float *vertices, int nv, const int *triangles, int nt, double dx,
+                      double margin, bbg_sdf_grid *g, float **values, int *stuck) {
+    if (!vertices || !triangles || nv < 3 || nt < 1) return fail(BBG_ERR_INVALID_ARGUMENT, "need a mesh");
+    if (!(dx > 0) || !(margin >= 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need dx > 0 and margin >= 0");
+    std::vector<float> tri(9 * (size_t)nt);
+    float lo[3] = {3.402823466e+38f, 3.402823466e+38f, 3.402823466e+38f};
+    float hi[3] = {-3.402823466e+38f, -3.402823466e+38f, -3.402823466e+38f};
+    for (int t = 0; t < nt; t++) {
+        for (int c = 0; c < 3; c++) {
+            const int v = triangles[3 * (size_t)t + c];
+            if (v < 0 || v >= nv) return fail(BBG_ERR_INVALID_ARGUMENT, "triangle %d: vertex %d out of range", t, v);
+            for (int k = 0; k < 3; k++) {
+                const float x = vertices[3 * (size_t)v + k];
+                if (!std::isfinite(x)) return fail(BBG_ERR_INVALID_ARGUMENT, "vertex %d is not finite", v);
+                tri[9 * (size_t)t + 3 * c + k] = x;
+                // the BVH root bound: the union of the triangles' bounds
+                lo[k] = x < lo[k] ? x : lo[k];
+                hi[k] = x > hi[k] ? x : hi[k];
+            }
+        }
+    }
+    if (bbg_status r = field_grid_for(lo, hi, dx, margin, g)) return r;
+    g->bounded = 1;
+    for (int k = 0; k < 3; k++) {
+        g->bounds_min[k] = lo[k];
+        g->bounds_max[k] = hi[k];
+    }
+    // gamma(n) = n eps / (1 - n eps) with the reference's MachineEpsilon, in double
+    float gam[4];
+    const int ns[4] = {2, 3, 5, 7};
+    for (int q = 0; q < 4; q++)
+        gam[q] = (float)(((double)(float)ns[q] * 5.96046e-08) / (1 - (double)(float)ns[q] * 5.96046e-08));
+    const size_t total = (size_t)g->nodes[0] * g->nodes[1] * g->nodes[2];
+    float *d_tri = nullptr, *d_out = nullptr;
+    unsigned *d_stuck = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_tri, sizeof(float) * tri.size());
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, sizeof(float) * total);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_stuck, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_tri, tri.data(), sizeof(float) * tri.size(), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_stuck, 0, sizeof(unsigned), s->stream);
+    unsigned h_stuck = 0;
+    if (e == cudaSuccess) {
+        launch_mesh_sdf(d_tri, nt, field_dev(*g, d_out), lo, hi, gam, d_out, d_stuck, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_stuck, d_stuck, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_tri);
+    cudaFree(d_stuck);
+    if (e != cudaSuccess) {
+        cudaFree(d_out);
+        return fail(BBG_ERR_CUDA, "mesh field: %s", cudaGetErrorString(e));
+    }
+    if (stuck) *stuck = (int)h_stuck;
+    *values = d_out;
+    return BBG_OK;
+}
+
+}  // namespace
+
+bbg_status bbg_mesh_sdf(bbg_solver s, const float *vertices, int nv, const int *triangles, int nt, double dx,
+                        double margin, bbg_sdf_grid *grid, float *values, size_t capacity, size_t *count,
+                        int *stuck) {
+    if (bbg_status r = check_solver(s)) return r;
+    bbg_sdf_grid g;
+    float *d = nullptr;
+    if (bbg_status r = mesh_field(s, vertices, nv, triangles, nt, dx, margin, &g, &d, stuck)) return r;
+    const size_t total = (size_t)g.nodes[0] * g.nodes[1] * g.nodes[2];
+    if (grid) *grid = g;
+    if (count) *count = total;
+    bbg_status r = BBG_OK;
+    if (values) {
+        if (capacity < total) {
+            r = fail(BBG_ERR_CAPACITY, "the field has %zu nodes", total);
+        } else {
+            const cudaError_t e = cudaMemcpy(values, d, sizeof(float) * total, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) r = fail(BBG_ERR_CUDA, "mesh field: %s", cudaGetErrorString(e));
+        }
+    }
+    cudaFree(d);
+    return r;
+}
+
+bbg_status bbg_collider_set_mesh(bbg_solver s, int index, const float *vertices, int nv, const int *triangles,
+                                 int nt, double dx, double margin) {
+    if (bbg_status r = check_field_target(s, index)) return r;
+    if (s->P.shapes[index].type != BBG_SHAPE_SDF)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "collider %d is not a field-only (BBG_SHAPE_SDF) collider", index);
+    bbg_sdf_grid g;
+    float *d = nullptr;
+    if (bbg_status r = mesh_field(s, vertices, nv, triangles, nt, dx, margin, &g, &d, nullptr)) return r;
+    return attach_field(s, index, g, d);
 }
 

@@ -104,4 +104,9 @@ void launch_sdf_generate(const ShapeDev &shape, const SdfDev &g, float iz, float
 // Shape queries of collider `index` at n points (xyz); 14 floats per point out (sdf.cu)
 void launch_shape_query(const Params &P, int index, int n, const float *pts, float *out, cudaStream_t s);
 
+// GenerateShapeSDF of a triangle mesh (9 floats per triangle) into g's node values; stuck
+// counts rays that gave up (mesh.cu)
+void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo[3], const float hi[3],
+                     const float gamma[4], float *out, unsigned *stuck, cudaStream_t s);
+
 }  // namespace bbg

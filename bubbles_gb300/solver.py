@@ -173,6 +173,28 @@ class Solver:
         """GenerateShapeSDF of a box or sphere collider on the device (attached to it)."""
         N.call("bbg_collider_generate_sdf", self.h, int(index), float(dx), float(margin))
 
+    def mesh_sdf(self, vertices, triangles, dx=0.01, margin=0.1):
+        """GenerateShapeSDF of a triangle mesh on the device: (nodes, origin, spacing, values,
+        bounds, stuck rays)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        g = N.SdfGrid()
+        cnt = ctypes.c_size_t()
+        stuck = ctypes.c_int()
+        args = (self.h, v.ctypes.data, len(v), t.ctypes.data, len(t), float(dx), float(margin), ctypes.byref(g))
+        N.call("bbg_mesh_sdf", *args, None, 0, ctypes.byref(cnt), ctypes.byref(stuck))
+        vals = np.empty(cnt.value, np.float32)
+        N.call("bbg_mesh_sdf", *args, vals.ctypes.data, vals.size, ctypes.byref(cnt), ctypes.byref(stuck))
+        return (np.array(g.nodes[:]), np.array(g.origin[:]), np.array(g.spacing[:]), vals,
+                (np.array(g.bounds_min[:]), np.array(g.bounds_max[:])), stuck.value)
+
+    def set_mesh_collider(self, index, vertices, triangles, dx=0.01, margin=0.1):
+        """A field-only collider `index` becomes the mesh (its field generated on the device)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        N.call("bbg_collider_set_mesh", self.h, int(index), v.ctypes.data, len(v), t.ctypes.data, len(t),
+               float(dx), float(margin))
+
     def get_sdf(self, index):
         """(nodes, origin, spacing, values) of collider `index`'s field."""
         g = N.SdfGrid()

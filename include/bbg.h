@@ -302,6 +302,21 @@ bbg_status bbg_collider_set_sdf(bbg_solver s, int index, const bbg_sdf_grid *gri
  * to max(|ClosestDistance|, 1e-5) signed by IsInside; the field is attached to the
  * collider.  Reference defaults: dx 0.01, margin 0.1. */
 bbg_status bbg_collider_generate_sdf(bbg_solver s, int index, double dx, double margin);
+/* GenerateShapeSDF of a triangle mesh (MakeMesh + GenerateShapeSDF, src/shapes/bvh.cpp:51-56,
+ * src/core/shape.cpp:479-510) on the device: vertices xyz (nv), triangles as vertex index
+ * triples (nt).  The grid covers the mesh bounds widened by margin x extent; a node holds
+ * max(least DistanceTriangle, 1e-5) (bvh.cpp:212-242), negative when a ray towards the
+ * bounds' centre crosses the mesh an odd number of times (MeshIsPointInside,
+ * shape.cpp:349-369, with the reference's watertight ray-triangle test and ray re-spawning).
+ * Values equal the reference's except where two triangles tie for a closest hit.  *stuck
+ * counts rays that met more than 256 surfaces (counted outside). */
+bbg_status bbg_mesh_sdf(bbg_solver s, const float *vertices, int nv, const int *triangles, int nt,
+                        double dx, double margin, bbg_sdf_grid *grid, float *values, size_t capacity,
+                        size_t *count, int *stuck);
+/* The same field attached to a BBG_SHAPE_SDF collider as a mesh's (bounded by the mesh):
+ * MakeCollider3 of a mesh shape, which generates its field (src/core/collider.cpp:340-348). */
+bbg_status bbg_collider_set_mesh(bbg_solver s, int index, const float *vertices, int nv, const int *triangles,
+                                 int nt, double dx, double margin);
 /* A collider's field: its grid, and its values when capacity (in floats) suffices;
  * *count = node count. */
 bbg_status bbg_collider_get_sdf(bbg_solver s, int index, bbg_sdf_grid *grid, float *values, size_t capacity,

@@ -16,6 +16,7 @@
 #include <util.h>
 
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "../sph_oracle.h"
@@ -305,6 +306,37 @@ void ref_make_sdf_sphere_collider(RefSim *s, int i, const double *center, double
     s->cs->colliders[i]->shape = MakeSDFShape(b, [c, r](const vec3f &p, Shape *, int) -> Float {
         return Distance(p, c) - r;
     }, (Float)dx, (Float)margin);
+}
+
+/* MakeMesh of a triangle mesh (vertices xyz, triangles as vertex index triples) with an
+ * identity transform, then GenerateShapeSDF(shape, dx, margin): the grid and up to
+ * `capacity` node values (x fastest).  Returns the node count. */
+int ref_mesh_sdf(const double *verts, int nv, const int *tris, int nt, double dx, double margin, int *nodes,
+                 double *origin, double *spacing, float *values, int capacity) {
+    ParsedMesh *mesh = new ParsedMesh();
+    mesh->p = new Point3f[(size_t)nv];
+    mesh->indices = new Point3i[3 * (size_t)nt];
+    for (int i = 0; i < nv; i++) mesh->p[i] = Point3f((Float)verts[3 * i], (Float)verts[3 * i + 1], (Float)verts[3 * i + 2]);
+    for (int i = 0; i < 3 * nt; i++) mesh->indices[i] = Point3i(tris[i], -1, -1);
+    mesh->nTriangles = nt;
+    mesh->nVertices = nv;
+    mesh->nUvs = 0;
+    mesh->nNormals = 0;
+    mesh->n = nullptr;
+    mesh->s = nullptr;
+    mesh->uv = nullptr;
+    strcpy(mesh->name, "mesh");
+    Shape *shape = MakeMesh(mesh, Transform(), false);
+    GenerateShapeSDF(shape, (Float)dx, (Float)margin);
+    FieldGrid3f *g = shape->grid;
+    for (int k = 0; k < 3; k++) {
+        nodes[k] = (int)g->resolution[k];
+        origin[k] = g->minPoint[k];
+        spacing[k] = g->spacing[k];
+    }
+    const int total = (int)g->total;
+    for (int q = 0; q < total && q < capacity; q++) values[q] = (float)g->field[q];
+    return total;
 }
 
 /* Collider i's field: nodes, origin, spacing; up to `capacity` values (x fastest). */

@@ -52,6 +52,8 @@ def load(variant):
                                                 ctypes.c_double]),
         "ref_collider_sdf": (ctypes.c_int, [_P, ctypes.c_int, _I32, _D, _D, ctypes.POINTER(ctypes.c_float),
                                             ctypes.c_int]),
+        "ref_mesh_sdf": (ctypes.c_int, [_D, ctypes.c_int, _I32, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
         "ref_sdf_probe": (None, [_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, _I32]),
         "ref_map_grid_emit": (ctypes.c_int, [_P, ctypes.c_double, _D]),
         "ref_destroy": (None, [_P]),
@@ -234,4 +236,20 @@ def emit_volume(shape, spacing, jitter=0.0, velocity=(0.0, 0.0, 0.0), max_partic
                             int(max_particles), int(seed), pos.ctypes.data_as(_D), vel.ctypes.data_as(_D),
                             capacity)
     return pos[:min(n, capacity)], vel[:min(n, capacity)]
+
+
+def mesh_sdf(vertices, triangles, dx, margin, variant="f32"):
+    """MakeMesh + GenerateShapeSDF of the reference: (nodes, origin, spacing, values)."""
+    lib = load(variant)
+    v = np.ascontiguousarray(vertices, np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    nodes = np.zeros(3, np.int32)
+    org = np.zeros(3)
+    sp = np.zeros(3)
+    args = (v.ctypes.data_as(_D), len(v), t.ctypes.data_as(_I32), len(t), float(dx), float(margin),
+            nodes.ctypes.data_as(_I32), org.ctypes.data_as(_D), sp.ctypes.data_as(_D))
+    n = lib.ref_mesh_sdf(*args, None, 0)
+    vals = np.zeros(n, np.float32)
+    lib.ref_mesh_sdf(*args, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n)
+    return nodes, org, sp, vals
 

@@ -28,6 +28,9 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   its grid, FieldGrid3f::Sample / Gradient, Shape::ClosestPoint and IsInside
                   at probe points, and TimeIntegrationCPU's collision response of 4,000
                   particles driven into the walls and the field.
+  mesh_f32.npz    GenerateShapeSDF of two triangle meshes (MakeMesh, shapes/bvh.cpp): a rotated
+                  icosphere and a rotated torus (rays cross it up to four times), their
+                  vertices and triangles beside the reference's grids and node values.
   emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
                   srand(seed) for boxes and spheres, with and without jitter, explicit
                   bounds, a reversed box and a binding max_particles (EMIT_CASES).
@@ -37,6 +40,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py emit      # emit_f32.npz only
     python tests/golden/make_golden.py continuous    # continuous_f32.npz only
     python tests/golden/make_golden.py sdf       # sdf_f32.npz only
+    python tests/golden/make_golden.py mesh      # mesh_f32.npz only
 """
 import json
 import os
@@ -218,6 +222,72 @@ def make_sdf():
     np.savez_compressed(os.path.join(HERE, "sdf_f32.npz"), **out)
 
 
+def rotation(ax, ay, az):
+    rx = np.array([[1, 0, 0], [0, np.cos(ax), -np.sin(ax)], [0, np.sin(ax), np.cos(ax)]])
+    ry = np.array([[np.cos(ay), 0, np.sin(ay)], [0, 1, 0], [-np.sin(ay), 0, np.cos(ay)]])
+    rz = np.array([[np.cos(az), -np.sin(az), 0], [np.sin(az), np.cos(az), 0], [0, 0, 1]])
+    return rz @ ry @ rx
+
+
+def icosphere(radius=0.2, center=(0.03, -0.02, 0.01), level=2, rot=(0.3, 0.5, 0.7)):
+    """A subdivided icosahedron on a sphere, rotated off the axes (float32 vertices)."""
+    t = (1 + 5 ** 0.5) / 2
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = [np.array(x, float) / np.linalg.norm(x) for x in v]
+    for _ in range(level):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = v[a] + v[b]
+                v.append(m / np.linalg.norm(m))
+                cache[key] = len(v) - 1
+            return cache[key]
+        nf = []
+        for a, b, c in f:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = nf
+    verts = np.array(v) @ rotation(*rot).T * radius + np.array(center)
+    return verts.astype(np.float32).astype(np.float64), np.array(f, np.int32)
+
+
+def torus(big=0.18, small=0.06, nu=24, nv=12, center=(-0.01, 0.02, 0.015), rot=(0.9, 0.2, 0.4)):
+    """A rotated torus of nu x nv quads split into triangles (float32 vertices)."""
+    verts, tris = [], []
+    for i in range(nu):
+        for j in range(nv):
+            u, w = 2 * np.pi * i / nu, 2 * np.pi * j / nv
+            verts.append(((big + small * np.cos(w)) * np.cos(u), (big + small * np.cos(w)) * np.sin(u),
+                          small * np.sin(w)))
+    for i in range(nu):
+        for j in range(nv):
+            a, b = i * nv + j, ((i + 1) % nu) * nv + j
+            c, d = ((i + 1) % nu) * nv + (j + 1) % nv, i * nv + (j + 1) % nv
+            tris += [(a, b, c), (a, c, d)]
+    verts = np.array(verts) @ rotation(*rot).T + np.array(center)
+    return verts.astype(np.float32).astype(np.float64), np.array(tris, np.int32)
+
+
+MESH_CASES = {"icosphere": (icosphere, 0.02, 0.1), "torus": (torus, 0.015, 0.15)}
+
+
+def make_mesh():
+    out = {}
+    for name, (make, dx, margin) in MESH_CASES.items():
+        v, t = make()
+        nodes, org, sp, vals = R.mesh_sdf(v, t, dx, margin)
+        out.update({name + "_vertices": v, name + "_triangles": t, name + "_dx": np.array(dx),
+                    name + "_margin": np.array(margin), name + "_nodes": nodes, name + "_origin": org,
+                    name + "_spacing": sp, name + "_values": vals})
+    np.savez_compressed(os.path.join(HERE, "mesh_f32.npz"), **out)
+
+
 # continuous emission cases: builder capacity, MapGridEmit distance, velocity
 CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
 
@@ -259,4 +329,6 @@ if __name__ == "__main__":
         make_continuous()
     if not what or what == ["sdf"]:
         make_sdf()
+    if not what or what == ["mesh"]:
+        make_mesh()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
