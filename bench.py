@@ -405,6 +405,29 @@ def seeding(bb, scene, final_pos, device, reps=3):
     o.close()
     out["map_grid_emit"] = {"particles": n, "added": added, "ms": 1e3 * gpu, "cpu_ms": 1e3 * cpu,
                             "cpu_kind": "port", "cpu_cores": 1, "same_as_oracle": bool(len(ref) == added)}
+    # GenerateShapeSDF of a triangle mesh: a torus of 1,152 triangles on a grid of 0.55M nodes
+    nu, nv = 32, 18
+    u, w = np.meshgrid(2 * np.pi * np.arange(nu) / nu, 2 * np.pi * np.arange(nv) / nv, indexing="ij")
+    big, small = 0.3, 0.1
+    verts = np.stack([(big + small * np.cos(w)) * np.cos(u), (big + small * np.cos(w)) * np.sin(u),
+                      small * np.sin(w)], axis=-1).reshape(-1, 3).astype(np.float32)
+    tris = []
+    for i in range(nu):
+        for j in range(nv):
+            a, b = i * nv + j, ((i + 1) % nu) * nv + j
+            c, d = ((i + 1) % nu) * nv + (j + 1) % nv, i * nv + (j + 1) % nv
+            tris += [(a, b, c), (a, c, d)]
+    s2 = bb.Solver(dict(scene), capacity=16, device=device)
+    s2.upload(final_pos[:16])
+    t = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        nodes, _, _, vals, _, stuck = s2.mesh_sdf(verts, np.array(tris, np.int32), dx=0.0075, margin=0.1)
+        t.append(time.perf_counter() - t0)
+    s2.close()
+    out["mesh_sdf"] = {"triangles": len(tris), "nodes": int(np.prod(nodes)), "ms": 1e3 * min(t),
+                       "inside_nodes": int((vals < 0).sum()), "stuck_rays": stuck,
+                       "note": "brute force over all triangles per node (distance and each ray pass)"}
     out["measured"] = "host wall clock around the C-ABI calls (single call; emitter median of %d)" % reps
     return out
 
