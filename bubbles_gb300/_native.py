@@ -194,6 +194,7 @@ SIGNATURES = {
     "bbg_emitter_desc_default": [ctypes.POINTER(EmitterDesc)],
     "bbg_emit_volume": [_P, ctypes.POINTER(EmitterDesc), _I, _IP],
     "bbg_map_grid": [_P, _IP],
+    "bbg_lnm_boundary": [_P, ctypes.c_double, _I, ctypes.c_void_p],
     "bbg_collider_set_sdf": [_P, _I, ctypes.POINTER(SdfGrid), ctypes.c_void_p],
     "bbg_collider_generate_sdf": [_P, _I, ctypes.c_double, ctypes.c_double],
     "bbg_collider_get_sdf": [_P, _I, ctypes.POINTER(SdfGrid), ctypes.c_void_p, ctypes.c_size_t,

@@ -2771,3 +2771,32 @@ bbg_status bbg_collider_set_mesh(bbg_solver s, int index, const float *vertices,
     return attach_field(s, index, g, d);
 }
 
+// ----------------------------------------------------------------------------
+// boundary classification: LNMBoundary (src/boundaries/lnm.h:245-275)
+// ----------------------------------------------------------------------------
+bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!levels || !(h > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need h > 0 and an output");
+    if (!s->setup_done || s->n <= 0) return fail(BBG_ERR_STATE, "no particles set up");
+    if (!s->grid_valid)   // the reference classifies the grid's distribution: make one
+        if (bbg_status r = grid_update(s)) return r;
+    // LNMComputeDelta: (min cell length / h)^dim as a float power, truncated to int
+    const float *len = s->P.g.len;
+    const float minlen = len[0] < len[1] ? (len[0] < len[2] ? len[0] : len[2]) : (len[1] < len[2] ? len[1] : len[2]);
+    const float pd = std::pow(minlen / (float)h, 3.0f);
+    const int delta = (!unbounded && pd > 0) ? (int)pd : 0x7fffffff;
+    int *d_level = nullptr, *d_out = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_level, sizeof(int) * ((size_t)s->P.g.total + 1));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, sizeof(int) * (size_t)s->n);
+    if (e == cudaSuccess) {
+        launch_lnm(s->P.g, s->B.start, s->B.cell, s->B.pid[s->pid_cur], s->n, delta, d_level, d_out, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(levels, d_out, sizeof(int) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_level);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "LNM boundary: %s", cudaGetErrorString(e));
+    return BBG_OK;
+}
+

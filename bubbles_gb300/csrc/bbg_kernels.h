@@ -109,4 +109,9 @@ void launch_shape_query(const Params &P, int index, int n, const float *pts, flo
 void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo[3], const float hi[3],
                      const float gamma[4], float *out, unsigned *stuck, cudaStream_t s);
 
+// LNM boundary levels (1, 2, 0) of n sorted slots into out (caller order through pid);
+// level: one int per cell (boundary.cu)
+void launch_lnm(const GridDev &g, const unsigned *start, const unsigned *cell, const int *pid, int n, int delta,
+                int *level, int *out, cudaStream_t s);
+
 }  // namespace bbg

@@ -218,6 +218,12 @@ class Solver:
                out["distance"].ctypes.data, out["inside"].ctypes.data)
         return out
 
+    def lnm_boundary(self, h, unbounded=False):
+        """LNMBoundary: each particle's level (1, 2, 0 inside), caller order."""
+        out = np.zeros(self.n, np.int32)
+        N.call("bbg_lnm_boundary", self.h, float(h), int(bool(unbounded)), out.ctypes.data)
+        return out
+
     def map_grid(self):
         """ContinuousParticleSetBuilder3::MapGrid: remember the occupied cells' positions."""
         out = ctypes.c_int()

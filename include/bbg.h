@@ -372,6 +372,14 @@ bbg_status bbg_emit_volume(bbg_solver s, const bbg_emitter_desc *desc, int appen
 bbg_status bbg_map_grid(bbg_solver s, int *mapped);
 bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocity[3], int *emitted);
 
+/* ----- boundary classification (LNM) ---------------------------------------------- */
+/* LNMBoundary, fast variant (src/boundaries/lnm.h:24-139, 245-275) on the grid's last
+ * distribution (one is made first when there is none): levels[i] of each particle (caller
+ * order) is 1 when its cell lies on the grid's border or next to an empty cell, 2 when its
+ * cell is next to a level-1 cell holding at most delta = (min cell length / h)^3 particles
+ * (any number when unbounded), else 0.  One thread per cell, then one per particle. */
+bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

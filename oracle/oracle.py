@@ -114,6 +114,7 @@ def load(variant="f32"):
         "orc_set_higher_level": (None, [_P, ctypes.c_int]),
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
+        "orc_lnm": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
         "orc_map_grid": (None, [_P]),
         "orc_map_grid_emit": (ctypes.c_long, [_P, ctypes.c_double, _D, ctypes.c_long]),
         "orc_shape_distance": (None, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, _I32]),
@@ -285,6 +286,12 @@ class OracleSim:
         return self.lib.orc_advance_sph(self.h, dt, int(inplace))
 
     # --- fields ---------------------------------------------------------------
+    def lnm(self, h, unbounded=False):
+        """LNMBoundary's particle levels (1, 2, 0 inside) on the current chains."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.orc_lnm(self.h, float(h), int(bool(unbounded)), _ptr(out, _I32))
+        return out
+
     def map_grid(self):
         """ContinuousParticleSetBuilder3::MapGrid on the current chains."""
         self.lib.orc_map_grid(self.h)

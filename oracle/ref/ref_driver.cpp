@@ -6,6 +6,7 @@
  */
 #include <collider.h>
 #include <emitter.h>
+#include <lnm.h>
 #include <cutil.h>
 #include <interaction.h>
 #include <pcisph_solver.h>
@@ -372,6 +373,15 @@ void ref_sdf_probe(RefSim *s, int i, int n, const double *pts, double *sample, d
         cd[q] = cq.signedDistance;
         inside[q] = shape->IsInside(p) ? 1 : 0;
     }
+}
+
+/* LNMBoundary (src/boundaries/lnm.h:245-275, the fast variant) on the grid's current
+ * chains with v0 reset to 0 first: each particle's level (1, 2, or 0 inside). */
+void ref_lnm(RefSim *s, double h, int unbounded, int *levels) {
+    for (int i = 0; i < s->n; i++) s->pSet->SetParticleV0(i, 0);
+    s->grid->UpdateQueryState();
+    LNMBoundary(s->pSet, s->grid, (Float)h, 0, nullptr, unbounded != 0);
+    for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
 }
 
 /* SerializerLoadParticles3 on a frame file: the first fluid section's particles (at most

@@ -52,6 +52,7 @@ def load(variant):
                                                 ctypes.c_double]),
         "ref_collider_sdf": (ctypes.c_int, [_P, ctypes.c_int, _I32, _D, _D, ctypes.POINTER(ctypes.c_float),
                                             ctypes.c_int]),
+        "ref_lnm": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
         "ref_mesh_sdf": (ctypes.c_int, [_D, ctypes.c_int, _I32, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
         "ref_sdf_probe": (None, [_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, _I32]),
@@ -137,6 +138,12 @@ class RefSim:
                                out["gradient"].ctypes.data_as(_D), out["point"].ctypes.data_as(_D),
                                out["normal"].ctypes.data_as(_D), out["distance"].ctypes.data_as(_D),
                                out["inside"].ctypes.data_as(_I32))
+        return out
+
+    def lnm(self, h, unbounded=False):
+        """LNMBoundary's particle levels (1, 2, 0 inside) on the current chains."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.ref_lnm(self.h, float(h), int(bool(unbounded)), out.ctypes.data_as(_I32))
         return out
 
     def map_grid_emit(self, d, velocity=(0.0, 0.0, 0.0)):

@@ -1726,3 +1726,53 @@ long orc_map_grid_emit(const orc_sim *s, double d, double *out, long capacity) {
     }
     return count;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* LNM boundary classification, fast variant (src/boundaries/lnm.h:24-33, 96-139, 245-275) */
+/* ------------------------------------------------------------------------------------ */
+void orc_lnm(const orc_sim *s, double h, int unbounded, int *levels) {
+    const int cur = s->active ? 1 : 0;
+    const unsigned total = s->g.total;
+    int *level = (int *)malloc(sizeof(int) * (total ? total : 1));
+    for (unsigned c = 0; c < total; c++) level[c] = -1;   /* UpdateQueryState */
+    /* LNMComputeDelta: (min cell length / h)^3 as a float power, truncated to int */
+    Float minlen = s->g.len[0] < s->g.len[1] ? s->g.len[0] : s->g.len[1];
+    minlen = minlen < s->g.len[2] ? minlen : s->g.len[2];
+    const float pd = powf((float)minlen / (float)h, 3.0f);
+    const int delta = (!unbounded && pd > 0) ? (int)pd : 2147483647;
+    /* L1: a cell with particles on the grid's border or next to an empty cell */
+    for (unsigned c = 0; c < total; c++) {
+        if (s->clen[cur][c] < 1) continue;
+        const int cnt = s->g.nbr_n[c];
+        if (cnt != 27) {
+            level[c] = 1;
+            continue;
+        }
+        for (int k = 0; k < cnt; k++)
+            if (s->clen[cur][s->g.nbr[27 * (size_t)c + k]] == 0) {
+                level[c] = 1;
+                break;
+            }
+    }
+    /* L2: a cell with particles next to an L1 cell holding at most delta particles */
+    for (unsigned c = 0; c < total; c++) {
+        if (s->clen[cur][c] < 1 || level[c] == 1) continue;
+        for (int k = 0; k < s->g.nbr_n[c]; k++) {
+            const int nb = s->g.nbr[27 * (size_t)c + k];
+            if (level[nb] == 1 && s->clen[cur][nb] <= delta) {
+                level[c] = 2;
+                break;
+            }
+        }
+    }
+    for (int i = 0; i < s->n; i++) levels[i] = 0;
+    for (unsigned c = 0; c < total; c++) {
+        if (level[c] != 1 && level[c] != 2) continue;
+        int node = s->head[cur][c];
+        for (int j = 0; j < s->clen[cur][c]; j++) {
+            levels[node] = level[c];
+            node = s->next[cur][node];
+        }
+    }
+    free(level);
+}

@@ -176,6 +176,12 @@ size_t   orc_frame_text(int n, int flags, const double *pos, const double *vel, 
 void     orc_map_grid(orc_sim *s);
 long     orc_map_grid_emit(const orc_sim *s, double distance, double *out, long capacity);
 
+/* LNMBoundary, fast variant (src/boundaries/lnm.h:245-275) on the current chains: each
+ * particle's level, 1 (a cell on the grid's border or next to an empty cell), 2 (next to
+ * an L1 cell holding at most delta = (min cell length / h)^3 particles; unbounded: any)
+ * or 0. */
+void     orc_lnm(const orc_sim *s, double h, int unbounded, int *levels);
+
 /* Shape::ClosestDistance and IsInside of a box or sphere at n points (src/core/shape.cpp:
  * 206-232, 275-282): the values SetNodeSDFKernel (shape.cpp:409-424) signs into a field. */
 void     orc_shape_distance(const orc_shape *shape, int n, const double *pts, double *distance, int *inside);

@@ -31,6 +31,9 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
   mesh_f32.npz    GenerateShapeSDF of two triangle meshes (MakeMesh, shapes/bvh.cpp): a rotated
                   icosphere and a rotated torus (rays cross it up to four times), their
                   vertices and triangles beside the reference's grids and node values.
+  lnm_f32.npz     LNMBoundary (boundaries/lnm.h, fast variant) levels of the 1,440-particle
+                  scene after 3 as-shipped substeps and a fresh grid distribution, for
+                  h = 0.01, 0.02, 0.04 and unbounded.
   emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
                   srand(seed) for boxes and spheres, with and without jitter, explicit
                   bounds, a reversed box and a binding max_particles (EMIT_CASES).
@@ -41,6 +44,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py continuous    # continuous_f32.npz only
     python tests/golden/make_golden.py sdf       # sdf_f32.npz only
     python tests/golden/make_golden.py mesh      # mesh_f32.npz only
+    python tests/golden/make_golden.py lnm       # lnm_f32.npz only
 """
 import json
 import os
@@ -288,6 +292,22 @@ def make_mesh():
     np.savez_compressed(os.path.join(HERE, "mesh_f32.npz"), **out)
 
 
+LNM_CASES = [(0.01, 0), (0.02, 0), (0.04, 0), (0.02, 1)]
+
+
+def make_lnm():
+    sc, p0 = pcisph_scene()
+    r = R.RefSim(sc, p0)
+    for _ in range(3):
+        r.advance_time_step(sc["dt"])
+    r.update_grid_distribution()
+    out = {"scene": np.array(json.dumps(clean(sc))), "pos": r.get(O.POSITION),
+           "cases": np.array(json.dumps(LNM_CASES))}
+    for i, (h, unbounded) in enumerate(LNM_CASES):
+        out["levels_%d" % i] = r.lnm(h, unbounded)
+    np.savez_compressed(os.path.join(HERE, "lnm_f32.npz"), **out)
+
+
 # continuous emission cases: builder capacity, MapGridEmit distance, velocity
 CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
 
@@ -331,4 +351,6 @@ if __name__ == "__main__":
         make_sdf()
     if not what or what == ["mesh"]:
         make_mesh()
+    if not what or what == ["lnm"]:
+        make_lnm()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
