@@ -202,6 +202,9 @@ SIGNATURES = {
     "bbg_mesh_sdf": [_P, ctypes.c_void_p, _I, ctypes.c_void_p, _I, ctypes.c_double, ctypes.c_double,
                      ctypes.POINTER(SdfGrid), ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), _IP],
     "bbg_collider_set_mesh": [_P, _I, ctypes.c_void_p, _I, ctypes.c_void_p, _I, ctypes.c_double, ctypes.c_double],
+    "bbg_marching_cubes": [_P, ctypes.POINTER(SdfGrid), ctypes.c_void_p, ctypes.c_double, _I, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                           ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)],
     "bbg_collider_query": [_P, _I, _I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "bbg_map_grid_emit": [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _IP],

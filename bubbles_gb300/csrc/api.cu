@@ -2800,3 +2800,72 @@ bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels) 
     return BBG_OK;
 }
 
+// ----------------------------------------------------------------------------
+// marching cubes (MarchingCubes, src/reconstruction/marching_cubes.cpp:204-457)
+// ----------------------------------------------------------------------------
+bbg_status bbg_marching_cubes(bbg_solver s, const bbg_sdf_grid *grid, const float *values, double iso,
+                              int rotate_faces, float *points, float *normals, size_t point_capacity,
+                              int *triangles, size_t triangle_capacity, size_t *npoints, size_t *ntriangles) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!grid || !values) return fail(BBG_ERR_INVALID_ARGUMENT, "null grid or values");
+    for (int k = 0; k < 3; k++)
+        if (grid->nodes[k] < 2 || !(grid->spacing[k] > 0))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "a field needs >= 2 nodes and spacing > 0 per axis");
+    const long long nodes = (long long)grid->nodes[0] * grid->nodes[1] * grid->nodes[2];
+    const long long cubes = (long long)(grid->nodes[0] - 1) * (grid->nodes[1] - 1) * (grid->nodes[2] - 1);
+    if (3 * nodes >= (1ll << 31)) return fail(BBG_ERR_CAPACITY, "the field has %lld nodes", nodes);
+    CK(mc_prepare());
+    McInput in;
+    in.nodes[0] = grid->nodes[0];
+    in.nodes[1] = grid->nodes[1];
+    in.nodes[2] = grid->nodes[2];
+    for (int k = 0; k < 3; k++) {
+        in.origin[k] = (float)grid->origin[k];
+        in.spacing[k] = (float)grid->spacing[k];
+        in.inv[k] = (float)(1.0 / (double)in.spacing[k]);   // invGridSize
+    }
+    in.iso = (float)iso;
+    float *d_vals = nullptr, *d_pts = nullptr, *d_nrm = nullptr;
+    int *d_tri = nullptr;
+    unsigned *b[7] = {};
+    const size_t sz[7] = {(size_t)cubes + 1, (size_t)cubes + 1, scan_partials_needed((unsigned)(cubes + 1)),
+                          (size_t)(3 * nodes) + 1, (size_t)(3 * nodes) + 1, (size_t)(3 * nodes) + 1,
+                          scan_partials_needed((unsigned)(3 * nodes + 1))};
+    cudaError_t e = cudaMalloc((void **)&d_vals, sizeof(float) * (size_t)nodes);
+    for (int q = 0; q < 7 && e == cudaSuccess; q++) e = cudaMalloc((void **)&b[q], sizeof(unsigned) * sz[q]);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_vals, values, sizeof(float) * (size_t)nodes, cudaMemcpyHostToDevice, s->stream);
+    in.values = d_vals;
+    size_t ntri = 0, nvert = 0;
+    unsigned *h = s->h_u;
+    if (e == cudaSuccess) e = mc_count(in, b[0], b[1], b[2], b[3], b[4], b[5], b[6], h, &ntri, &nvert, s->stream);
+    bbg_status r = BBG_OK;
+    if (e != cudaSuccess) {
+        r = fail(BBG_ERR_CUDA, "marching cubes: %s", cudaGetErrorString(e));
+    } else {
+        if (npoints) *npoints = nvert;
+        if (ntriangles) *ntriangles = ntri;
+        if (!points || !normals || !triangles || point_capacity < nvert || triangle_capacity < ntri) {
+            r = fail(BBG_ERR_CAPACITY, "the mesh has %zu points and %zu triangles", nvert, ntri);
+        } else {
+            e = cudaMalloc((void **)&d_pts, sizeof(float) * 3 * (nvert ? nvert : 1));
+            if (e == cudaSuccess) e = cudaMalloc((void **)&d_nrm, sizeof(float) * 3 * (nvert ? nvert : 1));
+            if (e == cudaSuccess) e = cudaMalloc((void **)&d_tri, sizeof(int) * 3 * (ntri ? ntri : 1));
+            if (e == cudaSuccess) {
+                mc_emit(in, b[1], b[3], b[5], rotate_faces ? 1 : 0, d_pts, d_nrm, d_tri, s->stream);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = cudaMemcpyAsync(points, d_pts, sizeof(float) * 3 * nvert, cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(normals, d_nrm, sizeof(float) * 3 * nvert, cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(triangles, d_tri, sizeof(int) * 3 * ntri, cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess) r = fail(BBG_ERR_CUDA, "marching cubes: %s", cudaGetErrorString(e));
+        }
+    }
+    cudaFree(d_vals);
+    cudaFree(d_pts);
+    cudaFree(d_nrm);
+    cudaFree(d_tri);
+    for (unsigned *p : b) cudaFree(p);
+    return r;
+}
+

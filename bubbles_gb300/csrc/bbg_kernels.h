@@ -114,4 +114,19 @@ void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo
 void launch_lnm(const GridDev &g, const unsigned *start, const unsigned *cell, const int *pid, int n, int delta,
                 int *level, int *out, cudaStream_t s);
 
+// Marching cubes of a vertex-centred field (mc.cu)
+struct McInput {
+    const float *values;   // device, x fastest
+    int nodes[3];
+    float origin[3], spacing[3];
+    float inv[3];          // (float)(1.0 / spacing)
+    float iso;
+};
+cudaError_t mc_prepare();
+cudaError_t mc_count(const McInput &in, unsigned *ntri_cube, unsigned *tri_start, unsigned *tri_part,
+                     unsigned *crossing, unsigned *flag_copy, unsigned *vindex, unsigned *v_part, unsigned *h,
+                     size_t *ntri, size_t *nvert, cudaStream_t s);
+void mc_emit(const McInput &in, const unsigned *tri_start, const unsigned *crossing, const unsigned *vindex,
+             int rotate, float *points, float *normals, int *tris, cudaStream_t s);
+
 }  // namespace bbg

@@ -218,6 +218,29 @@ class Solver:
                out["distance"].ctypes.data, out["inside"].ctypes.data)
         return out
 
+    def marching_cubes(self, nodes, origin, spacing, values, iso=0.0, rotate_faces=False):
+        """MarchingCubes of a vertex-centred field on the device: (points, normals,
+        triangles)."""
+        g = N.SdfGrid()
+        for k in range(3):
+            g.nodes[k] = int(nodes[k])
+            g.origin[k] = float(origin[k])
+            g.spacing[k] = float(spacing[k] if np.ndim(spacing) else spacing)
+        v = np.ascontiguousarray(values, dtype=np.float32).reshape(-1)
+        npt, ntr = ctypes.c_size_t(), ctypes.c_size_t()
+        st = N.load().bbg_marching_cubes(self.h, ctypes.byref(g), v.ctypes.data, float(iso), int(bool(rotate_faces)),
+                                         None, None, 0, None, 0, ctypes.byref(npt), ctypes.byref(ntr))
+        if st not in (N.OK, 4):
+            N.call("bbg_marching_cubes", self.h, ctypes.byref(g), v.ctypes.data, float(iso), 0, None, None, 0,
+                   None, 0, ctypes.byref(npt), ctypes.byref(ntr))
+        pts = np.empty((npt.value, 3), np.float32)
+        nrm = np.empty((npt.value, 3), np.float32)
+        tri = np.empty((ntr.value, 3), np.int32)
+        N.call("bbg_marching_cubes", self.h, ctypes.byref(g), v.ctypes.data, float(iso), int(bool(rotate_faces)),
+               pts.ctypes.data, nrm.ctypes.data, npt.value, tri.ctypes.data, ntr.value, ctypes.byref(npt),
+               ctypes.byref(ntr))
+        return pts, nrm, tri
+
     def lnm_boundary(self, h, unbounded=False):
         """LNMBoundary: each particle's level (1, 2, 0 inside), caller order."""
         out = np.zeros(self.n, np.int32)

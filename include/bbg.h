@@ -380,6 +380,21 @@ bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocit
  * (any number when unbounded), else 0.  One thread per cell, then one per particle. */
 bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels);
 
+/* ----- marching cubes ----------------------------------------------------------- */
+/* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field
+ * at iso on the device: a vertex on every grid edge whose ends straddle iso (at or below
+ * counts as inside), placed and given a normal (interpolated central-difference gradients,
+ * normalised) in the reference's float operations, so points and normals equal the
+ * reference's; triangles face away from the inside (rotate_faces reverses them).  The
+ * triangulation comes from a table derived here, not the reference's case table: in
+ * ambiguous configurations the connectivity (and count) of triangles can differ.  Points
+ * are ordered by edge (x edges, then y, then z, each by node), triangles by cube (x slowest,
+ * z fastest).  With too small capacities (or NULL buffers) the counts are returned with
+ * BBG_ERR_CAPACITY. */
+bbg_status bbg_marching_cubes(bbg_solver s, const bbg_sdf_grid *grid, const float *values, double iso,
+                              int rotate_faces, float *points, float *normals, size_t point_capacity,
+                              int *triangles, size_t triangle_capacity, size_t *npoints, size_t *ntriangles);
+
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
  * sorted particles) and how many members' records a thread requests together in the

@@ -7,6 +7,7 @@
 #include <collider.h>
 #include <emitter.h>
 #include <lnm.h>
+#include <marching_cubes.h>
 #include <cutil.h>
 #include <interaction.h>
 #include <pcisph_solver.h>
@@ -382,6 +383,34 @@ void ref_lnm(RefSim *s, double h, int unbounded, int *levels) {
     s->grid->UpdateQueryState();
     LNMBoundary(s->pSet, s->grid, (Float)h, 0, nullptr, unbounded != 0);
     for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
+}
+
+/* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field
+ * (nodes per axis, origin, spacing, values x fastest) at iso, single thread: the mesh's
+ * points, normals and triangles (at most the capacities stored).  Returns the point count;
+ * *ntri receives the triangle count. */
+int ref_marching_cubes(const int *nodes, const double *origin, const double *spacing, const float *values,
+                       double iso, int rotate, float *points, float *normals, int *tris, int pcap, int tcap,
+                       int *ntri) {
+    SetCPUThreads(1);
+    SetSystemUseCPU();
+    FieldGrid3f *g = cudaAllocateVx(FieldGrid3f, 1);
+    g->Build(vec3ui((unsigned)(nodes[0] - 1), (unsigned)(nodes[1] - 1), (unsigned)(nodes[2] - 1)),
+             vec3f((Float)spacing[0], (Float)spacing[1], (Float)spacing[2]), V3(origin), VertexCentered);
+    for (unsigned q = 0; q < g->total; q++) g->field[q] = (Float)values[q];
+    g->MarkFilled();
+    HostTriangleMesh3 mesh;
+    MarchingCubes(g, &mesh, (Float)iso, rotate != 0);
+    const int np = (int)mesh.points.size(), nt = (int)mesh.pointIndices.size();
+    for (int i = 0; i < np && i < pcap; i++)
+        for (int k = 0; k < 3; k++) {
+            points[3 * i + k] = (float)mesh.points[(size_t)i][k];
+            normals[3 * i + k] = (float)mesh.normals[(size_t)i][k];
+        }
+    for (int i = 0; i < nt && i < tcap; i++)
+        for (int k = 0; k < 3; k++) tris[3 * i + k] = (int)mesh.pointIndices[(size_t)i][k];
+    *ntri = nt;
+    return np;
 }
 
 /* SerializerLoadParticles3 on a frame file: the first fluid section's particles (at most

@@ -91,3 +91,12 @@ inline cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t a, cudaEvent_t b)
     *ms = std::chrono::duration<float, std::milli>(b->t - a->t).count();
     return cudaSuccess;
 }
+
+/* __constant__ symbols are plain host objects here */
+template <class T>
+inline cudaError_t cudaMemcpyToSymbol(T &symbol, const void *src, size_t count, size_t offset = 0, int kind = 0) {
+    (void)kind;
+    memcpy(reinterpret_cast<char *>(&symbol) + offset, src, count);
+    return cudaSuccess;
+}
+

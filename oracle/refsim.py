@@ -52,6 +52,10 @@ def load(variant):
                                                 ctypes.c_double]),
         "ref_collider_sdf": (ctypes.c_int, [_P, ctypes.c_int, _I32, _D, _D, ctypes.POINTER(ctypes.c_float),
                                             ctypes.c_int]),
+        "ref_marching_cubes": (ctypes.c_int, [_I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_double,
+                                              ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_float), _I32, ctypes.c_int, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_int)]),
         "ref_lnm": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
         "ref_mesh_sdf": (ctypes.c_int, [_D, ctypes.c_int, _I32, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
@@ -259,4 +263,23 @@ def mesh_sdf(vertices, triangles, dx, margin, variant="f32"):
     vals = np.zeros(n, np.float32)
     lib.ref_mesh_sdf(*args, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n)
     return nodes, org, sp, vals
+
+
+def marching_cubes(nodes, origin, spacing, values, iso=0.0, rotate=False, variant="f32"):
+    """MarchingCubes of the reference (single thread): (points, normals, triangles)."""
+    lib = load(variant)
+    nodes = np.ascontiguousarray(nodes, np.int32)
+    org = np.ascontiguousarray(origin, np.float64)
+    sp = np.ascontiguousarray(spacing, np.float64)
+    vals = np.ascontiguousarray(values, np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    nt = ctypes.c_int()
+    cap = 12 * int(np.prod(nodes))
+    pts = np.zeros((cap, 3), np.float32)
+    nrm = np.zeros((cap, 3), np.float32)
+    tri = np.zeros((cap, 3), np.int32)
+    n = lib.ref_marching_cubes(nodes.ctypes.data_as(_I32), org.ctypes.data_as(_D), sp.ctypes.data_as(_D),
+                               vals.ctypes.data_as(fp), float(iso), int(bool(rotate)), pts.ctypes.data_as(fp),
+                               nrm.ctypes.data_as(fp), tri.ctypes.data_as(_I32), cap, cap, ctypes.byref(nt))
+    return pts[:n], nrm[:n], tri[:nt.value]
 

@@ -34,6 +34,9 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
   lnm_f32.npz     LNMBoundary (boundaries/lnm.h, fast variant) levels of the 1,440-particle
                   scene after 3 as-shipped substeps and a fresh grid distribution, for
                   h = 0.01, 0.02, 0.04 and unbounded.
+  mc_f32.npz      MarchingCubes (reconstruction/marching_cubes.cpp) of two fields on a 21x22x23
+                  grid: two overlapping spheres' distance (iso 0) and a random field (every
+                  cube configuration): the reference's points, normals and triangles.
   emit_f32.npz    particles VolumeParticleEmitter3 (core/emitter.cpp) emitted after
                   srand(seed) for boxes and spheres, with and without jitter, explicit
                   bounds, a reversed box and a binding max_particles (EMIT_CASES).
@@ -45,6 +48,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py sdf       # sdf_f32.npz only
     python tests/golden/make_golden.py mesh      # mesh_f32.npz only
     python tests/golden/make_golden.py lnm       # lnm_f32.npz only
+    python tests/golden/make_golden.py mc        # mc_f32.npz only
 """
 import json
 import os
@@ -292,6 +296,29 @@ def make_mesh():
     np.savez_compressed(os.path.join(HERE, "mesh_f32.npz"), **out)
 
 
+def mc_fields():
+    """The marching-cubes fixture's grid and its two fields (float32 node values)."""
+    nodes = np.array([21, 22, 23], np.int32)
+    org = np.array([-0.5, -0.52, -0.55])
+    sp = np.array([0.05, 0.05, 0.05])
+    i, j, k = np.meshgrid(np.arange(nodes[0]), np.arange(nodes[1]), np.arange(nodes[2]), indexing="ij")
+    idx = np.stack([i.ravel(order="F"), j.ravel(order="F"), k.ravel(order="F")], axis=1)
+    pos = org.astype(np.float32) + sp.astype(np.float32) * idx.astype(np.float32)
+    blobs = np.minimum(np.linalg.norm(pos - np.array([0.03, 0.01, -0.02]), axis=1) - 0.3,
+                       np.linalg.norm(pos - np.array([0.25, 0.2, 0.1]), axis=1) - 0.15).astype(np.float32)
+    noise = np.random.default_rng(3).normal(size=len(pos)).astype(np.float32)
+    return nodes, org, sp, {"blobs": blobs, "noise": noise}
+
+
+def make_mc():
+    nodes, org, sp, fields = mc_fields()
+    out = {"nodes": nodes, "origin": org, "spacing": sp}
+    for name, vals in fields.items():
+        p, n, t = R.marching_cubes(nodes, org, sp, vals, 0.0)
+        out.update({name + "_values": vals, name + "_points": p, name + "_normals": n, name + "_triangles": t})
+    np.savez_compressed(os.path.join(HERE, "mc_f32.npz"), **out)
+
+
 LNM_CASES = [(0.01, 0), (0.02, 0), (0.04, 0), (0.02, 1)]
 
 
@@ -353,4 +380,6 @@ if __name__ == "__main__":
         make_mesh()
     if not what or what == ["lnm"]:
         make_lnm()
+    if not what or what == ["mc"]:
+        make_mc()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
