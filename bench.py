@@ -432,6 +432,85 @@ def seeding(bb, scene, final_pos, device, reps=3):
     return out
 
 
+def postprocess(bb, scene, final_pos, device):
+    """Post-processing on the grid, end to end through the C ABI (host wall clock, result
+    copied back), beside the oracle's restatement of the reference's CPU code (single
+    thread):
+    - boundary classification of the final state: LNMBoundary (fast), LNMBoundarySingle,
+      LNMBoundaryExtended (5 levels), XiaoweiBoundary and LNMBoundary with the Xiaowei L2
+      filter, on the same grid distribution and densities;
+    - DiltsSpokeBoundary of a jittered BCC sphere of about 95 K particles at the spacing;
+    - MarchingCubes of two overlapping spheres' distance on a 256^3 vertex grid (no CPU
+      leg: the reference's own MarchingCubes is not part of the oracle)."""
+    import ctypes
+    from oracle import oracle as O
+    sp = scene["spacing"]
+    out = {}
+    o = O.OracleSim(scene, final_pos)
+    o.update_grid_distribution()
+    o.compute_density(0)
+    rho = o.get(O.DENSITY)
+    s = bb.Solver(dict(scene), pos=final_pos, device=device)
+    s.update_grid_distribution()
+    s.set(bb.FIELD_DENSITY, rho)
+    runs = {"lnm": (lambda: s.lnm_boundary(sp), lambda: o.lnm(sp)),
+            "lnm_single": (lambda: s.lnm_boundary_single(sp), lambda: o.lnm_single(sp)),
+            "lnm_extended": (lambda: s.lnm_boundary_extended(sp, 5), lambda: o.lnm_extended(sp, 5)),
+            "xiaowei": (lambda: s.boundary_test("xiaowei", sp), lambda: o.xiaowei(sp)),
+            "lnm_xiaowei": (lambda: s.lnm_boundary_geometric(sp, "xiaowei")[0],
+                            lambda: o.lnm_geometric(sp, 1)[0])}
+    for name, (dev, cpu) in runs.items():
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            got = dev()
+            t.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        want = cpu()
+        c = time.perf_counter() - t0
+        out[name] = {"particles": len(final_pos), "ms": 1e3 * min(t[1:]), "cpu_ms": 1e3 * c,
+                     "same_as_oracle": bool(np.array_equal(got, want))}
+    s.close()
+    o.close()
+    ctypes.CDLL(None).srand(3)
+    ball, _ = O.emit_volume({"type": "sphere", "center": (0.0, 0.0, 0.0), "radius": 0.18 * (sp / 0.008)}, sp,
+                            jitter=0.2)
+    s = bb.Solver(dict(scene), pos=ball, device=device)
+    s.update_grid_distribution()
+    t = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        got = s.boundary_test("dilts")
+        t.append(time.perf_counter() - t0)
+    o = O.OracleSim(scene, ball)
+    o.update_grid_distribution()
+    t0 = time.perf_counter()
+    want = o.dilts()
+    c = time.perf_counter() - t0
+    o.close()
+    out["dilts"] = {"particles": len(ball), "boundary": int(got.sum()), "ms": 1e3 * min(t), "cpu_ms": 1e3 * c,
+                    "same_as_oracle": bool(np.array_equal(got, want))}
+    # marching cubes of two overlapping spheres on 256^3 nodes
+    m = 256
+    ax = np.linspace(-1.0, 1.0, m, dtype=np.float32)
+    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")   # x fastest in memory
+    d1 = np.sqrt((x - 0.2) ** 2 + y ** 2 + z ** 2) - 0.5
+    d2 = np.sqrt((x + 0.3) ** 2 + (y - 0.1) ** 2 + z ** 2) - 0.4
+    vals = np.minimum(d1, d2).astype(np.float32).ravel()
+    del x, y, z, d1, d2
+    spacing = float(ax[1] - ax[0])
+    t = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        pts, _, tris = s.marching_cubes((m, m, m), (-1.0, -1.0, -1.0), (spacing,) * 3, vals, 0.0)
+        t.append(time.perf_counter() - t0)
+    s.close()
+    out["marching_cubes"] = {"nodes": m ** 3, "points": len(pts), "triangles": len(tris), "ms": 1e3 * min(t[1:]),
+                             "note": "field upload, both passes and the mesh download included"}
+    out["measured"] = "host wall clock around the C-ABI calls (best of the repeats after the first)"
+    return out
+
+
 def run_ours(args, scene, pos):
     import torch
 
@@ -573,10 +652,11 @@ def run_ours(args, scene, pos):
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
         batch_offsets = g.layout() if scene.get("batch") else None
-        frames = seeds = None
+        frames = seeds = post = None
         if not scene.get("batch") and not args.no_frames and rank == 0:
             frames = frame_io(bb, g, scene, n, local)
             seeds = seeding(bb, scene, final_pos, local)
+            post = postprocess(bb, scene, final_pos, local)
         g.close()
 
     if rank != 0:
@@ -675,6 +755,7 @@ def run_ours(args, scene, pos):
         line["frame_io"] = frames
     if seeds is not None:
         line["seeding"] = seeds
+        line["postprocess"] = post
     print(json.dumps(line), flush=True)
     barrier(dist)
 

@@ -2774,30 +2774,174 @@ bbg_status bbg_collider_set_mesh(bbg_solver s, int index, const float *vertices,
 // ----------------------------------------------------------------------------
 // boundary classification: LNMBoundary (src/boundaries/lnm.h:245-275)
 // ----------------------------------------------------------------------------
-bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels) {
+// LNMComputeDelta (lnm.h:24-33): (min cell length / h)^dim as a float power
+static float lnm_pre_delta(bbg_solver s, double h) {
+    const float *len = s->P.g.len;
+    const float minlen = len[0] < len[1] ? (len[0] < len[2] ? len[0] : len[2]) : (len[1] < len[2] ? len[1] : len[2]);
+    return std::pow(minlen / (float)h, 3.0f);
+}
+
+// the kernels' delta from a float parameter (LNMBoundaryL2Kernel, LNMBoundaryLKKernel):
+// truncated when positive, any count when unbounded
+static int lnm_delta(bbg_solver s, double h, int unbounded) {
+    const float pd = unbounded ? -1.f : lnm_pre_delta(s, h);
+    return pd > 0 ? (int)pd : 0x7fffffff;
+}
+
+static bbg_status lnm_check(bbg_solver s, double h, const int *out) {
     if (bbg_status r = check_solver(s)) return r;
-    if (!levels || !(h > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need h > 0 and an output");
+    if (!out || !(h > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need h > 0 and an output");
     if (!s->setup_done || s->n <= 0) return fail(BBG_ERR_STATE, "no particles set up");
     if (!s->grid_valid)   // the reference classifies the grid's distribution: make one
         if (bbg_status r = grid_update(s)) return r;
-    // LNMComputeDelta: (min cell length / h)^dim as a float power, truncated to int
-    const float *len = s->P.g.len;
-    const float minlen = len[0] < len[1] ? (len[0] < len[2] ? len[0] : len[2]) : (len[1] < len[2] ? len[1] : len[2]);
-    const float pd = std::pow(minlen / (float)h, 3.0f);
-    const int delta = (!unbounded && pd > 0) ? (int)pd : 0x7fffffff;
-    int *d_level = nullptr, *d_out = nullptr;
-    cudaError_t e = cudaMalloc((void **)&d_level, sizeof(int) * ((size_t)s->P.g.total + 1));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, sizeof(int) * (size_t)s->n);
-    if (e == cudaSuccess) {
-        launch_lnm(s->P.g, s->B.start, s->B.cell, s->B.pid[s->pid_cur], s->n, delta, d_level, d_out, s->stream);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(levels, d_out, sizeof(int) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaFree(d_level);
-    cudaFree(d_out);
-    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "LNM boundary: %s", cudaGetErrorString(e));
     return BBG_OK;
+}
+
+// device scratch of the boundary passes: cell levels, per-particle output and values, queue
+struct LnmScratch {
+    int *level = nullptr, *out = nullptr, *val = nullptr, *queue = nullptr, *counts = nullptr;
+    cudaError_t alloc(size_t cells, size_t n) {
+        cudaError_t e = cudaMalloc((void **)&level, sizeof(int) * (cells + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&out, sizeof(int) * n);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&val, sizeof(int) * n);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&queue, sizeof(int) * n);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&counts, sizeof(int) * 4);
+        return e;
+    }
+    ~LnmScratch() {
+        cudaFree(level);
+        cudaFree(out);
+        cudaFree(val);
+        cudaFree(queue);
+        cudaFree(counts);
+    }
+};
+
+static bbg_status lnm_finish(bbg_solver s, cudaError_t e, const LnmScratch &w, int *levels, const char *what) {
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(levels, w.out, sizeof(int) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return BBG_OK;
+}
+
+// The particle tests' arguments: Xiaowei at kernel radius 6h (xiaowei.h:26-33), Dilts at
+// 0.75 x the set's radius (the target spacing, particle.h:536-541; dilts.h:30-33), the
+// spoke angles i pi / 64 and j 2 pi / 64 rounded to float and their sines and cosines by
+// the C library's float functions, as the reference computes them on the host.
+static BoundaryArgs boundary_args(bbg_solver s, double h) {
+    BoundaryArgs A;
+    A.g = s->P.g;
+    A.iz = s->P.iz;
+    A.start = s->B.start;
+    A.pos = s->B.pos[s->state];
+    A.rho = s->B.rho;
+    A.pid = s->B.pid[s->pid_cur];
+    const float hf = (float)h;
+    const float rho6 = (float)(6.0 * (double)hf);
+    const float h2 = rho6 * rho6, h3 = h2 * rho6;
+    A.x_rhot = (float)(0.7 * 1000.0);
+    A.x_h2 = h2;
+    A.x_wc = 315.0 / (64.0 * 3.14159265358979323846 * (double)h3);
+    A.x_limit = 0.15 * (double)rho6;
+    const float radius = (float)s->desc.target_spacing;
+    A.d_rad = (float)((double)radius * 0.75);
+    A.d_lim = (A.d_rad + A.d_rad) - 0.0001f;
+    const float samples = (float)64;
+    for (int i = 0; i <= 64; i++) {
+        const float u = (float)(i * 3.14159265358979323846 / (double)samples);
+        const float v = (float)(i * 6.283185307179586 / (double)samples);
+        A.spoke[i] = sinf(u);
+        A.spoke[65 + i] = cosf(u);
+        A.spoke[130 + i] = sinf(v);
+        A.spoke[195 + i] = cosf(v);
+    }
+    return A;
+}
+
+// ----------------------------------------------------------------------------
+// boundary classification: LNMBoundary (src/boundaries/lnm.h:245-289) and its variants
+// ----------------------------------------------------------------------------
+bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels) {
+    if (bbg_status r = lnm_check(s, h, levels)) return r;
+    LnmScratch w;
+    cudaError_t e = w.alloc(s->P.g.total, (size_t)s->n);
+    if (e == cudaSuccess)
+        launch_lnm(s->P.g, s->B.start, s->B.cell, s->B.pid[s->pid_cur], s->n, lnm_delta(s, h, unbounded), w.level,
+                   w.out, s->stream);
+    return lnm_finish(s, e, w, levels, "LNM boundary");
+}
+
+bbg_status bbg_lnm_boundary_single(bbg_solver s, double h, int unbounded, int *levels) {
+    if (bbg_status r = lnm_check(s, h, levels)) return r;
+    // LNMBoundarySingleKernel takes delta as an int: truncated first, then any count unless positive
+    const int pre = unbounded ? -1 : (int)lnm_pre_delta(s, h);
+    LnmScratch w;
+    cudaError_t e = w.alloc(s->P.g.total, (size_t)s->n);
+    if (e == cudaSuccess)
+        launch_lnm_single(s->P.g, s->B.start, s->B.cell, s->B.pid[s->pid_cur], s->n, pre > 0 ? pre : 0x7fffffff,
+                          w.level, w.out, s->stream);
+    return lnm_finish(s, e, w, levels, "LNM single-pass boundary");
+}
+
+bbg_status bbg_lnm_boundary_extended(bbg_solver s, double h, int max_level, int unbounded, int *levels) {
+    if (bbg_status r = lnm_check(s, h, levels)) return r;
+    LnmScratch w;
+    cudaError_t e = w.alloc(s->P.g.total, (size_t)s->n);
+    // LNMClassifyLazyGPU: levels 0..max_level, or until a sweep changes nothing
+    const long cap = (long)s->P.g.total + 2;
+    for (long L = 0; e == cudaSuccess; L++) {
+        if (max_level < 0) e = cudaMemsetAsync(w.counts, 0, sizeof(int), s->stream);
+        if (e == cudaSuccess) launch_lnm_once(s->P.g, s->B.start, w.level, (int)L, w.counts, s->stream);
+        if (max_level > -1) {
+            if (L >= max_level) break;
+            continue;
+        }
+        int changed = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&changed, w.counts, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (!changed || L >= cap) break;
+    }
+    if (e == cudaSuccess)
+        launch_lnm_extended_finish(s->P.g, s->P.iz, s->B.pos[s->state], s->B.start, s->B.cell, s->B.pid[s->pid_cur],
+                                   s->n, lnm_delta(s, h, unbounded), w.level, w.val, w.out, s->stream);
+    return lnm_finish(s, e, w, levels, "LNM extended boundary");
+}
+
+bbg_status bbg_lnm_boundary_geometric(bbg_solver s, double h, int algorithm, int unbounded, int *levels,
+                                      int *queued, int *accepted) {
+    if (bbg_status r = lnm_check(s, h, levels)) return r;
+    if (algorithm != BBG_BOUNDARY_XIAOWEI && algorithm != BBG_BOUNDARY_DILTS)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "unknown L2 filter %d", algorithm);
+    if (algorithm == BBG_BOUNDARY_XIAOWEI && !(s->valid & bit(BBG_FIELD_DENSITY)))
+        return fail(BBG_ERR_STATE, "the Xiaowei test reads the particle densities: none are valid");
+    LnmScratch w;
+    cudaError_t e = w.alloc(s->P.g.total, (size_t)s->n);
+    if (e == cudaSuccess)
+        launch_lnm_geometric(boundary_args(s, h), s->B.cell, s->n, lnm_delta(s, h, unbounded), algorithm, w.level,
+                             w.queue, w.counts, w.out, s->stream);
+    int counts[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, w.counts, sizeof counts, cudaMemcpyDeviceToHost, s->stream);
+    if (bbg_status r = lnm_finish(s, e, w, levels, "LNM boundary with a geometric filter")) return r;
+    if (queued) *queued = counts[0];
+    if (accepted) *accepted = counts[1];
+    return BBG_OK;
+}
+
+// XiaoweiBoundary (src/boundaries/xiaowei.h:80-87), DiltsSpokeBoundary (dilts.h:155-163)
+bbg_status bbg_boundary_test(bbg_solver s, int method, double h, int *flags) {
+    if (method == BBG_BOUNDARY_DILTS && !(h > 0)) h = 1.0;   // Dilts does not use h
+    if (bbg_status r = lnm_check(s, h, flags)) return r;
+    if (method != BBG_BOUNDARY_XIAOWEI && method != BBG_BOUNDARY_DILTS)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "unknown boundary test %d", method);
+    if (method == BBG_BOUNDARY_XIAOWEI && !(s->valid & bit(BBG_FIELD_DENSITY)))
+        return fail(BBG_ERR_STATE, "the Xiaowei test reads the particle densities: none are valid");
+    LnmScratch w;
+    cudaError_t e = w.alloc(s->P.g.total, (size_t)s->n);
+    if (e == cudaSuccess) launch_boundary_test(boundary_args(s, h), method, s->n, w.out, s->stream);
+    return lnm_finish(s, e, w, flags, "boundary test");
 }
 
 // ----------------------------------------------------------------------------

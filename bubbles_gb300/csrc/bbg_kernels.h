@@ -111,6 +111,29 @@ void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo
 
 // LNM boundary levels (1, 2, 0) of n sorted slots into out (caller order through pid);
 // level: one int per cell (boundary.cu)
+// boundary.cu: arguments of the particle tests of the boundary classification
+struct BoundaryArgs {
+    GridDev g;
+    float iz;
+    const unsigned *start;
+    const float4 *pos;    // current positions, slot order
+    const float *rho;     // densities, slot order (Xiaowei)
+    const int *pid;
+    float x_rhot;         // Xiaowei: 0.7 * water density; 6h squared; 315 / (64 pi (6h)^3);
+    float x_h2;           // 0.15 * 6h (as double)
+    double x_wc, x_limit;
+    float d_rad, d_lim;   // Dilts: 0.75 * radius; 2 rad - Epsilon
+    float spoke[260];     // sin u, cos u, sin v, cos v of the 65 spoke angles (host libm)
+};
+void launch_lnm_single(const GridDev &g, const unsigned *start, const unsigned *cell, const int *pid, int n,
+                       int delta, int *level, int *out, cudaStream_t s);
+void launch_lnm_once(const GridDev &g, const unsigned *start, int *level, int L, int *changed, cudaStream_t s);
+void launch_lnm_extended_finish(const GridDev &g, float iz, const float4 *pos, const unsigned *start,
+                                const unsigned *cell, const int *pid, int n, int delta, int *level, int *val,
+                                int *out, cudaStream_t s);
+void launch_lnm_geometric(const BoundaryArgs &A, const unsigned *cell, int n, int delta, int algorithm,
+                          int *level, int *queue, int *counts, int *out, cudaStream_t s);
+void launch_boundary_test(const BoundaryArgs &A, int algorithm, int n, int *out, cudaStream_t s);
 void launch_lnm(const GridDev &g, const unsigned *start, const unsigned *cell, const int *pid, int n, int delta,
                 int *level, int *out, cudaStream_t s);
 

@@ -68,6 +68,9 @@ def shapes_from_scene(scene):
     return arr, len(cols)
 
 
+BOUNDARY_TESTS = {"xiaowei": 1, "dilts": 2}
+
+
 class Solver:
     """One GPU particle system (PciSphSolver3 or SphSolver3 semantics)."""
 
@@ -245,6 +248,35 @@ class Solver:
         """LNMBoundary: each particle's level (1, 2, 0 inside), caller order."""
         out = np.zeros(self.n, np.int32)
         N.call("bbg_lnm_boundary", self.h, float(h), int(bool(unbounded)), out.ctypes.data)
+        return out
+
+    def lnm_boundary_single(self, h, unbounded=False):
+        """LNMBoundarySingle: the N2x2 classification in one pass (1, 2, 0), caller order."""
+        out = np.zeros(self.n, np.int32)
+        N.call("bbg_lnm_boundary_single", self.h, float(h), int(bool(unbounded)), out.ctypes.data)
+        return out
+
+    def lnm_boundary_extended(self, h, max_level=5, unbounded=False):
+        """LNMBoundaryExtended: levels 1, 2 (filtered L2), 3.. max_level, 0, caller order."""
+        out = np.zeros(self.n, np.int32)
+        N.call("bbg_lnm_boundary_extended", self.h, float(h), int(max_level), int(bool(unbounded)),
+               out.ctypes.data)
+        return out
+
+    def lnm_boundary_geometric(self, h, algorithm, unbounded=False):
+        """LNMBoundary with the Xiaowei ("xiaowei" / 1) or Dilts ("dilts" / 2) L2 filter:
+        (levels, queued, accepted)."""
+        alg = BOUNDARY_TESTS.get(algorithm, algorithm)
+        out = np.zeros(self.n, np.int32)
+        q, a = ctypes.c_int(), ctypes.c_int()
+        N.call("bbg_lnm_boundary_geometric", self.h, float(h), int(alg), int(bool(unbounded)), out.ctypes.data,
+               ctypes.byref(q), ctypes.byref(a))
+        return out, q.value, a.value
+
+    def boundary_test(self, method, h=0.0):
+        """XiaoweiBoundary ("xiaowei", at h) or DiltsSpokeBoundary ("dilts"): 1 per boundary particle."""
+        out = np.zeros(self.n, np.int32)
+        N.call("bbg_boundary_test", self.h, int(BOUNDARY_TESTS.get(method, method)), float(h), out.ctypes.data)
         return out
 
     def map_grid(self):

@@ -380,6 +380,40 @@ bbg_status bbg_map_grid_emit(bbg_solver s, double distance, const double velocit
  * (any number when unbounded), else 0.  One thread per cell, then one per particle. */
 bbg_status bbg_lnm_boundary(bbg_solver s, double h, int unbounded, int *levels);
 
+/* LNMBoundarySingle (lnm.h:167-256): the N2x2 classification in one pass.  A cell with
+ * particles is L1 on the grid's border; otherwise its 5x5x5 neighbourhood, walked in the
+ * reference's order (y, x, z), decides at the first adjacent empty cell (L1) or the first
+ * adjacent cell holding at most delta particles that lies on the border (L2); without
+ * either, L2 when an adjacent cell holding 1..delta particles touches an empty cell.
+ * delta is (min cell length / h)^3 truncated to int, any count when that is 0 or unbounded. */
+bbg_status bbg_lnm_boundary_single(bbg_solver s, double h, int unbounded, int *levels);
+
+/* LNMBoundaryExtended (lnm.h:291-462): cell levels by sweeps (0 empty, 1 border or next to
+ * an empty cell, k next to a level k-1 cell) for k up to max_level (max_level < 0: until a
+ * sweep changes nothing); each particle takes its hashed cell's level (0 past max_level);
+ * a non-L1 cell next to an L1 cell holding at most delta particles gives its particles 2,
+ * the other level-2 cells 3; L1 cells 1. */
+bbg_status bbg_lnm_boundary_extended(bbg_solver s, double h, int max_level, int unbounded, int *levels);
+
+/* Particle tests of boundary.  XIAOWEI (xiaowei.h:21-78): density below 700, or the
+ * std-kernel (radius 6h) weighted mean of the 27 cells' positions farther than 0.9h from
+ * the particle; reads the set's densities (BBG_FIELD_DENSITY must be valid).  DILTS
+ * (dilts.h:110-153): one of the 65 x 65 spoke points on the sphere of radius 0.75 x the
+ * target spacing lies outside every overlapping neighbour's sphere (h unused). */
+#define BBG_BOUNDARY_XIAOWEI 1
+#define BBG_BOUNDARY_DILTS 2
+
+/* LNMBoundary with a geometric L2 filter (algorithm XIAOWEI or DILTS; lnm.h:57-112,
+ * 258-289): L1 as the fast variant; the particles of L2 cells are queued and marked 2 only
+ * when the test finds them on the boundary, else 0.  queued / accepted (optional): the
+ * work queue's size and accepted count, as the reference's bounds app reports them. */
+bbg_status bbg_lnm_boundary_geometric(bbg_solver s, double h, int algorithm, int unbounded, int *levels,
+                                      int *queued, int *accepted);
+
+/* XiaoweiBoundary / DiltsSpokeBoundary (xiaowei.h:80-87, dilts.h:155-163): flags[i] = 1 for
+ * each boundary particle, one thread per particle. */
+bbg_status bbg_boundary_test(bbg_solver s, int method, double h, int *flags);
+
 /* ----- marching cubes ----------------------------------------------------------- */
 /* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field
  * at iso on the device: a vertex on every grid edge whose ends straddle iso (at or below

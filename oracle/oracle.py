@@ -115,6 +115,11 @@ def load(variant="f32"):
         "orc_get_cells": (ctypes.c_int, [_P, _U32, _U32, _U32]),
         "orc_get_buckets": (ctypes.c_int, [_P, _I32, _I32]),
         "orc_lnm": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
+        "orc_lnm_single": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
+        "orc_lnm_extended": (None, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I32]),
+        "orc_lnm_geometric": (None, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I32, _I32]),
+        "orc_xiaowei": (None, [_P, ctypes.c_double, _I32]),
+        "orc_dilts": (None, [_P, _I32]),
         "orc_map_grid": (None, [_P]),
         "orc_map_grid_emit": (ctypes.c_long, [_P, ctypes.c_double, _D, ctypes.c_long]),
         "orc_shape_distance": (None, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, _I32]),
@@ -290,6 +295,38 @@ class OracleSim:
         """LNMBoundary's particle levels (1, 2, 0 inside) on the current chains."""
         out = np.zeros(self.n, np.int32)
         self.lib.orc_lnm(self.h, float(h), int(bool(unbounded)), _ptr(out, _I32))
+        return out
+
+    def lnm_single(self, h, unbounded=False):
+        """LNMBoundarySingle's particle levels (1, 2, 0)."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.orc_lnm_single(self.h, float(h), int(bool(unbounded)), _ptr(out, _I32))
+        return out
+
+    def lnm_extended(self, h, max_level=5, unbounded=False):
+        """LNMBoundaryExtended's particle levels (1, 2, 3.. max_level, 0)."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.orc_lnm_extended(self.h, float(h), int(max_level), int(bool(unbounded)), _ptr(out, _I32))
+        return out
+
+    def lnm_geometric(self, h, algorithm, unbounded=False):
+        """LNMBoundary with the Xiaowei (1) or Dilts (2) L2 filter: (levels, queued, accepted)."""
+        out = np.zeros(self.n, np.int32)
+        st = np.zeros(2, np.int32)
+        self.lib.orc_lnm_geometric(self.h, float(h), int(algorithm), int(bool(unbounded)),
+                                   _ptr(out, _I32), _ptr(st, _I32))
+        return out, int(st[0]), int(st[1])
+
+    def xiaowei(self, h):
+        """XiaoweiParticleIsBoundary of every particle on the stored densities."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.orc_xiaowei(self.h, float(h), _ptr(out, _I32))
+        return out
+
+    def dilts(self):
+        """DiltsSpokeParticleIsBoundary of every particle."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.orc_dilts(self.h, _ptr(out, _I32))
         return out
 
     def map_grid(self):

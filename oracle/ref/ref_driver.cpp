@@ -385,6 +385,66 @@ void ref_lnm(RefSim *s, double h, int unbounded, int *levels) {
     for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
 }
 
+/* LNMBoundarySingle (src/boundaries/lnm.h:167-256): the N2x2 classification in one pass. */
+void ref_lnm_single(RefSim *s, double h, int unbounded, int *levels) {
+    for (int i = 0; i < s->n; i++) s->pSet->SetParticleV0(i, 0);
+    s->grid->UpdateQueryState();
+    LNMBoundarySingle(s->pSet, s->grid, (Float)h, unbounded != 0);
+    for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
+}
+
+/* LNMBoundaryExtended (src/boundaries/lnm.h:440-462): voxel levels up to max_level, the
+ * LK filter and the L2 -> L3 promotion, as the bounds app calls it (cells invalidated,
+ * v0 cleared). */
+void ref_lnm_extended(RefSim *s, double h, int max_level, int unbounded, int *levels) {
+    for (int i = 0; i < s->n; i++) s->pSet->SetParticleV0(i, 0);
+    s->grid->UpdateQueryState();
+    LNMInvalidateCells(s->grid);
+    LNMBoundaryExtended(s->pSet, s->grid, (Float)h, max_level, 0, unbounded != 0);
+    for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
+}
+
+/* LNMBoundary with a geometric L2 filter (algorithm 1: Xiaowei, 2: Dilts spoke) through
+ * the reference's work queue (lnm.h:57-79, 258-289).  stats[0] = particles queued (L2
+ * cells), stats[1] = accepted as boundary. */
+void ref_lnm_geometric(RefSim *s, double h, int algorithm, int unbounded, int *levels, int *stats) {
+    for (int i = 0; i < s->n; i++) s->pSet->SetParticleV0(i, 0);
+    s->grid->UpdateQueryState();
+    LNMWorkQueue *q = cudaAllocateVx(LNMWorkQueue, 1);
+    q->SetSlots(s->n);
+    LNMBoundary(s->pSet, s->grid, (Float)h, algorithm, q, unbounded != 0);
+    stats[0] = q->size;
+    stats[1] = q->counter;
+    for (int i = 0; i < s->n; i++) levels[i] = s->pSet->GetParticleV0(i);
+}
+
+/* XiaoweiBoundary (src/boundaries/xiaowei.h:21-88) on the stored densities: 1 boundary. */
+void ref_xiaowei(RefSim *s, double h, int *flags) {
+    for (int i = 0; i < s->n; i++) flags[i] = XiaoweiParticleIsBoundary(s->pSet, s->grid, (Float)h, i);
+}
+
+/* DiltsSpokeBoundary (src/boundaries/dilts.h:110-163): 1 boundary. */
+void ref_dilts(RefSim *s, int *flags) {
+    for (int i = 0; i < s->n; i++) flags[i] = DiltsSpokeParticleIsBoundary(s->grid, s->pSet, i);
+}
+
+/* The spoke sample points of DiltsSpokeTakeUniformPoint around the origin for r = 1, in
+ * the reference's order; returns the count. */
+int ref_dilts_points(float *out, int cap) {
+    vec3f o(0, 0, 0);
+    int done = 0, i = 0, j = 0, k = 0;
+    while (!done) {
+        vec3f p = DiltsSpokeTakeUniformPoint(o, (Float)1, done, i, j, DILTS_LINEAR_SAMPLE_COUNT);
+        if (k < cap) {
+            out[3 * k] = (float)p.x;
+            out[3 * k + 1] = (float)p.y;
+            out[3 * k + 2] = (float)p.z;
+        }
+        k++;
+    }
+    return k;
+}
+
 /* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field
  * (nodes per axis, origin, spacing, values x fastest) at iso, single thread: the mesh's
  * points, normals and triangles (at most the capacities stored).  Returns the point count;

@@ -57,6 +57,12 @@ def load(variant):
                                               ctypes.POINTER(ctypes.c_float), _I32, ctypes.c_int, ctypes.c_int,
                                               ctypes.POINTER(ctypes.c_int)]),
         "ref_lnm": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
+        "ref_lnm_single": (None, [_P, ctypes.c_double, ctypes.c_int, _I32]),
+        "ref_lnm_extended": (None, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I32]),
+        "ref_lnm_geometric": (None, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I32, _I32]),
+        "ref_xiaowei": (None, [_P, ctypes.c_double, _I32]),
+        "ref_dilts": (None, [_P, _I32]),
+        "ref_dilts_points": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
         "ref_mesh_sdf": (ctypes.c_int, [_D, ctypes.c_int, _I32, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
         "ref_sdf_probe": (None, [_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, _I32]),
@@ -148,6 +154,36 @@ class RefSim:
         """LNMBoundary's particle levels (1, 2, 0 inside) on the current chains."""
         out = np.zeros(self.n, np.int32)
         self.lib.ref_lnm(self.h, float(h), int(bool(unbounded)), out.ctypes.data_as(_I32))
+        return out
+
+    def lnm_single(self, h, unbounded=False):
+        """LNMBoundarySingle's particle levels."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.ref_lnm_single(self.h, float(h), int(bool(unbounded)), out.ctypes.data_as(_I32))
+        return out
+
+    def lnm_extended(self, h, max_level=5, unbounded=False):
+        """LNMBoundaryExtended's particle levels."""
+        out = np.zeros(self.n, np.int32)
+        self.lib.ref_lnm_extended(self.h, float(h), int(max_level), int(bool(unbounded)), out.ctypes.data_as(_I32))
+        return out
+
+    def lnm_geometric(self, h, algorithm, unbounded=False):
+        """LNMBoundary with the Xiaowei (1) or Dilts (2) L2 filter: (levels, queued, accepted)."""
+        out = np.zeros(self.n, np.int32)
+        st = np.zeros(2, np.int32)
+        self.lib.ref_lnm_geometric(self.h, float(h), int(algorithm), int(bool(unbounded)),
+                                   out.ctypes.data_as(_I32), st.ctypes.data_as(_I32))
+        return out, int(st[0]), int(st[1])
+
+    def xiaowei(self, h):
+        out = np.zeros(self.n, np.int32)
+        self.lib.ref_xiaowei(self.h, float(h), out.ctypes.data_as(_I32))
+        return out
+
+    def dilts(self):
+        out = np.zeros(self.n, np.int32)
+        self.lib.ref_dilts(self.h, out.ctypes.data_as(_I32))
         return out
 
     def map_grid_emit(self, d, velocity=(0.0, 0.0, 0.0)):
@@ -263,6 +299,14 @@ def mesh_sdf(vertices, triangles, dx, margin, variant="f32"):
     vals = np.zeros(n, np.float32)
     lib.ref_mesh_sdf(*args, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n)
     return nodes, org, sp, vals
+
+
+def dilts_points(variant="f32"):
+    """DiltsSpokeTakeUniformPoint's points around the origin for r = 1, (k, 3) float32."""
+    lib = load(variant)
+    out = np.zeros((5000, 3), np.float32)
+    k = lib.ref_dilts_points(out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 5000)
+    return out[:k]
 
 
 def marching_cubes(nodes, origin, spacing, values, iso=0.0, rotate=False, variant="f32"):

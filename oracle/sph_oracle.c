@@ -1776,3 +1776,294 @@ void orc_lnm(const orc_sim *s, double h, int unbounded, int *levels) {
     }
     free(level);
 }
+
+/* LNMComputeDelta (lnm.h:24-33): (min cell length / h)^3 as a float power */
+static float lnm_pre_delta(const orc_sim *s, double h) {
+    Float minlen = s->g.len[0] < s->g.len[1] ? s->g.len[0] : s->g.len[1];
+    minlen = minlen < s->g.len[2] ? minlen : s->g.len[2];
+    return powf((float)minlen / (float)h, 3.0f);
+}
+
+/* the levels of cells at or below 2 written to their chains' particles */
+static void lnm_set_chain(const orc_sim *s, unsigned c, int L, int *levels) {
+    const int cur = s->active ? 1 : 0;
+    int node = s->head[cur][c];
+    for (int j = 0; j < s->clen[cur][c]; j++) {
+        levels[node] = L;
+        node = s->next[cur][node];
+    }
+}
+
+static void cell_coords(const ogrid *g, unsigned c, int u[3]) {
+    u[0] = (int)(c % (unsigned)g->dims[0]);
+    u[1] = (int)((c / (unsigned)g->dims[0]) % (unsigned)g->dims[1]);
+    u[2] = (int)(c / ((unsigned)g->dims[0] * (unsigned)g->dims[1]));
+}
+
+/* LNMBoundaryAreCoords1x1 (lnm.h:144-160): distinct cells at most one step apart per axis */
+static int lnm_1x1(const int a[3], const int b[3]) {
+    int eval = 0;
+    for (int q = 0; q < 3; q++) {
+        int ef = abs(a[q] - b[q]);
+        if (ef < 2) eval += ef;
+        else return 0;
+    }
+    return eval > 0 && eval <= 3;
+}
+
+/* LNMBoundarySingle (lnm.h:167-256): per cell with particles, L1 on the border; otherwise the
+ * 5x5x5 neighbourhood in the reference's order (y, x, z) stops at the first empty adjacent
+ * cell (L1) or the first adjacent cell with at most delta particles on the border (L2);
+ * without a stop, L2 when an adjacent cell with at most delta particles touches one of the
+ * empty cells met. */
+void orc_lnm_single(const orc_sim *s, double h, int unbounded, int *levels) {
+    const int cur = s->active ? 1 : 0;
+    const ogrid *g = &s->g;
+    const float pd = lnm_pre_delta(s, h);
+    const int pre = unbounded ? -1 : (int)pd;   /* the kernel's int parameter */
+    const int delta = pre > 0 ? pre : 2147483647;
+    for (int i = 0; i < s->n; i++) levels[i] = 0;
+    for (unsigned c = 0; c < g->total; c++) {
+        if (s->clen[cur][c] == 0) continue;
+        if (g->nbr_n[c] != 27) {
+            lnm_set_chain(s, c, 1, levels);
+            continue;
+        }
+        int u[3], src[125][3], cand[125][3], nsrc = 0, ncand = 0, is_l1 = 0, is_l2 = 0, stop = 0;
+        cell_coords(g, c, u);
+        for (int j = u[1] - 2; j <= u[1] + 2 && !stop; j++) {
+            if (j < 0 || j >= g->dims[1]) continue;
+            for (int i = u[0] - 2; i <= u[0] + 2 && !stop; i++) {
+                if (i < 0 || i >= g->dims[0]) continue;
+                for (int k = u[2] - 2; k <= u[2] + 2 && !stop; k++) {
+                    if (k < 0 || k >= g->dims[2]) continue;
+                    const int f[3] = {i, j, k};
+                    const unsigned fid = (unsigned)i + (unsigned)j * g->dims[0] + (unsigned)k * g->dims[0] * g->dims[1];
+                    if (fid == c) continue;
+                    const int n = s->clen[cur][fid];
+                    const int adj = lnm_1x1(f, u);
+                    if (n == 0) {
+                        if (adj) {
+                            is_l1 = 1;
+                            stop = 1;
+                        } else {
+                            memcpy(src[nsrc++], f, sizeof f);
+                        }
+                    } else if (adj && n <= delta) {
+                        if (g->nbr_n[fid] != 27) {
+                            is_l2 = 1;
+                            nsrc = ncand = 0;
+                            stop = 1;
+                        } else if (!is_l2) {
+                            memcpy(cand[ncand++], f, sizeof f);
+                        }
+                    }
+                }
+            }
+        }
+        if (is_l1) {
+            lnm_set_chain(s, c, 1, levels);
+        } else if (nsrc > 0 && ncand > 0) {
+            for (int a = 0; a < nsrc && !is_l2; a++)
+                for (int b = 0; b < ncand && !is_l2; b++) is_l2 = lnm_1x1(src[a], cand[b]);
+        }
+        if (is_l2) lnm_set_chain(s, c, 2, levels);
+    }
+}
+
+/* LNMBoundaryExtended (lnm.h:291-462): voxel levels by LNMComputeOnce sweeps (0: empty,
+ * 1: border or next to an empty cell, k: next to a level k-1 cell) for levels 0..max_level
+ * (or until a sweep changes nothing when max_level < 0); particle attributes from the cell
+ * of their hashed position; then the LK filter (a non-L1 cell next to an L1 cell holding at
+ * most delta particles: 2) and unfiltered level-2 cells promoted to 3. */
+void orc_lnm_extended(const orc_sim *s, double h, int max_level, int unbounded, int *levels) {
+    const int cur = s->active ? 1 : 0;
+    const ogrid *g = &s->g;
+    int *level = (int *)malloc(sizeof(int) * (g->total ? g->total : 1));
+    for (unsigned c = 0; c < g->total; c++) level[c] = -1;
+    int L = 0;
+    for (;;) {
+        int changed = 0;
+        for (unsigned c = 0; c < g->total; c++) {
+            if (level[c] > -1) continue;
+            if (s->clen[cur][c] == 0) {
+                level[c] = 0;
+                changed = 1;
+            } else if (g->nbr_n[c] != 27) {
+                level[c] = 1;
+                changed = 1;
+            } else if (L > 0) {
+                for (int q = 0; q < g->nbr_n[c]; q++) {
+                    const int nb = g->nbr[27 * (size_t)c + q];
+                    if ((unsigned)nb != c && level[nb] == L - 1) {
+                        level[c] = L;
+                        changed = 1;
+                        break;
+                    }
+                }
+            }
+        }
+        int done = !changed;
+        if (max_level > -1) done = L >= max_level;
+        if (done) break;
+        L++;
+    }
+    for (int i = 0; i < s->n; i++) {
+        const int lv = level[grid_hash(g, s->pos[i])];
+        levels[i] = lv > 0 ? lv : 0;
+    }
+    const float pd = unbounded ? -1.f : lnm_pre_delta(s, h);
+    const int delta = pd > 0 ? (int)pd : 2147483647;
+    for (unsigned c = 0; c < g->total; c++) {
+        if (s->clen[cur][c] > 0 && level[c] != 1) {
+            for (int q = 0; q < g->nbr_n[c]; q++) {
+                const int nb = g->nbr[27 * (size_t)c + q];
+                if (level[nb] == 1 && s->clen[cur][nb] <= delta) {
+                    level[c] = -2;
+                    lnm_set_chain(s, c, 2, levels);
+                    break;
+                }
+            }
+        } else if (level[c] == 1) {
+            lnm_set_chain(s, c, 1, levels);
+        }
+    }
+    for (unsigned c = 0; c < g->total; c++)
+        if (s->clen[cur][c] > 0 && level[c] == 2) lnm_set_chain(s, c, 3, levels);
+    free(level);
+}
+
+/* XiaoweiParticleIsBoundary (xiaowei.h:21-78): density below 0.7 of water's, or the
+ * std-kernel (radius 6h) weighted mean of the 27 cells' positions farther than 0.15 * 6h */
+static int xiaowei_is_boundary(const orc_sim *s, Float h, int id) {
+    const int cur = s->active ? 1 : 0;
+    const Float rhot = 0.7 * 1000.0;
+    const Float rho = 6.0 * h;
+    if (s->density[id] < rhot) return 1;
+    const v3 pi = s->pos[id];
+    const unsigned c = grid_hash(&s->g, pi);
+    const kern k = kern_std(rho);
+    Float wsum = 0;
+    v3 sum = V(0, 0, 0);
+    for (int q = 0; q < s->g.nbr_n[c]; q++) {
+        const int nb = s->g.nbr[27 * (size_t)c + q];
+        int node = s->head[cur][nb];
+        for (int j = 0; j < s->clen[cur][nb]; j++) {
+            const v3 pj = s->pos[node];
+            const Float w = std_W(&k, vlen(vsub(pi, pj)));
+            sum = vadd(sum, vmul(pj, w));
+            wsum += w;
+            node = s->next[cur][node];
+        }
+    }
+    const Float inv = (Float)1 / wsum;
+    sum = V(sum.x * inv, sum.y * inv, sum.z * inv);
+    const Float asym = vlen(vsub(pi, sum));
+    return asym > 0.15 * rho ? 1 : 0;
+}
+
+/* DiltsSpokeTakeUniformPoint's angles (dilts.h:70-97) with the C library's float sine and
+ * cosine: tab[0..64] sin u, [65..129] cos u, [130..194] sin v, [195..259] cos v */
+static void dilts_table(Float *tab) {
+    const Float samples = (Float)64;
+    for (int i = 0; i <= 64; i++) {
+        const Float u = i * ORC_PI / samples;
+        const Float v = i * 6.283185307179586 / samples;
+        tab[i] = FSIN(u);
+        tab[65 + i] = FCOS(u);
+        tab[130 + i] = FSIN(v);
+        tab[195 + i] = FCOS(v);
+    }
+}
+
+/* DiltsSpokeParticleIsBoundary (dilts.h:110-153): a spoke point of the sphere of radius
+ * 0.75 * spacing around the particle outside every overlapping neighbour's sphere */
+static int dilts_is_boundary(const orc_sim *s, int id, const Float *tab) {
+    const int cur = s->active ? 1 : 0;
+    const v3 pi = s->pos[id];
+    const unsigned c = grid_hash(&s->g, pi);
+    const Float rad = s->radius * 0.75;
+    v3 cand[1024];
+    int n = 0;
+    for (int q = 0; q < s->g.nbr_n[c]; q++) {
+        const int nb = s->g.nbr[27 * (size_t)c + q];
+        int node = s->head[cur][nb];
+        for (int j = 0; j < s->clen[cur][nb]; j++) {
+            if (node != id) {
+                const v3 pj = s->pos[node];
+                const Float d = vlen(vsub(pi, pj));
+                if (!(d > (rad + rad) - ORC_EPSILON) && n < 1024) cand[n++] = pj;
+            }
+            node = s->next[cur][node];
+        }
+    }
+    for (int i = 0; i <= 64; i++)
+        for (int j = 0; j <= 64; j++) {
+            const Float su = tab[i], cu = tab[65 + i], sv = tab[130 + j], cv = tab[195 + j];
+            const v3 dir = V(su * cv, su * sv, cu);
+            const v3 pt = vadd(vmul(dir, rad), pi);
+            int inside = 0;
+            for (int q = 0; q < n && !inside; q++)
+                if (vlen(vsub(cand[q], pt)) <= rad) inside = 1;
+            if (!inside) return 1;
+        }
+    return 0;
+}
+
+void orc_xiaowei(const orc_sim *s, double h, int *flags) {
+    for (int i = 0; i < s->n; i++) flags[i] = xiaowei_is_boundary(s, (Float)h, i);
+}
+
+void orc_dilts(const orc_sim *s, int *flags) {
+    Float tab[260];
+    dilts_table(tab);
+    for (int i = 0; i < s->n; i++) flags[i] = dilts_is_boundary(s, i, tab);
+}
+
+/* LNMBoundary with a geometric L2 filter (lnm.h:57-112, 258-289): L1 as the fast variant;
+ * the particles of L2 cells are queued and marked 2 only when the Xiaowei (1) or Dilts
+ * spoke (2) test finds them on the boundary.  stats: queued, accepted. */
+void orc_lnm_geometric(const orc_sim *s, double h, int algorithm, int unbounded, int *levels, int *stats) {
+    const int cur = s->active ? 1 : 0;
+    const ogrid *g = &s->g;
+    int *level = (int *)malloc(sizeof(int) * (g->total ? g->total : 1));
+    Float tab[260];
+    dilts_table(tab);
+    for (unsigned c = 0; c < g->total; c++) level[c] = -1;
+    for (int i = 0; i < s->n; i++) levels[i] = 0;
+    const float pd = unbounded ? -1.f : lnm_pre_delta(s, h);
+    const int delta = pd > 0 ? (int)pd : 2147483647;
+    for (unsigned c = 0; c < g->total; c++) {
+        if (s->clen[cur][c] < 1) continue;
+        int l1 = g->nbr_n[c] != 27;
+        for (int k = 0; k < g->nbr_n[c] && !l1; k++)
+            if (s->clen[cur][g->nbr[27 * (size_t)c + k]] == 0) l1 = 1;
+        if (l1) {
+            level[c] = 1;
+            lnm_set_chain(s, c, 1, levels);
+        }
+    }
+    stats[0] = stats[1] = 0;
+    for (unsigned c = 0; c < g->total; c++) {
+        if (s->clen[cur][c] < 1 || level[c] == 1) continue;
+        for (int k = 0; k < g->nbr_n[c]; k++) {
+            const int nb = g->nbr[27 * (size_t)c + k];
+            if (level[nb] == 1 && s->clen[cur][nb] <= delta) {
+                level[c] = 2;
+                int node = s->head[cur][c];
+                for (int j = 0; j < s->clen[cur][c]; j++) {
+                    stats[0]++;
+                    const int b = algorithm == 1 ? xiaowei_is_boundary(s, (Float)h, node)
+                                                 : dilts_is_boundary(s, node, tab);
+                    if (b > 0) {
+                        levels[node] = 2;
+                        stats[1]++;
+                    }
+                    node = s->next[cur][node];
+                }
+                break;
+            }
+        }
+    }
+    free(level);
+}

@@ -181,6 +181,11 @@ long     orc_map_grid_emit(const orc_sim *s, double distance, double *out, long 
  * an L1 cell holding at most delta = (min cell length / h)^3 particles; unbounded: any)
  * or 0. */
 void     orc_lnm(const orc_sim *s, double h, int unbounded, int *levels);
+void     orc_lnm_single(const orc_sim *s, double h, int unbounded, int *levels);
+void     orc_lnm_extended(const orc_sim *s, double h, int max_level, int unbounded, int *levels);
+void     orc_lnm_geometric(const orc_sim *s, double h, int algorithm, int unbounded, int *levels, int *stats);
+void     orc_xiaowei(const orc_sim *s, double h, int *flags);
+void     orc_dilts(const orc_sim *s, int *flags);
 
 /* Shape::ClosestDistance and IsInside of a box or sphere at n points (src/core/shape.cpp:
  * 206-232, 275-282): the values SetNodeSDFKernel (shape.cpp:409-424) signs into a field. */

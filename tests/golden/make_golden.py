@@ -34,6 +34,11 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
   lnm_f32.npz     LNMBoundary (boundaries/lnm.h, fast variant) levels of the 1,440-particle
                   scene after 3 as-shipped substeps and a fresh grid distribution, for
                   h = 0.01, 0.02, 0.04 and unbounded.
+  boundary_f32.npz  the other boundary classifications of boundaries/lnm.h, xiaowei.h and
+                  dilts.h (LNMBoundarySingle, LNMBoundaryExtended, LNMBoundary with the Xiaowei
+                  and Dilts L2 filters, XiaoweiBoundary, DiltsSpokeBoundary) of a jittered BCC
+                  sphere the reference's emitter made (srand(7)), with the densities the
+                  reference computed; and DiltsSpokeTakeUniformPoint's points for r = 1.
   mc_f32.npz      MarchingCubes (reconstruction/marching_cubes.cpp) of two fields on a 21x22x23
                   grid: two overlapping spheres' distance (iso 0) and a random field (every
                   cube configuration): the reference's points, normals and triangles.
@@ -49,6 +54,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py mesh      # mesh_f32.npz only
     python tests/golden/make_golden.py lnm       # lnm_f32.npz only
     python tests/golden/make_golden.py mc        # mc_f32.npz only
+    python tests/golden/make_golden.py boundary  # boundary_f32.npz only
 """
 import json
 import os
@@ -335,6 +341,44 @@ def make_lnm():
     np.savez_compressed(os.path.join(HERE, "lnm_f32.npz"), **out)
 
 
+# boundary fixture: a jittered BCC sphere emitted by the reference in the small container
+BOUNDARY_SPHERE = {"type": "sphere", "center": (0.0, -0.03, 0.0), "radius": 0.2}
+BOUNDARY_CASES = {
+    "single": [(0.02, 0), (0.04, 0), (0.02, 1)],
+    "extended": [(0.02, 5, 0), (0.02, 2, 0), (0.02, -1, 0), (0.04, 5, 1)],
+    "geometric": [(0.02, 1, 0), (0.04, 1, 0), (0.02, 2, 0)],
+    "xiaowei": [0.02, 0.01],
+}
+
+
+def boundary_scene():
+    sc = scenes.base_scene("pcisph", 0.02, (0.6, 0.5, 0.6))
+    sc["dt"] = 4e-4
+    pos, _ = R.emit_volume(BOUNDARY_SPHERE, 0.02, jitter=0.2, seed=7)
+    return sc, pos
+
+
+def make_boundary():
+    sc, pos = boundary_scene()
+    r = R.RefSim(sc, pos)
+    r.update_grid_distribution()
+    r.compute_density(0)
+    out = {"scene": np.array(json.dumps(clean(sc))), "pos": r.get(O.POSITION), "density": r.get(O.DENSITY),
+           "cases": np.array(json.dumps(BOUNDARY_CASES))}
+    for i, (h, ub) in enumerate(BOUNDARY_CASES["single"]):
+        out["single_%d" % i] = r.lnm_single(h, ub)
+    for i, (h, ml, ub) in enumerate(BOUNDARY_CASES["extended"]):
+        out["extended_%d" % i] = r.lnm_extended(h, ml, ub)
+    for i, (h, alg, ub) in enumerate(BOUNDARY_CASES["geometric"]):
+        lv, q, a = r.lnm_geometric(h, alg, ub)
+        out["geometric_%d" % i], out["geometric_stats_%d" % i] = lv, np.array([q, a], np.int32)
+    for i, h in enumerate(BOUNDARY_CASES["xiaowei"]):
+        out["xiaowei_%d" % i] = r.xiaowei(h)
+    out["dilts"] = r.dilts()
+    out["dilts_points"] = R.dilts_points()
+    np.savez_compressed(os.path.join(HERE, "boundary_f32.npz"), **out)
+
+
 # continuous emission cases: builder capacity, MapGridEmit distance, velocity
 CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
 
@@ -382,4 +426,6 @@ if __name__ == "__main__":
         make_lnm()
     if not what or what == ["mc"]:
         make_mc()
+    if not what or what == ["boundary"]:
+        make_boundary()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
