@@ -507,6 +507,30 @@ def postprocess(bb, scene, final_pos, device):
     s.close()
     out["marching_cubes"] = {"nodes": m ** 3, "points": len(pts), "triangles": len(tris), "ms": 1e3 * min(t[1:]),
                              "note": "field upload, both passes and the mesh download included"}
+    # the surface app on the final state: Zhu-Bridson field (kernel 2 x spacing, cells of
+    # 2 x spacing) and marching cubes, beside the oracle's field
+    sc = bb.surface_scene(final_pos, sp)
+    s = bb.Solver(sc, pos=final_pos, device=device)
+    t = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        s.update_grid_distribution()
+        nodes, org, spc, vals = s.particle_sdf("zhu", 2 * sp, sp)
+        pts, _, tris = s.marching_cubes(nodes, org, spc, vals, 0.0)
+        t.append(time.perf_counter() - t0)
+    s.close()
+    o = O.OracleSim(sc, final_pos)
+    o.update_grid_distribution()
+    t0 = time.perf_counter()
+    want = o.particle_sdf(0, 2 * sp, sp)
+    c = time.perf_counter() - t0
+    o.close()
+    out["surface_zhu_bridson"] = {"particles": len(final_pos), "field_nodes": int(np.prod(nodes)),
+                                  "triangles": len(tris), "ms": 1e3 * min(t[1:]), "cpu_field_ms": 1e3 * c,
+                                  "same_field_as_oracle": bool(np.array_equal(vals.view(np.uint32),
+                                                                              want[3].view(np.uint32))),
+                                  "note": "distribution, field, marching cubes and mesh download; the CPU leg is "
+                                          "the field alone"}
     out["measured"] = "host wall clock around the C-ABI calls (best of the repeats after the first)"
     return out
 

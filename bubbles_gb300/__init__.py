@@ -8,7 +8,7 @@ from ._native import BbgError, device_count, load  # noqa: F401
 from . import _native as native  # noqa: F401
 from .solver import (BatchSolver, PciSphSolver3, Solver, SphSolver3, build_grid,  # noqa: F401
                      compute_delta_denom, compute_mass, desc_from_scene, format_g,
-                     frame_section)
+                     frame_section, reconstruct_surface, surface_scene)
 from . import scenes  # noqa: F401
 
 FIELD_POSITION = native.FIELD_POSITION

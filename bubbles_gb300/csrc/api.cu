@@ -2945,6 +2945,94 @@ bbg_status bbg_boundary_test(bbg_solver s, int method, double h, int *flags) {
 }
 
 // ----------------------------------------------------------------------------
+// the surface app's particle-to-field step: ParticlesToSDF_Surface (apps/surface.cpp:388-470)
+// ----------------------------------------------------------------------------
+// The field's grid from the domain grid's bounds: by spacing, cells of 2 x mc_spacing from
+// pMin + half a cell, ceil(extent / cell) cells per axis; by resolution, that many nodes at
+// the largest of extent / (nodes - 1), from pMin + half of it.  Float operations as the app.
+static bbg_status particle_sdf_grid(bbg_solver s, double mc_spacing, const int *resolution, bbg_sdf_grid *g) {
+    const GridDev &d = s->P.g;
+    int cells[3];
+    float ds;
+    if (!resolution) {
+        if (!(mc_spacing > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need a positive marching-cubes spacing");
+        ds = (float)mc_spacing * 2.0f;
+        for (int k = 0; k < 3; k++) {
+            const float c = std::ceil((d.bmax[k] - d.bmin[k]) / ds);
+            if (!(c >= 0 && c <= 4096)) return fail(BBG_ERR_INVALID_ARGUMENT, "a field of %g cells across", (double)c);
+            cells[k] = (int)c;
+        }
+    } else {
+        float dk[3];
+        for (int k = 0; k < 3; k++) {
+            if (resolution[k] < 2 || resolution[k] > 4097)
+                return fail(BBG_ERR_INVALID_ARGUMENT, "resolution must be in [2, 4097] nodes per axis");
+            cells[k] = resolution[k] - 1;
+            dk[k] = (d.bmax[k] - d.bmin[k]) / (float)cells[k];
+        }
+        const float m12 = dk[1] < dk[2] ? dk[2] : dk[1];
+        ds = dk[0] < m12 ? m12 : dk[0];
+    }
+    memset(g, 0, sizeof(*g));
+    for (int k = 0; k < 3; k++) {
+        g->nodes[k] = cells[k] + 1;
+        g->origin[k] = d.bmin[k] + ds * 0.5f;
+        g->spacing[k] = ds;
+    }
+    return BBG_OK;
+}
+
+bbg_status bbg_particle_sdf(bbg_solver s, int method, double kernel_radius, double mc_spacing, const int *resolution,
+                            bbg_sdf_grid *grid, float *values, size_t capacity) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!grid) return fail(BBG_ERR_INVALID_ARGUMENT, "null grid");
+    if (method != BBG_SURFACE_ZHU_BRIDSON && method != BBG_SURFACE_SPH)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "unknown particle field method %d", method);
+    if (!(kernel_radius > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "need a positive kernel radius");
+    if (bbg_status r = particle_sdf_grid(s, mc_spacing, resolution, grid)) return r;
+    const size_t total = (size_t)grid->nodes[0] * grid->nodes[1] * grid->nodes[2];
+    if (!values) return BBG_OK;
+    if (capacity < total) return fail(BBG_ERR_CAPACITY, "the field has %zu nodes, room for %zu", total, capacity);
+    if (!s->setup_done || s->n <= 0) return fail(BBG_ERR_STATE, "no particles set up");
+    if (!s->grid_valid)
+        if (bbg_status r = grid_update(s)) return r;
+    if (method == BBG_SURFACE_SPH && !(s->valid & bit(BBG_FIELD_DENSITY)))
+        return fail(BBG_ERR_STATE, "the SPH field reads the particle densities: none are valid");
+    SurfaceArgs A;
+    memset(&A, 0, sizeof(A));
+    A.g = s->P.g;
+    A.iz = s->P.iz;
+    A.iz6 = s->P.iz6;
+    A.start = s->B.start;
+    A.pos = s->B.pos[s->state];
+    A.rho = s->B.rho;
+    A.method = method;
+    for (int k = 0; k < 3; k++) {
+        A.nodes[k] = grid->nodes[k];
+        A.org[k] = (float)grid->origin[k];
+        A.sp[k] = (float)grid->spacing[k];
+    }
+    const float dx = A.g.bmax[0] - A.g.bmin[0], dy = A.g.bmax[1] - A.g.bmin[1], dz = A.g.bmax[2] - A.g.bmin[2];
+    A.inf = std::sqrt(dx * dx + dy * dy + dz * dz);
+    A.radius = (float)kernel_radius;
+    A.offset = A.radius * 0.25f;
+    A.mass = s->mass;
+    A.r2 = A.radius * A.radius;
+    A.wc = 315.0 / (64.0 * 3.14159265358979323846 * (double)(A.r2 * A.radius));
+    float *d_out = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_out, sizeof(float) * total);
+    if (e == cudaSuccess) {
+        launch_particle_sdf(A, d_out, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(values, d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "particle field: %s", cudaGetErrorString(e));
+    return BBG_OK;
+}
+
+// ----------------------------------------------------------------------------
 // marching cubes (MarchingCubes, src/reconstruction/marching_cubes.cpp:204-457)
 // ----------------------------------------------------------------------------
 bbg_status bbg_marching_cubes(bbg_solver s, const bbg_sdf_grid *grid, const float *values, double iso,

@@ -134,6 +134,23 @@ void launch_lnm_extended_finish(const GridDev &g, float iz, const float4 *pos, c
 void launch_lnm_geometric(const BoundaryArgs &A, const unsigned *cell, int n, int delta, int algorithm,
                           int *level, int *queue, int *counts, int *out, cudaStream_t s);
 void launch_boundary_test(const BoundaryArgs &A, int algorithm, int n, int *out, cudaStream_t s);
+// surface.cu: ParticlesToSDF_Surface's field (method 0 Zhu-Bridson, 1 SPH)
+struct SurfaceArgs {
+    GridDev g;
+    float iz, iz6;
+    const unsigned *start;
+    const float4 *pos;
+    const float *rho;
+    int method;
+    int nodes[3];
+    float org[3], sp[3];
+    float inf;            // the domain grid's diagonal length
+    float radius;         // kernel radius
+    float offset;         // Zhu-Bridson: radius x threshold
+    float mass, r2;       // SPH: particle mass, radius squared,
+    double wc;            // 315 / (64 pi radius^3)
+};
+void launch_particle_sdf(const SurfaceArgs &A, float *out, cudaStream_t s);
 void launch_lnm(const GridDev &g, const unsigned *start, const unsigned *cell, const int *pid, int n, int delta,
                 int *level, int *out, cudaStream_t s);
 

@@ -69,6 +69,34 @@ def shapes_from_scene(scene):
 
 
 BOUNDARY_TESTS = {"xiaowei": 1, "dilts": 2}
+SURFACE_METHODS = {"zhu": 0, "sph": 1}
+
+
+def surface_scene(pos, spacing):
+    """The surface app's SPH set and domain for particles at `spacing`
+    (UtilBuildGridForBuilder: the positions' float bounds grown by the spacing, cells of
+    twice the spacing; SphSolver3::Setup with relative kernel radius 2, mass from
+    ComputeMass)."""
+    p = np.asarray(pos, np.float32).reshape(-1, 3)
+    sp = np.float32(spacing)
+    lo = p.min(axis=0) - sp
+    hi = p.max(axis=0) + sp
+    return {"solver": "sph", "spacing": float(spacing), "target_density": 1000.0, "relative_kernel_radius": 2.0,
+            "grid_spacing_scale": 2.0, "domain_min": tuple(float(x) for x in lo),
+            "domain_max": tuple(float(x) for x in hi), "colliders": [], "gravity": (0.0, 0.0, 0.0)}
+
+
+def reconstruct_surface(pos, spacing, kernel_radius, mc_spacing, method="zhu", iso=None, resolution=None,
+                        device=0):
+    """The reference's surface app on the device: particles -> field (Zhu-Bridson or SPH,
+    densities from the set's own density pass) -> MarchingCubes at iso (0 by default).
+    Returns (points, normals, triangles)."""
+    sc = surface_scene(pos, spacing)
+    with Solver(sc, pos=pos, device=device) as s:
+        s.update_grid_distribution()
+        s.compute_density(0)
+        nodes, org, sp, vals = s.particle_sdf(method, kernel_radius, mc_spacing, resolution)
+        return s.marching_cubes(nodes, org, sp, vals, 0.0 if iso is None else iso)
 
 
 class Solver:
@@ -220,6 +248,19 @@ class Solver:
                out["gradient"].ctypes.data, out["point"].ctypes.data, out["normal"].ctypes.data,
                out["distance"].ctypes.data, out["inside"].ctypes.data)
         return out
+
+    def particle_sdf(self, method="zhu", kernel_radius=0.04, mc_spacing=0.02, resolution=None):
+        """ParticlesToSDF_Surface's field over this solver's domain ("zhu" Zhu-Bridson, "sph"):
+        (nodes, origin, spacing, values), values x fastest."""
+        m = SURFACE_METHODS.get(method, method)
+        g = N.SdfGrid()
+        res = None if resolution is None else (ctypes.c_int * 3)(*[int(r) for r in resolution])
+        N.call("bbg_particle_sdf", self.h, int(m), float(kernel_radius), float(mc_spacing), res, ctypes.byref(g),
+               None, 0)
+        vals = np.empty(int(np.prod(g.nodes[:])), np.float32)
+        N.call("bbg_particle_sdf", self.h, int(m), float(kernel_radius), float(mc_spacing), res, ctypes.byref(g),
+               vals.ctypes.data, vals.size)
+        return np.array(g.nodes[:]), np.array(g.origin[:]), np.array(g.spacing[:]), vals
 
     def marching_cubes(self, nodes, origin, spacing, values, iso=0.0, rotate_faces=False):
         """MarchingCubes of a vertex-centred field on the device: (points, normals,

@@ -414,6 +414,25 @@ bbg_status bbg_lnm_boundary_geometric(bbg_solver s, double h, int algorithm, int
  * each boundary particle, one thread per particle. */
 bbg_status bbg_boundary_test(bbg_solver s, int method, double h, int *flags);
 
+/* ----- the surface app's particle field ------------------------------------------ */
+/* ParticlesToSDF_Surface (apps/surface.cpp:276-470): a vertex-centred field over the solver's
+ * domain grid for marching cubes.  The field's grid: with resolution NULL, cells of
+ * 2 x mc_spacing from the domain's min corner plus half a cell, ceil(extent / cell) cells
+ * per axis; else resolution[k] nodes at the largest of extent / (resolution - 1).  Each
+ * node outside the domain holds the domain's diagonal length; inside, over the particles of
+ * the 27 cells around it:
+ *   ZHU_BRIDSON: |p - x_avg| - 0.25 R, x_avg the mean of positions weighted by
+ *                max(0, (1 - (d/R)^2)^3) for d < R (the diagonal length when no weight);
+ *   SPH:         0.5 - sum (m / rho_j) W_std(d, R)  (BBG_FIELD_DENSITY must be valid).
+ * The app builds its domain from the particles' bounds grown by the spacing, on cells of
+ * twice the spacing, with an SPH set of that spacing and relative kernel radius 2.
+ * With values NULL only *grid is filled; otherwise capacity must hold every node.  One
+ * thread per node on the device. */
+#define BBG_SURFACE_ZHU_BRIDSON 0
+#define BBG_SURFACE_SPH 1
+bbg_status bbg_particle_sdf(bbg_solver s, int method, double kernel_radius, double mc_spacing, const int *resolution,
+                            bbg_sdf_grid *grid, float *values, size_t capacity);
+
 /* ----- marching cubes ----------------------------------------------------------- */
 /* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field
  * at iso on the device: a vertex on every grid edge whose ends straddle iso (at or below

@@ -120,6 +120,8 @@ def load(variant="f32"):
         "orc_lnm_geometric": (None, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I32, _I32]),
         "orc_xiaowei": (None, [_P, ctypes.c_double, _I32]),
         "orc_dilts": (None, [_P, _I32]),
+        "orc_particle_sdf": (ctypes.c_long, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _I32,
+                                             _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_long]),
         "orc_map_grid": (None, [_P]),
         "orc_map_grid_emit": (ctypes.c_long, [_P, ctypes.c_double, _D, ctypes.c_long]),
         "orc_shape_distance": (None, [ctypes.POINTER(Shape), ctypes.c_int, _D, _D, _I32]),
@@ -328,6 +330,21 @@ class OracleSim:
         out = np.zeros(self.n, np.int32)
         self.lib.orc_dilts(self.h, _ptr(out, _I32))
         return out
+
+    def particle_sdf(self, method, kernel, mc_spacing, resolution=None):
+        """The surface app's field (0 Zhu-Bridson, 1 SPH) over the domain grid and the stored
+        densities: (nodes, origin float32, spacing float32, values float32, x fastest)."""
+        res = np.zeros(3, np.int32) if resolution is None else np.ascontiguousarray(resolution, np.int32)
+        nodes = np.zeros(3, np.int32)
+        org = np.zeros(3)
+        sp = np.zeros(1)
+        args = lambda v, cap: (self.h, int(method), float(kernel), float(mc_spacing), int(resolution is not None),
+                               _ptr(res, _I32), _ptr(nodes, _I32), _ptr(org), _ptr(sp),
+                               v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), cap)
+        total = self.lib.orc_particle_sdf(*args(np.zeros(1, np.float32), 0))
+        vals = np.zeros(total, np.float32)
+        self.lib.orc_particle_sdf(*args(vals, total))
+        return nodes.copy(), org.astype(np.float32), np.float32(sp[0]), vals
 
     def map_grid(self):
         """ContinuousParticleSetBuilder3::MapGrid on the current chains."""

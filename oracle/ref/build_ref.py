@@ -32,7 +32,7 @@ SOURCES = [
     "shapes/sphere.cpp", "shapes/box.cpp", "shapes/sphere2.cpp", "shapes/rectangle2.cpp",
     "shapes/bvh.cpp", "generator/bcclattice.cpp", "generator/triangle.cpp",
     "equations/sph_equations2.cpp", "third/serializer.cpp", "third/obj_loader.cpp",
-    "reconstruction/marching_cubes.cpp",
+    "reconstruction/marching_cubes.cpp", "apps/surface.cpp", "third/ply_loader.cpp",
 ]
 LAUNCH = re.compile(r"(\w+)<<<\s*([^,>]+?)\s*,\s*([^>]+?)\s*>>>\s*\((.*)\);")
 

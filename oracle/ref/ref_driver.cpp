@@ -16,6 +16,8 @@
 #include <sph_solver.h>
 #include <transform.h>
 #include <util.h>
+#include <statics.h>
+#include <host_mesh.h>
 
 #include <cstdint>
 #include <cstring>
@@ -443,6 +445,112 @@ int ref_dilts_points(float *out, int cap) {
         k++;
     }
     return k;
+}
+
+} /* extern "C" */
+
+/* The surface app's options (apps/surface.cpp:19-32), declared here with the same layout so
+ * ParticlesToSDF_Surface can be called as the app calls it. */
+typedef struct {
+    Float kernel;
+    Float spacing;
+    Float marchingCubeSpacing;
+    Float iso;
+    std::string input;
+    std::string output;
+    int method;
+    int inflags;
+    int legacy;
+    bool byResolution;
+    vec3ui resolution;
+    TriangleMeshFormat outformat;
+} surface_opts;
+
+FieldGrid3f *ParticlesToSDF_Surface(ParticleSetBuilder3 *pBuilder, surface_opts *opts, TimerList &timer);
+Float ZhuBridsonSDF(vec3f p, Grid3 *grid, ParticleSet3 *pSet, Float kernelRadius, Float threshold);
+Float SphSDF(vec3f p, Grid3 *grid, ParticleSet3 *pSet, Float kernelRadius);
+
+extern "C" {
+
+/* The surface app's particle-to-field step (apps/surface.cpp:388-470, methods 0 Zhu-Bridson
+ * and 1 SPH).  direct = 1 calls ParticlesToSDF_Surface itself; direct = 0 runs the same steps
+ * with the reference's own pieces (UtilBuildGridForBuilder, SphSolver3::Setup, the grid
+ * distribution and density passes, FieldGrid3f::Build, ZhuBridsonSDF / SphSDF) so that the
+ * densities and the domain grid can be returned too.  Returns the node count (values up to
+ * cap stored); nodes[3], origin[3], spacing[1]; dom[6] the domain bounds; dens[n]. */
+long ref_surface_sdf(const double *pos, int n, double spacing, double kernel, double mc_spacing, int by_res,
+                     const int *res, int method, int direct, int *nodes, double *origin, double *sdf_spacing,
+                     float *values, long cap, double *dom, float *dens) {
+    SetCPUThreads(1);
+    SetSystemUseCPU();
+    ParticleSetBuilder3 builder;
+    for (int i = 0; i < n; i++) builder.AddParticle(V3(pos + 3 * i));
+    FieldGrid3f *g = nullptr;
+    if (direct) {
+        surface_opts opts;
+        opts.kernel = (Float)kernel;
+        opts.spacing = (Float)spacing;
+        opts.marchingCubeSpacing = (Float)mc_spacing;
+        opts.iso = 0;
+        opts.method = method;
+        opts.inflags = 0;
+        opts.legacy = 0;
+        opts.byResolution = by_res != 0;
+        opts.resolution = by_res ? vec3ui((unsigned)res[0], (unsigned)res[1], (unsigned)res[2]) : vec3ui(0);
+        TimerList timer;
+        g = ParticlesToSDF_Surface(&builder, &opts, timer);
+    } else {
+        const Float spacingScale = 2.0, threshold = 0.25, sp = (Float)spacing, radius = (Float)kernel;
+        Float sdfSpacing = (Float)mc_spacing;
+        Grid3 *grid = UtilBuildGridForBuilder(&builder, sp, spacingScale);
+        Bounds3f b = grid->GetBounds();
+        SphSolver3 solver;
+        SphParticleSet3 *sphpSet = SphParticleSet3FromBuilder(&builder);
+        ParticleSet3 *pSet = sphpSet->GetParticleSet();
+        solver.Initialize(DefaultSphSolverData3());
+        solver.Setup(WaterDensity, sp, spacingScale, grid, sphpSet);
+        UpdateGridDistributionGPU(solver.solverData);
+        ComputeDensityGPU(solver.solverData);
+        grid->UpdateQueryState();
+        g = cudaAllocateVx(FieldGrid3f, 1);
+        if (!by_res) {
+            sdfSpacing *= spacingScale;
+            vec3f p0 = b.pMin + 0.5 * vec3f(sdfSpacing);
+            int nx = std::ceil(b.ExtentOn(0) / sdfSpacing);
+            int ny = std::ceil(b.ExtentOn(1) / sdfSpacing);
+            int nz = std::ceil(b.ExtentOn(2) / sdfSpacing);
+            g->Build(vec3ui(nx, ny, nz), sdfSpacing, p0, VertexCentered);
+        } else {
+            vec3ui r = vec3ui((unsigned)res[0], (unsigned)res[1], (unsigned)res[2]) - vec3ui(1);
+            Float dx = b.ExtentOn(0) / (Float)r.x;
+            Float dy = b.ExtentOn(1) / (Float)r.y;
+            Float dz = b.ExtentOn(2) / (Float)r.z;
+            Float ds = Max(dx, Max(dy, dz));
+            vec3f p0 = b.pMin + 0.5 * vec3f(ds);
+            g->Build(r, ds, p0, VertexCentered);
+        }
+        Float inf = b.Diagonal().Length();
+        for (int i = 0; i < (int)g->total; i++) {
+            vec3ui u = DimensionalIndex(i, g->resolution, 3);
+            vec3f p = g->GetDataPosition(u);
+            Float estimate = inf;
+            if (method == 0) estimate = ZhuBridsonSDF(p, grid, pSet, radius, threshold);
+            else if (method == 1) estimate = SphSDF(p, grid, pSet, radius);
+            g->SetValueAt(estimate, u);
+        }
+        for (int k = 0; k < 3; k++) {
+            dom[k] = b.pMin[k];
+            dom[3 + k] = b.pMax[k];
+        }
+        for (int i = 0; i < n; i++) dens[i] = (float)pSet->GetParticleDensity(i);
+    }
+    for (int k = 0; k < 3; k++) {
+        nodes[k] = (int)g->resolution[k];
+        origin[k] = g->minPoint[k];
+    }
+    sdf_spacing[0] = g->spacing[0];
+    for (long q = 0; q < (long)g->total && q < cap; q++) values[q] = (float)g->field[q];
+    return (long)g->total;
 }
 
 /* MarchingCubes (src/reconstruction/marching_cubes.cpp:204-457) of a vertex-centred field

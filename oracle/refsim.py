@@ -63,6 +63,10 @@ def load(variant):
         "ref_xiaowei": (None, [_P, ctypes.c_double, _I32]),
         "ref_dilts": (None, [_P, _I32]),
         "ref_dilts_points": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+        "ref_surface_sdf": (ctypes.c_long, [_D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, _I32, ctypes.c_int, ctypes.c_int, _I32, _D, _D,
+                                            ctypes.POINTER(ctypes.c_float), ctypes.c_long, _D,
+                                            ctypes.POINTER(ctypes.c_float)]),
         "ref_mesh_sdf": (ctypes.c_int, [_D, ctypes.c_int, _I32, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         _I32, _D, _D, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
         "ref_sdf_probe": (None, [_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, _I32]),
@@ -299,6 +303,34 @@ def mesh_sdf(vertices, triangles, dx, margin, variant="f32"):
     vals = np.zeros(n, np.float32)
     lib.ref_mesh_sdf(*args, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n)
     return nodes, org, sp, vals
+
+
+def surface_sdf(pos, spacing, kernel, mc_spacing, method=0, resolution=None, direct=False, variant="f32"):
+    """The surface app's particle-to-field step (ParticlesToSDF_Surface; method 0 Zhu-Bridson,
+    1 SPH): dict of nodes, origin, spacing, values (x fastest) and, unless direct, the domain
+    grid's bounds and the particles' densities."""
+    lib = load(variant)
+    p = np.ascontiguousarray(pos, np.float64)
+    n = len(p)
+    res = np.zeros(3, np.int32) if resolution is None else np.ascontiguousarray(resolution, np.int32)
+    nodes = np.zeros(3, np.int32)
+    org = np.zeros(3)
+    sp = np.zeros(1)
+    dom = np.zeros(6)
+    dens = np.zeros(max(n, 1), np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    args = lambda vals, cap: (p.ctypes.data_as(_D), n, float(spacing), float(kernel), float(mc_spacing),
+                              int(resolution is not None), res.ctypes.data_as(_I32), int(method), int(bool(direct)),
+                              nodes.ctypes.data_as(_I32), org.ctypes.data_as(_D), sp.ctypes.data_as(_D),
+                              vals.ctypes.data_as(fp), cap, dom.ctypes.data_as(_D), dens.ctypes.data_as(fp))
+    total = lib.ref_surface_sdf(*args(np.zeros(1, np.float32), 0))
+    vals = np.zeros(total, np.float32)
+    lib.ref_surface_sdf(*args(vals, total))
+    out = {"nodes": nodes.copy(), "origin": org.astype(np.float32), "spacing": np.float32(sp[0]), "values": vals}
+    if not direct:
+        out["domain"] = dom.astype(np.float32)
+        out["density"] = dens[:n].copy()
+    return out
 
 
 def dilts_points(variant="f32"):

@@ -2010,6 +2010,92 @@ static int dilts_is_boundary(const orc_sim *s, int id, const Float *tab) {
     return 0;
 }
 
+/* The surface app's field (apps/surface.cpp:276-470, ParticlesToSDF_Surface with
+ * ZhuBridsonSDF (method 0) or SphSDF (1)) over the sim's domain grid and densities.  The
+ * field's grid: cells of 2 mc_spacing (by_res = 0) or res[k] nodes at the largest extent /
+ * (res - 1); origin the domain's min corner plus half a cell.  Returns the node count
+ * (values up to cap stored, x fastest). */
+long orc_particle_sdf(const orc_sim *s, int method, double kernel, double mc_spacing, int by_res, const int *res,
+                      int nodes[3], double origin[3], double *spacing, float *values, long cap) {
+    const int cur = s->active ? 1 : 0;
+    const ogrid *g = &s->g;
+    const v3 mn = g->b.mn, mx = g->b.mx;
+    Float ds;
+    int cells[3];
+    if (!by_res) {
+        ds = (Float)mc_spacing;
+        ds *= (Float)2.0;
+        for (int k = 0; k < 3; k++) {
+            const Float ext = vget(mx, k) - vget(mn, k);
+            cells[k] = (int)ceil(ext / ds);
+        }
+    } else {
+        Float dk[3];
+        for (int k = 0; k < 3; k++) {
+            cells[k] = res[k] - 1;
+            dk[k] = (vget(mx, k) - vget(mn, k)) / (Float)cells[k];
+        }
+        const Float m12 = dk[1] < dk[2] ? dk[2] : dk[1];
+        ds = dk[0] < m12 ? m12 : dk[0];
+    }
+    const Float half = ds * (Float)0.5;
+    const v3 org = V(mn.x + half, mn.y + half, mn.z + half);
+    for (int k = 0; k < 3; k++) {
+        nodes[k] = cells[k] + 1;
+        origin[k] = vget(org, k);
+    }
+    *spacing = ds;
+    const long total = (long)nodes[0] * nodes[1] * nodes[2];
+    const Float inf = vlen(vsub(mx, mn));
+    const Float R = (Float)kernel;
+    const kern kr = kern_std(R);
+    for (long q = 0; q < total && q < cap; q++) {
+        const unsigned ux = (unsigned)(q % nodes[0]), uy = (unsigned)((q / nodes[0]) % nodes[1]);
+        const unsigned uz = (unsigned)(q / ((long)nodes[0] * nodes[1]));
+        const v3 p = V(org.x + ds * (Float)ux, org.y + ds * (Float)uy, org.z + ds * (Float)uz);
+        if (!inside3(p, g->b)) {
+            values[q] = (float)inf;
+            continue;
+        }
+        const unsigned c = grid_hash(g, p);
+        Float wsum = 0;
+        v3 avg = V(0, 0, 0);
+        for (int k = 0; k < g->nbr_n[c]; k++) {
+            const int nb = g->nbr[27 * (size_t)c + k];
+            int node = s->head[cur][nb];
+            for (int j = 0; j < s->clen[cur][nb]; j++) {
+                const v3 xi = s->pos[node];
+                const Float d = vlen(vsub(p, xi));
+                if (method == 0) {
+                    if (d < R) {
+                        const Float t = d / R;
+                        const double cube = (1.0 - t * t) * (1.0 - t * t) * (1.0 - t * t);
+                        const Float cf = (Float)cube;
+                        const Float w = (Float)0 < cf ? cf : (Float)0;
+                        wsum += w;
+                        avg = vadd(avg, vmul(xi, w));
+                    }
+                } else {
+                    wsum += (s->mass / s->density[node]) * std_W(&kr, d);
+                }
+                node = s->next[cur][node];
+            }
+        }
+        Float v;
+        if (method != 0) {
+            v = (Float)0.5 - wsum;
+        } else if (wsum > 0) {
+            const Float inv = 1.0 / wsum;
+            avg = V(avg.x * inv, avg.y * inv, avg.z * inv);
+            v = vlen(vsub(p, avg)) - R * (Float)0.25;
+        } else {
+            v = inf;
+        }
+        values[q] = (float)v;
+    }
+    return total;
+}
+
 void orc_xiaowei(const orc_sim *s, double h, int *flags) {
     for (int i = 0; i < s->n; i++) flags[i] = xiaowei_is_boundary(s, (Float)h, i);
 }

@@ -186,6 +186,8 @@ void     orc_lnm_extended(const orc_sim *s, double h, int max_level, int unbound
 void     orc_lnm_geometric(const orc_sim *s, double h, int algorithm, int unbounded, int *levels, int *stats);
 void     orc_xiaowei(const orc_sim *s, double h, int *flags);
 void     orc_dilts(const orc_sim *s, int *flags);
+long     orc_particle_sdf(const orc_sim *s, int method, double kernel, double mc_spacing, int by_res, const int *res,
+                          int nodes[3], double origin[3], double *spacing, float *values, long cap);
 
 /* Shape::ClosestDistance and IsInside of a box or sphere at n points (src/core/shape.cpp:
  * 206-232, 275-282): the values SetNodeSDFKernel (shape.cpp:409-424) signs into a field. */

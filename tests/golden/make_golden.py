@@ -39,6 +39,10 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
                   and Dilts L2 filters, XiaoweiBoundary, DiltsSpokeBoundary) of a jittered BCC
                   sphere the reference's emitter made (srand(7)), with the densities the
                   reference computed; and DiltsSpokeTakeUniformPoint's points for r = 1.
+  surface_f32.npz the surface app's particle field (ParticlesToSDF_Surface, Zhu-Bridson and
+                  SPH, by spacing and by resolution) of the same sphere, the densities and
+                  domain it used (its own pieces, checked equal to the app function called
+                  directly), and the reference's MarchingCubes of the by-spacing fields.
   mc_f32.npz      MarchingCubes (reconstruction/marching_cubes.cpp) of two fields on a 21x22x23
                   grid: two overlapping spheres' distance (iso 0) and a random field (every
                   cube configuration): the reference's points, normals and triangles.
@@ -55,6 +59,7 @@ Float`, FP64 = as shipped) it stores the inputs and the reference's outputs:
     python tests/golden/make_golden.py lnm       # lnm_f32.npz only
     python tests/golden/make_golden.py mc        # mc_f32.npz only
     python tests/golden/make_golden.py boundary  # boundary_f32.npz only
+    python tests/golden/make_golden.py surface   # surface_f32.npz only
 """
 import json
 import os
@@ -379,6 +384,27 @@ def make_boundary():
     np.savez_compressed(os.path.join(HERE, "boundary_f32.npz"), **out)
 
 
+# surface fixture: (method, resolution or None) of ParticlesToSDF_Surface on the boundary
+# fixture's sphere, kernel radius 0.04, marching-cubes spacing 0.02
+SURFACE_CASES = [(0, None), (1, None), (0, (40, 36, 44)), (1, (40, 36, 44))]
+
+
+def make_surface():
+    pos, _ = R.emit_volume(BOUNDARY_SPHERE, 0.02, jitter=0.2, seed=7)
+    out = {"pos": pos, "cases": np.array(json.dumps(SURFACE_CASES))}
+    for i, (method, res) in enumerate(SURFACE_CASES):
+        r = R.surface_sdf(pos, 0.02, 0.04, 0.02, method, resolution=res)
+        d = R.surface_sdf(pos, 0.02, 0.04, 0.02, method, resolution=res, direct=True)
+        assert np.array_equal(r["values"].view(np.uint32), d["values"].view(np.uint32))
+        for k in ("nodes", "origin", "spacing", "values"):
+            out["%s_%d" % (k, i)] = r[k]
+        out["domain"], out["density"] = r["domain"], r["density"]
+        if res is None:
+            p, n, t = R.marching_cubes(r["nodes"], r["origin"], (float(r["spacing"]),) * 3, r["values"], 0.0)
+            out["mc_points_%d" % i], out["mc_normals_%d" % i], out["mc_triangles_%d" % i] = p, n, t
+    np.savez_compressed(os.path.join(HERE, "surface_f32.npz"), **out)
+
+
 # continuous emission cases: builder capacity, MapGridEmit distance, velocity
 CONTINUOUS_CASES = [(5000, 0.01, (0.1, 0.0, 0.0)), (1800, 0.01, (0.0, -0.5, 0.0))]
 
@@ -428,4 +454,6 @@ if __name__ == "__main__":
         make_mc()
     if not what or what == ["boundary"]:
         make_boundary()
+    if not what or what == ["surface"]:
+        make_surface()
     print("\n".join(sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))))
