@@ -248,7 +248,7 @@ bbg_status free_all(bbg_solver s) {
     void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
                     B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
                     B.cell_old, B.sub, B.count, B.start, B.partials, B.tmp, B.nbr, B.st, B.stage,
-                    B.red, B.list, B.inv_rho, B.pprev};
+                    B.red, B.list, B.inv_rho, B.pprev, B.soa};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     Prof *keep = B.prof;
@@ -909,6 +909,7 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.rho, n); ALLOC(B.press, n); ALLOC(B.rhostar, n); ALLOC(B.derr, n);
     ALLOC(B.cell, n); ALLOC(B.cell_old, n); ALLOC(B.sub, n); ALLOC(B.tmp, n); ALLOC(B.nbr, n);
     ALLOC(B.list, (size_t)kMaxList * n); ALLOC(B.inv_rho, n); ALLOC(B.pprev, n);
+    ALLOC(B.soa, 3 * (n + 1)); B.soa_stride = n + (n & 1);
     ALLOC(B.count, (size_t)s->cells); ALLOC(B.start, (size_t)s->cells + 1);
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);

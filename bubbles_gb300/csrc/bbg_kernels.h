@@ -34,6 +34,8 @@ struct DevBufs {
     ListEntry *list;           // member lists: kMaxList entries per particle,
                                // member-major (list[q * n + i]; tile.cuh)
     float *inv_rho;            // 1 / density
+    float *soa;                // density pass: step-start x, y, z as three arrays of soa_stride
+    size_t soa_stride;
     float *pprev;              // pressure of the previous substep, in the current order
     StepState *st;
     float *stage;              // n * 3 floats of staging for host copies

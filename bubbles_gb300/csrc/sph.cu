@@ -44,6 +44,38 @@ constexpr int kDensityMinBlocks = 12 * kTile / kMaxTile;
 // density pass: branch-free candidate loop with membership bit masks (build-time choice;
 // measured 4 % faster than the branchy loop on GB300)
 constexpr bool kDensityMask = BBG_DENSITY_MASK != 0;
+#ifndef BBG_DENSITY_X2
+#define BBG_DENSITY_X2 1
+#endif
+// density pass on packed pairs of candidates (f32x2 arithmetic on structure-of-arrays
+// positions; build-time choice)
+constexpr bool kDensityX2 = BBG_DENSITY_X2 != 0;
+
+// Two floats in one 64-bit register pair, for the packed f32x2 instructions of sm_100+.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2_pack(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 
 // a neighbour's position and velocity records
 struct PosVel {
@@ -152,6 +184,109 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     nbr[i] = cnt;
     if (P.nscenes > 0) P.scene[i] = (unsigned short)scene_of(P, pi.z);
     if (listed > kMaxList || !fits) cell[i] = cw | kWide;
+    if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
+}
+
+// Structure-of-arrays copy of the positions for the packed density pass.
+__global__ void __launch_bounds__(kThreads)
+k_soa(int n, const float4 *__restrict__ pos, float *__restrict__ sx, float *__restrict__ sy, float *__restrict__ sz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    sx[i] = p.x;
+    sy[i] = p.y;
+    sz[i] = p.z;
+}
+
+// k_density with candidates taken two at a time: the even-aligned pairs of each 32-candidate
+// chunk load x, y, z as float2 from the structure-of-arrays copy and compute both squared
+// distances and kernel terms with f32x2 instructions; the membership test, the sums (one per
+// lane of the pair) and the member list are those of k_density.
+__global__ void __launch_bounds__(kMaxTile, kDensityMinBlocks)
+k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
+             const unsigned *__restrict__ start, const float *__restrict__ sx, const float *__restrict__ sy,
+             const float *__restrict__ sz, float *__restrict__ rho, float *__restrict__ inv_rho,
+             float *__restrict__ press, int *__restrict__ nbr, ListEntry *__restrict__ list, int compute_pressure,
+             StepState *st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 pi = pos[i];
+    const unsigned cw = cell[i];
+    const size_t n = (size_t)P.n;
+    float s0 = 0.f, s1 = 0.f;
+    int cnt = 0;      // bucket members, i included
+    int listed = 0;   // members other than i
+    const bool crowded = candidate_count(P.g, start, cw & ~kWide) > kMaxCandidates;
+    if (crowded) {
+        s0 = 1.f;
+        cnt = 1;
+        atomicAdd(&st->crowded, 1u);
+    } else {
+        const f2 X = f2_pack(pi.x, pi.x), Y = f2_pack(pi.y, pi.y), Z = f2_pack(pi.z, pi.z);
+        const f2 NIH = f2_pack(-P.inv_h2, -P.inv_h2), ONE = f2_pack(1.f, 1.f);
+        const float lo = P.nb_lo, hi = P.nb_hi, ih2 = P.inv_h2;
+        tile_rows(P.g, start, cw & ~kWide, [&](int, unsigned b, unsigned e) {
+            for (unsigned cb = b; cb < e; cb += 32u) {
+                const unsigned ce = min(e, cb + 32u);
+                unsigned m = 0u;
+                unsigned j = cb;
+                auto single = [&](unsigned q) {
+                    const float4 pj = make_float4(__ldg(&sx[q]), __ldg(&sy[q]), __ldg(&sz[q]), 0.f);
+                    const float r2 = dist2(pi, pj);
+                    const bool mem = r2 < lo || (r2 <= hi && std_member_exact(P, pi, pj));
+                    const float x = 1.f - r2 * ih2;
+                    s0 += mem ? x * x * x : 0.f;
+                    m |= (unsigned)mem << (q - cb);
+                };
+                if (j & 1u) single(j++);
+                for (; j + 1u < ce; j += 2u) {
+                    const float2 ax = __ldg(reinterpret_cast<const float2 *>(sx + j));
+                    const float2 ay = __ldg(reinterpret_cast<const float2 *>(sy + j));
+                    const float2 az = __ldg(reinterpret_cast<const float2 *>(sz + j));
+                    const f2 dx = f2_sub(f2_pack(ax.x, ax.y), X);
+                    const f2 dy = f2_sub(f2_pack(ay.x, ay.y), Y);
+                    const f2 dz = f2_sub(f2_pack(az.x, az.y), Z);
+                    const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                    const f2 x = f2_fma(r2, NIH, ONE);
+                    const f2 x3 = f2_mul(f2_mul(x, x), x);
+                    float r0, r1, c0, c1;
+                    f2_unpack(r2, r0, r1);
+                    f2_unpack(x3, c0, c1);
+                    bool m0 = r0 < lo, m1 = r1 < lo;
+                    if ((!m0 && r0 <= hi) || (!m1 && r1 <= hi)) {   // rare: the exact test's band
+                        if (!m0 && r0 <= hi) m0 = std_member_exact(P, pi, make_float4(ax.x, ay.x, az.x, 0.f));
+                        if (!m1 && r1 <= hi) m1 = std_member_exact(P, pi, make_float4(ax.y, ay.y, az.y, 0.f));
+                    }
+                    s0 += m0 ? c0 : 0.f;
+                    s1 += m1 ? c1 : 0.f;
+                    m |= ((unsigned)m0 | ((unsigned)m1 << 1)) << (j - cb);
+                }
+                if (j < ce) single(j);
+                cnt += __popc(m);
+                if ((unsigned)i - cb < ce - cb) m &= ~(1u << ((unsigned)i - cb));   // the particle itself
+                while (m) {
+                    const unsigned q = cb + (unsigned)(__ffs((int)m) - 1);
+                    m &= m - 1u;
+                    if (listed < kMaxList) list[(size_t)listed * n + (size_t)i] = list_code(q, 0u);
+                    listed++;
+                }
+            }
+        });
+    }
+    const float di = (s0 + s1) * P.std_c * P.mass;
+    if (compute_pressure) {
+        float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
+        if (p < 0.f) p *= P.neg_scale;
+        press[i] = p;
+        reinterpret_cast<float *>(&pos[i])[3] = p / (di * di);   // pos.w = p / rho^2
+    }
+    rho[i] = di;
+    const float ir = 1.f / di;
+    inv_rho[i] = ir;
+    reinterpret_cast<float *>(&vel[i])[3] = ir;                   // vel.w = 1 / rho
+    nbr[i] = cnt;
+    if (P.nscenes > 0) P.scene[i] = (unsigned short)scene_of(P, pi.z);
+    if (listed > kMaxList) cell[i] = cw | kWide;
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
@@ -582,8 +717,16 @@ __global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
     const int t = B.tune.block;
-    k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
-                                               B.press, B.nbr, B.list, compute_pressure, B.st);
+    if (kDensityX2 && !kListRelative) {
+        float *sx = B.soa, *sy = B.soa + B.soa_stride, *sz = B.soa + 2 * B.soa_stride;
+        k_soa<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], sx, sy, sz);
+        k_density_x2<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, sx, sy, sz,
+                                                      B.rho, B.inv_rho, B.press, B.nbr, B.list, compute_pressure,
+                                                      B.st);
+    } else {
+        k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
+                                                   B.press, B.nbr, B.list, compute_pressure, B.st);
+    }
     BBG_PEND(B, s);
 }
 
