@@ -535,6 +535,28 @@ def postprocess(bb, scene, final_pos, device):
     return out
 
 
+def energy_log(g, scene, substeps, path=None, every=10):
+    """FP64 mass and energy of the state every `every` substeps of a run after the timed
+    region (device reductions, bbg_energy), as JSONL records; optionally written to `path`."""
+    dt = scene["dt"]
+    recs = []
+    for k in range(substeps + 1):
+        if k % every == 0:
+            e = g.energy()
+            recs.append({"substep": k, "mass": e["mass"], "kinetic": e["kinetic"], "potential": e["potential"],
+                         "total": e["kinetic"] + e["potential"], "momentum": [float(x) for x in e["momentum"]]})
+        if k < substeps:
+            g.advance_time_step(dt)
+    if path:
+        with open(path, "w") as f:
+            for r in recs:
+                f.write(json.dumps(r) + "\n")
+    tot = [r["total"] for r in recs]
+    return {"every": every, "substeps": substeps, "records": recs,
+            "mass_change": recs[-1]["mass"] - recs[0]["mass"], "energy_change": tot[-1] - tot[0],
+            "measured": "FP64 device reductions after the timed region (gravity potential against the origin)"}
+
+
 def run_ours(args, scene, pos):
     import torch
 
@@ -676,6 +698,10 @@ def run_ours(args, scene, pos):
         sampler.stop()
         final_pos, final_vel = pos_h.copy(), vel_h.copy()
         batch_offsets = g.layout() if scene.get("batch") else None
+        energy = None
+        steps_e = args.energy_steps if args.energy_steps >= 0 else (100 if args.config == "pcisph_4m" else 0)
+        if steps_e > 0 and rank == 0:
+            energy = energy_log(g, scene, steps_e, args.energy_log)
         frames = seeds = post = None
         if not scene.get("batch") and not args.no_frames and rank == 0:
             frames = frame_io(bb, g, scene, n, local)
@@ -780,6 +806,8 @@ def run_ours(args, scene, pos):
     if seeds is not None:
         line["seeding"] = seeds
         line["postprocess"] = post
+    if energy is not None:
+        line["energy_log"] = energy
     print(json.dumps(line), flush=True)
     barrier(dist)
 
@@ -798,6 +826,10 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cpu-slab", type=int, default=32, help="z-layers of the block for the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--energy-steps", type=int, default=-1,
+                    help="substeps of FP64 mass/energy logging after the timed region (every 10); "
+                         "default 100 for pcisph_4m, else none")
+    ap.add_argument("--energy-log", default=None, help="JSONL file for the mass/energy records")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
     ap.add_argument("--no-frames", action="store_true",
                     help="skip the particle-frame and seeding timings (frame writer / reader, emitters)")

@@ -1382,6 +1382,31 @@ bbg_status bbg_get_scalars(bbg_solver s, double out[8]) {
     return BBG_OK;
 }
 
+// FP64 totals of the state: mass, kinetic energy, potential energy and momentum
+bbg_status bbg_energy(bbg_solver s, double out[6]) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!out) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");
+    if (s->n <= 0) return fail(BBG_ERR_STATE, "no particles");
+    const int nb = energy_blocks(s->n);
+    double *d = nullptr;
+    std::vector<double> h((size_t)nb * kEnergyTerms);
+    cudaError_t e = cudaMalloc((void **)&d, sizeof(double) * h.size());
+    if (e == cudaSuccess) {
+        launch_energy(s->P, s->B, s->state, s->desc.gravity, d, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(BBG_ERR_CUDA, "energy: %s", cudaGetErrorString(e));
+    for (int t = 0; t < kEnergyTerms; t++) {
+        double v = 0.0;
+        for (int b = 0; b < nb; b++) v += h[(size_t)b * kEnergyTerms + t];
+        out[t] = v;
+    }
+    return BBG_OK;
+}
+
 bbg_status bbg_get_grid(bbg_solver s, int dims[3], double geo[12]) {
     if (bbg_status r = check_solver(s)) return r;
     if (!dims || !geo) return fail(BBG_ERR_INVALID_ARGUMENT, "null output");

@@ -97,6 +97,10 @@ void launch_sph_forces(const Params &P, const DevBufs &B, int buf, float dt, cud
 void launch_accumulate_integrate(const Params &P, const DevBufs &B, int buf, float dt,
                                  cudaStream_t s);
 void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cudaStream_t s);
+// FP64 totals (mass, kinetic, potential, momentum x, y, z): energy_blocks(n) partial rows
+constexpr int kEnergyTerms = 6;
+int energy_blocks(int n);
+void launch_energy(const Params &P, const DevBufs &B, int buf, const double g[3], double *partial, cudaStream_t s);
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
                              cudaStream_t s);
 

@@ -840,6 +840,49 @@ void launch_integrate(const Params &P, const DevBufs &B, int buf, float dt, cuda
     BBG_PEND(B, s);
 }
 
+// FP64 totals of the particle state: mass, kinetic energy, potential energy in the constant
+// gravity field and momentum.  One partial row per block, summed by the host in block order,
+// so the totals do not depend on scheduling.
+constexpr int kEnergyBlocks = 1024;
+__global__ void __launch_bounds__(kThreads)
+k_energy(int n, const float4 *__restrict__ pos, const float4 *__restrict__ vel, double mass, double gx, double gy,
+         double gz, double *__restrict__ partial) {
+    double acc[kEnergyTerms] = {0, 0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos[i], v = vel[i];
+        const double vx = v.x, vy = v.y, vz = v.z;
+        acc[0] += mass;
+        acc[1] += 0.5 * mass * (vx * vx + vy * vy + vz * vz);
+        acc[2] -= mass * (gx * (double)p.x + gy * (double)p.y + gz * (double)p.z);
+        acc[3] += mass * vx;
+        acc[4] += mass * vy;
+        acc[5] += mass * vz;
+    }
+    __shared__ double red[kThreads / 32][kEnergyTerms];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int t = 0; t < kEnergyTerms; t++) {
+        const double v = warp_sum_d(acc[t]);
+        if (lane == 0) red[wid][t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kEnergyTerms) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w][threadIdx.x];
+        partial[blockIdx.x * kEnergyTerms + threadIdx.x] = v;
+    }
+}
+
+int energy_blocks(int n) {
+    const int b = blocks_for(n, kThreads);
+    return b < kEnergyBlocks ? (b > 0 ? b : 1) : kEnergyBlocks;
+}
+
+void launch_energy(const Params &P, const DevBufs &B, int buf, const double g[3], double *partial, cudaStream_t s) {
+    k_energy<<<energy_blocks(P.n), kThreads, 0, s>>>(P.n, B.pos[buf], B.vel[buf], (double)P.mass, g[0], g[1], g[2],
+                                                     partial);
+}
+
 void launch_pseudo_viscosity(const Params &P, const DevBufs &B, int new_buf, float factor,
                              cudaStream_t s) {
     BBG_PBEGIN(B, KID_PSEUDO_VISCOSITY, s, -1);

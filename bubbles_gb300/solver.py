@@ -249,6 +249,12 @@ class Solver:
                out["distance"].ctypes.data, out["inside"].ctypes.data)
         return out
 
+    def energy(self):
+        """FP64 totals of the state: mass, kinetic, potential, momentum (3)."""
+        out = np.zeros(6)
+        N.call("bbg_energy", self.h, out.ctypes.data)
+        return {"mass": out[0], "kinetic": out[1], "potential": out[2], "momentum": out[3:6].copy()}
+
     def particle_sdf(self, method="zhu", kernel_radius=0.04, mc_spacing=0.02, resolution=None):
         """ParticlesToSDF_Surface's field over this solver's domain ("zhu" Zhu-Bridson, "sph"):
         (nodes, origin, spacing, values), values x fastest."""

@@ -545,6 +545,11 @@ bbg_status bbg_download_device(bbg_solver s, float *d_pos, float *d_vel);
  * target density, particle radius, relative kernel radius. */
 bbg_status bbg_get_scalars(bbg_solver s, double out[8]);
 bbg_status bbg_get_grid(bbg_solver s, int dims[3], double geo[12]);
+/* FP64 totals of the current state, reduced on the device (fixed block partials summed in
+ * order, so repeatable): out = {mass, kinetic energy sum m|v|^2/2, potential energy
+ * -sum m g.x in the scene's gravity, momentum x, y, z}.  The run logs of the large
+ * configuration record them every 10 substeps. */
+bbg_status bbg_energy(bbg_solver s, double out[6]);
 /* Grid state after the last update: cell id of each particle (caller order),
  * particle count per cell, and particle ids in cell-sorted order (stable by id). */
 bbg_status bbg_dump_grid(bbg_solver s, uint32_t *cell_of_particle, uint32_t *cell_counts,

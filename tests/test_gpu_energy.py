@@ -1,0 +1,34 @@
+"""FP64 mass / energy / momentum reductions of the particle state (bbg_energy), against the
+same sums in numpy FP64 over the downloaded state."""
+import numpy as np
+import pytest
+
+import bubbles_gb300 as bb
+
+pytestmark = pytest.mark.gpu
+
+
+def test_energy_matches_numpy(gpu, small):
+    sc, pos = small
+    with bb.Solver(sc, pos=pos) as s:
+        for _ in range(5):
+            s.advance_time_step(sc["dt"])
+        p, v = s.download()
+        e = s.energy()
+        m = s.scalars()["mass"]
+    p = p.astype(np.float64)
+    v = v.astype(np.float64)
+    g = np.array(sc["gravity"], np.float64)
+    assert e["mass"] == pytest.approx(m * len(p), rel=1e-12)
+    assert e["kinetic"] == pytest.approx(0.5 * m * np.sum(v * v), rel=1e-10)
+    assert e["potential"] == pytest.approx(-m * np.sum(p @ g), rel=1e-10, abs=1e-12)
+    assert np.allclose(e["momentum"], m * v.sum(axis=0), rtol=1e-10, atol=1e-12)
+    assert e["kinetic"] > 0
+
+
+def test_energy_is_repeatable(gpu, small):
+    sc, pos = small
+    with bb.Solver(sc, pos=pos) as s:
+        s.advance_time_step(sc["dt"])
+        a, b = s.energy(), s.energy()
+    assert a["kinetic"] == b["kinetic"] and a["potential"] == b["potential"]
