@@ -112,7 +112,8 @@ class StepStats(ctypes.Structure):
                 ("neighbor_overflow", ctypes.c_int),
                 ("out_of_grid", ctypes.c_int),
                 ("max_force", ctypes.c_double),
-                ("crowded", ctypes.c_int)]
+                ("crowded", ctypes.c_int),
+                ("nonfinite", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -423,6 +423,7 @@ void add_substep_stats(bbg_solver s, float dt) {
     a.neighbor_overflow = (int)st->nbr_overflow;
     a.out_of_grid = (int)st->out_of_grid;
     a.crowded = (int)st->crowded;
+    a.nonfinite = (int)st->nonfinite;
     float f;
     memcpy(&f, &st->max_force_bits, 4);
     a.max_force = f;

@@ -84,6 +84,16 @@ struct PosVel {
 
 static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
+__device__ __forceinline__ bool finite_state(v3 x, v3 v) {
+    return isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+}
+
+// warp-aggregated count of the lanes with a non-finite integrated state (all lanes call it)
+__device__ __forceinline__ void count_nonfinite(bool bad, StepState *st) {
+    const unsigned m = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(&st->nonfinite, (unsigned)__popc(m));
+}
+
 // True when some corrector iteration before k already met the tolerance
 // (ComputePressureForceAndIntegrate's break, pcisph_equations3.cpp:243-246).
 __device__ __forceinline__ bool converged_before(const Params &P, const StepState *st, int k) {
@@ -519,6 +529,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
+    bool bad = false;   // integrated position or velocity not finite
     bool active = i < P.n;
     if (active && P.nscenes > 0) {
         // batch: each scene stops at its own convergence
@@ -558,6 +569,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
             pos_out[i] = F4(x);
             vel_out[i] = F4(v);
             fbits = __float_as_uint(vlen(ft));
+            bad = !finite_state(x, v);
         } else if (mode != 1) {
             v3 xs;
             predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
@@ -566,6 +578,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
     }
     fbits = warp_max_u(fbits);
     if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
+    count_nonfinite(bad, st);
 }
 
 // End of one corrector iteration in the graph-driven loop: stop when the density error
@@ -593,6 +606,7 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
     tile_setup(P.g, cell, start, P.n, T);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned fbits = 0;
+    bool bad = false;   // integrated position or velocity not finite
     if (i < P.n) {
         const float4 pi = pos[i];
         const float4 vi = vel[i];
@@ -632,9 +646,11 @@ k_sph_forces(Params P, const float4 *__restrict__ pos, const float4 *__restrict_
         pos_out[i] = F4(x);
         vel_out[i] = F4(v);
         fbits = __float_as_uint(vlen(f));
+        bad = !finite_state(x, v);
     }
     fbits = warp_max_u(fbits);
     if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
+    count_nonfinite(bad, st);
 }
 
 // AccumulateForcesFor + TimeIntegrationFor (AccumulateAndIntegrateGPU,

@@ -142,6 +142,8 @@ typedef struct {
     double max_force;                 /* max |F| after the last substep (CFL input) */
     int crowded;                      /* cells / particles past the work caps of a degenerate
                                          state (a cell of > 512 particles, > 1,024 candidates) */
+    int nonfinite;                    /* particles whose integrated position or velocity is
+                                         not finite (NaN or infinite) in the last substep */
 } bbg_step_stats;
 
 /* Learned warm start (pressure_init = BBG_PRESSURE_INIT_LEARNED): a per-particle MLP

@@ -32,3 +32,20 @@ def test_energy_is_repeatable(gpu, small):
         s.advance_time_step(sc["dt"])
         a, b = s.energy(), s.energy()
     assert a["kinetic"] == b["kinetic"] and a["potential"] == b["potential"]
+
+
+def test_nonfinite_state_is_counted(gpu, small):
+    """Failure detection without a GPU fault: a NaN planted in the host input spreads
+    through its neighbours and the step reports the non-finite particles; a healthy run
+    reports none."""
+    sc, pos = small
+    with bb.Solver(sc, pos=pos) as s:
+        st = s.advance_time_step(sc["dt"], stats=True)
+        assert st["nonfinite"] == 0
+    bad = np.array(pos, np.float32)
+    bad[len(bad) // 2, 1] = np.nan
+    with bb.Solver(sc, pos=bad) as s:
+        st = s.advance_time_step(sc["dt"], stats=True)
+        assert st["nonfinite"] >= 1
+        p, _ = s.download()
+        assert np.isnan(p).any(axis=1).sum() == st["nonfinite"]
