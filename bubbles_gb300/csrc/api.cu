@@ -2737,6 +2737,19 @@ bbg_status mesh_field(bbg_solver s, const float *vertices, int nv, const int *tr
     for (int q = 0; q < 4; q++)
         gam[q] = (float)(((double)(float)ns[q] * 5.96046e-08) / (1 - (double)(float)ns[q] * 5.96046e-08));
     const size_t total = (size_t)g->nodes[0] * g->nodes[1] * g->nodes[2];
+    // tiles of consecutive triangles with their boxes; the distance margin is 1e-3 of the
+    // mesh's bounding diagonal
+    const size_t ntile = (size_t)mesh_tiles(nt);
+    std::vector<float> tiles(6 * ntile), dtri(9 * (size_t)nt), dtiles(6 * ntile);
+    mesh_tile_bounds(tri.data(), nt, tiles.data());
+    mesh_morton_order(tri.data(), nt, lo, hi, dtri.data());
+    mesh_tile_bounds(dtri.data(), nt, dtiles.data());
+    const double ex = (double)hi[0] - lo[0], ey = (double)hi[1] - lo[1], ez = (double)hi[2] - lo[2];
+    const float margin_abs = (float)(1e-3 * std::sqrt(ex * ex + ey * ey + ez * ez));
+    // one upload: triangles, their tiles, the Morton-ordered triangles, their tiles
+    tri.insert(tri.end(), tiles.begin(), tiles.end());
+    tri.insert(tri.end(), dtri.begin(), dtri.end());
+    tri.insert(tri.end(), dtiles.begin(), dtiles.end());
     float *d_tri = nullptr, *d_out = nullptr;
     unsigned *d_stuck = nullptr;
     cudaError_t e = cudaMalloc((void **)&d_tri, sizeof(float) * tri.size());
@@ -2746,7 +2759,9 @@ bbg_status mesh_field(bbg_solver s, const float *vertices, int nv, const int *tr
     if (e == cudaSuccess) e = cudaMemsetAsync(d_stuck, 0, sizeof(unsigned), s->stream);
     unsigned h_stuck = 0;
     if (e == cudaSuccess) {
-        launch_mesh_sdf(d_tri, nt, field_dev(*g, d_out), lo, hi, gam, d_out, d_stuck, s->stream);
+        const float *d_tiles = d_tri + 9 * (size_t)nt, *d_dtri = d_tiles + 6 * ntile;
+        launch_mesh_sdf(d_tri, nt, d_tiles, d_dtri, d_dtri + 9 * (size_t)nt, margin_abs, field_dev(*g, d_out), lo, hi,
+                        gam, d_out, d_stuck, s->stream);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_stuck, d_stuck, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream);

@@ -112,8 +112,14 @@ void launch_shape_query(const Params &P, int index, int n, const float *pts, flo
 
 // GenerateShapeSDF of a triangle mesh (9 floats per triangle) into g's node values; stuck
 // counts rays that gave up (mesh.cu)
-void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo[3], const float hi[3],
-                     const float gamma[4], float *out, unsigned *stuck, cudaStream_t s);
+// mesh.cu: tiles of consecutive triangles with their bounding boxes (6 floats per tile)
+int mesh_tiles(int ntri);
+void mesh_tile_bounds(const float *tri, int ntri, float *tiles);
+void mesh_morton_order(const float *tri, int ntri, const float lo[3], const float hi[3], float *sorted);
+// tri/tiles: the caller's order (ray passes); dtri/dtiles: the Morton order (distance pass)
+void launch_mesh_sdf(const float *tri, int ntri, const float *tiles, const float *dtri, const float *dtiles,
+                     float margin, const SdfDev &g, const float lo[3], const float hi[3], const float gamma[4],
+                     float *out, unsigned *stuck, cudaStream_t s);
 
 // LNM boundary levels (1, 2, 0) of n sorted slots into out (caller order through pid);
 // level: one int per cell (boundary.cu)

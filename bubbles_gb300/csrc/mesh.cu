@@ -15,6 +15,10 @@
 #include "bbg_internal.cuh"
 #include "bbg_kernels.h"
 
+#include <algorithm>
+#include <utility>
+#include <vector>
+
 namespace bbg {
 
 static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -189,8 +193,51 @@ __device__ v3 offset_origin(const Hit &h, v3 w) {
 
 constexpr int kMaxRayHits = 256;   // a ray stuck on degenerate geometry gives up (outside)
 
-__global__ void k_mesh_sdf(const float *__restrict__ tri, int ntri, SdfDev g, v3 lo, v3 hi, Gammas G,
-                           float *__restrict__ out, unsigned *__restrict__ stuck) {
+// Triangles are visited in tiles of kMeshTile consecutive triangles, each split into
+// kMeshTile / kMeshSub sub-tiles, every tile and sub-tile with its bounding box: one is
+// skipped when its box cannot hold a better answer, which leaves every result equal to the
+// scan over all triangles.
+//  - distance: skipped when the box lies farther than the best distance so far by more than
+//    1 % plus an absolute margin (1e-3 of the mesh's bounding diagonal), so a skipped
+//    triangle's computed distance cannot be below the best despite rounding;
+//  - rays: skipped when the conservative ray-box test (Bounds3::IntersectP with the gamma
+//    growth, the test of the reference's BVH) rejects the box for the current tMax, which
+//    never rejects a box holding a hit at or before tMax.
+constexpr int kMeshTile = 64;
+constexpr int kMeshSub = 8;
+
+// The box tests of the two passes.
+__device__ __forceinline__ bool box_near(const float *__restrict__ bx, v3 p, float d, float margin) {
+    const float ex = fmaxf(fmaxf(__ldg(&bx[0]) - p.x, p.x - __ldg(&bx[3])), 0.f);
+    const float ey = fmaxf(fmaxf(__ldg(&bx[1]) - p.y, p.y - __ldg(&bx[4])), 0.f);
+    const float ez = fmaxf(fmaxf(__ldg(&bx[2]) - p.z, p.z - __ldg(&bx[5])), 0.f);
+    return !(sqrtf(ex * ex + ey * ey + ez * ez) > d * 1.01f + margin);
+}
+
+__device__ __forceinline__ bool box_on_ray(const float *__restrict__ bx, v3 o, v3 dir, float tmax, float g3) {
+    return hits_bounds(V(__ldg(&bx[0]), __ldg(&bx[1]), __ldg(&bx[2])), V(__ldg(&bx[3]), __ldg(&bx[4]), __ldg(&bx[5])), o,
+                       dir, tmax, g3);
+}
+
+// f(t) for every triangle t of the tiles and sub-tiles that keep(box) accepts, in order
+template <class Keep, class F>
+__device__ __forceinline__ void mesh_walk(const float *__restrict__ tiles, int ntri, Keep &&keep, F &&f) {
+    const int ntiles = (ntri + kMeshTile - 1) / kMeshTile, nsub = (ntri + kMeshSub - 1) / kMeshSub;
+    const float *sub = tiles + 6 * ntiles;
+    for (int b = 0; b < ntiles; b++) {
+        if (!keep(tiles + 6 * b)) continue;
+        const int s1 = min(nsub, (b + 1) * (kMeshTile / kMeshSub));
+        for (int q = b * (kMeshTile / kMeshSub); q < s1; q++) {
+            if (!keep(sub + 6 * q)) continue;
+            const int t1 = min(ntri, (q + 1) * kMeshSub);
+            for (int t = q * kMeshSub; t < t1; t++) f(t);
+        }
+    }
+}
+
+__global__ void k_mesh_sdf(const float *__restrict__ tri, int ntri, const float *__restrict__ tiles,
+                           const float *__restrict__ dtri, const float *__restrict__ dtiles, float margin,
+                           SdfDev g, v3 lo, v3 hi, Gammas G, float *__restrict__ out, unsigned *__restrict__ stuck) {
     const unsigned total = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz;
     const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= total) return;
@@ -199,12 +246,13 @@ __global__ void k_mesh_sdf(const float *__restrict__ tri, int ntri, SdfDev g, v3
     const unsigned j = rem / (unsigned)g.nx, i = rem % (unsigned)g.nx;
     const v3 p = V(fa(g.org[0], fm(g.sp[0], (float)i)), fa(g.org[1], fm(g.sp[1], (float)j)),
                    fa(g.org[2], fm(g.sp[2], (float)k)));
-    // MeshClosestDistance: the least DistanceTriangle (strictly smaller replaces)
+    // MeshClosestDistance: the least DistanceTriangle (strictly smaller replaces; the least
+    // value does not depend on the order, so this pass walks the Morton-ordered copy)
     float d = 3.1622776601683794e+18f;   // SqrtInfinity
-    for (int t = 0; t < ntri; t++) {
-        const float dt = distance_triangle(p, tri_vertex(tri, t, 0), tri_vertex(tri, t, 1), tri_vertex(tri, t, 2));
+    mesh_walk(dtiles, ntri, [&](const float *bx) { return box_near(bx, p, d, margin); }, [&](int t) {
+        const float dt = distance_triangle(p, tri_vertex(dtri, t, 0), tri_vertex(dtri, t, 1), tri_vertex(dtri, t, 2));
         if (dt < d) d = dt;
-    }
+    });
     // MeshIsPointInside: ray towards the bounds' centre, closest hits counted
     const v3 center = vmul(vadd(lo, hi), 0.5f);
     const v3 to = vsub(center, p);
@@ -217,9 +265,10 @@ __global__ void k_mesh_sdf(const float *__restrict__ tri, int ntri, SdfDev g, v3
         Hit h;
         bool any = false;
         if (hits_bounds(lo, hi, o, dir, tmax, G.g3)) {
-            for (int t = 0; t < ntri; t++)
+            mesh_walk(tiles, ntri, [&](const float *bx) { return box_on_ray(bx, o, dir, tmax, G.g3); }, [&](int t) {
                 any |= intersect_triangle(o, dir, tmax, tri_vertex(tri, t, 0), tri_vertex(tri, t, 1),
                                           tri_vertex(tri, t, 2), G, h);
+            });
         }
         if (!any) {
             done = true;
@@ -239,8 +288,57 @@ __global__ void k_mesh_sdf(const float *__restrict__ tri, int ntri, SdfDev g, v3
 
 }  // namespace
 
-void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo[3], const float hi[3],
-                     const float gamma[4], float *out, unsigned *stuck, cudaStream_t s) {
+// boxes of the tiles, then of the sub-tiles (6 floats each)
+int mesh_tiles(int ntri) { return (ntri + kMeshTile - 1) / kMeshTile + (ntri + kMeshSub - 1) / kMeshSub; }
+
+static void tile_boxes(const float *tri, int ntri, int size, float *tiles) {
+    for (int b = 0; b < (ntri + size - 1) / size; b++) {
+        float *bx = tiles + 6 * b;
+        for (int k = 0; k < 3; k++) {
+            bx[k] = 3.402823466e+38f;
+            bx[3 + k] = -3.402823466e+38f;
+        }
+        for (int t = b * size; t < ntri && t < (b + 1) * size; t++)
+            for (int c = 0; c < 3; c++)
+                for (int k = 0; k < 3; k++) {
+                    const float x = tri[9 * (size_t)t + 3 * c + k];
+                    bx[k] = x < bx[k] ? x : bx[k];
+                    bx[3 + k] = x > bx[3 + k] ? x : bx[3 + k];
+                }
+    }
+}
+
+void mesh_tile_bounds(const float *tri, int ntri, float *tiles) {
+    tile_boxes(tri, ntri, kMeshTile, tiles);
+    tile_boxes(tri, ntri, kMeshSub, tiles + 6 * ((ntri + kMeshTile - 1) / kMeshTile));
+}
+
+// The triangles in the Morton order of their centroids (30-bit codes in the mesh bounds,
+// ties by index), for the distance pass's tiles.
+void mesh_morton_order(const float *tri, int ntri, const float lo[3], const float hi[3], float *sorted) {
+    std::vector<std::pair<unsigned, int>> key((size_t)ntri);
+    for (int t = 0; t < ntri; t++) {
+        unsigned code = 0;
+        unsigned q[3];
+        for (int k = 0; k < 3; k++) {
+            const float c = (tri[9 * (size_t)t + k] + tri[9 * (size_t)t + 3 + k] + tri[9 * (size_t)t + 6 + k]) / 3.f;
+            const float ext = hi[k] - lo[k];
+            float u = ext > 0.f ? (c - lo[k]) / ext : 0.f;
+            u = u < 0.f ? 0.f : (u > 1.f ? 1.f : u);
+            q[k] = (unsigned)(u * 1023.f);
+        }
+        for (int bit = 9; bit >= 0; bit--)
+            for (int k = 0; k < 3; k++) code = (code << 1) | ((q[k] >> bit) & 1u);
+        key[(size_t)t] = std::make_pair(code, t);
+    }
+    std::sort(key.begin(), key.end());
+    for (int r = 0; r < ntri; r++)
+        for (int q = 0; q < 9; q++) sorted[9 * (size_t)r + q] = tri[9 * (size_t)key[(size_t)r].second + q];
+}
+
+void launch_mesh_sdf(const float *tri, int ntri, const float *tiles, const float *dtri, const float *dtiles,
+                     float margin, const SdfDev &g, const float lo[3], const float hi[3], const float gamma[4],
+                     float *out, unsigned *stuck, cudaStream_t s) {
     const long long total = (long long)g.nx * g.ny * g.nz;
     Gammas G;
     G.g2 = gamma[0];
@@ -250,7 +348,7 @@ void launch_mesh_sdf(const float *tri, int ntri, const SdfDev &g, const float lo
     v3 l, h;
     l.x = lo[0]; l.y = lo[1]; l.z = lo[2];
     h.x = hi[0]; h.y = hi[1]; h.z = hi[2];
-    k_mesh_sdf<<<blocks_for(total, 128), 128, 0, s>>>(tri, ntri, g, l, h, G, out, stuck);
+    k_mesh_sdf<<<blocks_for(total, 128), 128, 0, s>>>(tri, ntri, tiles, dtri, dtiles, margin, g, l, h, G, out, stuck);
 }
 
 }  // namespace bbg

@@ -293,7 +293,16 @@ def torus(big=0.18, small=0.06, nu=24, nv=12, center=(-0.01, 0.02, 0.015), rot=(
     return verts.astype(np.float32).astype(np.float64), np.array(tris, np.int32)
 
 
-MESH_CASES = {"icosphere": (icosphere, 0.02, 0.1), "torus": (torus, 0.015, 0.15)}
+def soup(count=300, seed=5):
+    """Triangles of random size, position and orientation in index order with no spatial
+    coherence (overlapping, not closed): the worst case for skipping tiles of triangles."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-0.2, 0.2, (count, 1, 3))
+    v = (c + rng.normal(0.0, 0.05, (count, 3, 3))).astype(np.float32).reshape(-1, 3)
+    return v, np.arange(3 * count, dtype=np.int32).reshape(-1, 3)
+
+
+MESH_CASES = {"icosphere": (icosphere, 0.02, 0.1), "torus": (torus, 0.015, 0.15), "soup": (soup, 0.02, 0.1)}
 
 
 def make_mesh():

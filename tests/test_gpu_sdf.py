@@ -123,7 +123,7 @@ def test_generate_sdf_of_analytic_shapes(gpu, small, which):
 MESH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mesh_f32.npz")
 
 
-@pytest.mark.parametrize("name", ["icosphere", "torus"])
+@pytest.mark.parametrize("name", ["icosphere", "torus", "soup"])
 def test_mesh_field_matches_reference(gpu, small, name):
     """GenerateShapeSDF of a triangle mesh: the grid and every node's distance equal the
     reference's; the inside sign too, except where two triangles tie for a ray's closest
