@@ -664,17 +664,22 @@ def run_ours(args, scene, pos):
         learned = variant == "learned"
 
         def e2e_step():
-            g.upload(pos_h, vel_h)
-            if warm:
-                g.set(bb.FIELD_PRESSURE, pr_h)
-            if learned:
-                g.set(bb.FIELD_DIVERGENCE, dv_h)
-            g.advance_time_step(dt)
-            g.download(pos_h, vel_h)
-            if warm:
-                g.get(bb.FIELD_PRESSURE, out=pr_h)
-            if learned:
-                g.get(bb.FIELD_DIVERGENCE, out=dv_h)
+            if scene.get("batch"):
+                g.upload(pos_h, vel_h)
+                if warm:
+                    g.set(bb.FIELD_PRESSURE, pr_h)
+                if learned:
+                    g.set(bb.FIELD_DIVERGENCE, dv_h)
+                g.advance_time_step(dt)
+                g.download(pos_h, vel_h)
+                if warm:
+                    g.get(bb.FIELD_PRESSURE, out=pr_h)
+                if learned:
+                    g.get(bb.FIELD_DIVERGENCE, out=dv_h)
+                return
+            # the host-resident step of the C ABI: uploads, substep, downloads, one sync
+            g.step_host(dt, pos_h, vel_h, pr_h if warm else None, dv_h if learned else None,
+                        pos_h, vel_h, pr_h if warm else None, dv_h if learned else None)
 
         def e2e_reset():
             pos_h[:] = snap_p

@@ -201,6 +201,7 @@ SIGNATURES = {
     "bbg_lnm_boundary_geometric": [_P, ctypes.c_double, _I, _I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "bbg_boundary_test": [_P, _I, ctypes.c_double, ctypes.c_void_p],
     "bbg_energy": [_P, ctypes.c_void_p],
+    "bbg_step_host": [_P, ctypes.c_double, _I] + [ctypes.c_void_p] * 8 + [ctypes.c_void_p],
     "bbg_particle_sdf": [_P, _I, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                          ctypes.c_void_p, ctypes.c_size_t],
     "bbg_collider_set_sdf": [_P, _I, ctypes.POINTER(SdfGrid), ctypes.c_void_p],

@@ -78,6 +78,7 @@ struct bbg_solver_s {
     int dims[3];
     StepState *h_st = nullptr;   // pinned host mirror of the device step state
     unsigned *h_u = nullptr;     // pinned scratch
+    float *d_stage2 = nullptr;   // 2 x capacity floats: the carried scalars of bbg_step_host
     int last_max_it = 1;
     float last_tol = 0.01f;
     int pcisph_last_substep = 0;
@@ -237,6 +238,8 @@ bbg_status free_all(bbg_solver s) {
     drop_graphs(s);
     free_mlp(s);
     free_frame(s);
+    if (s->d_stage2) cudaFree(s->d_stage2);
+    s->d_stage2 = nullptr;
     void *batch[] = {s->d_zb, s->d_box, s->d_sst, s->d_scene};
     for (void *p : batch)
         if (p) cudaFree(p);
@@ -1260,6 +1263,66 @@ bbg_status bbg_advance_time_step(bbg_solver s, double dt, bbg_step_stats *stats)
         if ((r = read_step_state(s))) return r;
         add_substep_stats(s, (float)dt);
         *stats = s->acc;
+    }
+    return BBG_OK;
+}
+
+// One substep with the state in host memory: the uploads, AdvanceTimeStep and the downloads
+// of bbg_upload_particles, bbg_set_field, bbg_advance_time_step, bbg_download and
+// bbg_get_field, queued on the solver's stream with one synchronisation at the end.
+bbg_status bbg_step_host(bbg_solver s, double dt, int n, const float *pos, const float *vel, const float *pressure,
+                         const float *divergence, float *pos_out, float *vel_out, float *pressure_out,
+                         float *divergence_out, bbg_step_stats *stats) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!pos || !vel || n <= 0) return fail(BBG_ERR_INVALID_ARGUMENT, "need n > 0 positions and velocities");
+    if (n > s->capacity) return fail(BBG_ERR_CAPACITY, "%d particles exceed capacity %d", n, s->capacity);
+    if (!s->setup_done) return fail(BBG_ERR_STATE, "bbg_setup has not been called");
+    if (!(dt > 0)) return fail(BBG_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if ((divergence || divergence_out) && !s->mlp_alloc)
+        return fail(BBG_ERR_STATE, "the divergence field belongs to the learned warm start");
+    if ((pressure || divergence || pressure_out || divergence_out) && !s->d_stage2)
+        CK(cudaMalloc((void **)&s->d_stage2, sizeof(float) * 2 * (size_t)s->capacity));
+    const size_t nn = (size_t)n;
+    float *dp = s->B.stage, *dv = s->B.stage + 3 * (size_t)s->capacity;
+    float *sp = s->d_stage2, *sd = s->d_stage2 ? s->d_stage2 + s->capacity : nullptr;
+    CK(cudaMemcpyAsync(dp, pos, sizeof(float) * 3 * nn, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dv, vel, sizeof(float) * 3 * nn, cudaMemcpyHostToDevice, s->stream));
+    if (bbg_status r = upload_common(s, dp, dv, n)) return r;
+    if (pressure) {
+        CK(cudaMemcpyAsync(sp, pressure, sizeof(float) * nn, cudaMemcpyHostToDevice, s->stream));
+        launch_set_scalar(s->B.press, s->B.slot, sp, n, s->stream);
+        CK_LAUNCH();
+        s->valid |= bit(BBG_FIELD_PRESSURE);
+    }
+    if (divergence) {
+        CK(cudaMemcpyAsync(sd, divergence, sizeof(float) * nn, cudaMemcpyHostToDevice, s->stream));
+        launch_set_scalar(s->mlp.divsum, s->B.slot, sd, n, s->stream);
+        CK_LAUNCH();
+    }
+    if (bbg_status r = substep(s, (float)dt)) return r;
+    if (pos_out || vel_out) {
+        launch_download(s->B, s->state, s->pid_cur, pos_out ? dp : nullptr, vel_out ? dv : nullptr, n, s->stream);
+        CK_LAUNCH();
+        if (pos_out) CK(cudaMemcpyAsync(pos_out, dp, sizeof(float) * 3 * nn, cudaMemcpyDeviceToHost, s->stream));
+        if (vel_out) CK(cudaMemcpyAsync(vel_out, dv, sizeof(float) * 3 * nn, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (pressure_out) {
+        launch_get_scalar(s->B.press, s->B.slot, sp, n, s->stream);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(pressure_out, sp, sizeof(float) * nn, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (divergence_out) {
+        launch_get_scalar(s->mlp.divsum, s->B.slot, sd, n, s->stream);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(divergence_out, sd, sizeof(float) * nn, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (stats) {
+        memset(&s->acc, 0, sizeof(s->acc));
+        if (bbg_status r = read_step_state(s)) return r;   // synchronises the stream
+        add_substep_stats(s, (float)dt);
+        *stats = s->acc;
+    } else {
+        CK(cudaStreamSynchronize(s->stream));
     }
     return BBG_OK;
 }

@@ -249,6 +249,21 @@ class Solver:
                out["distance"].ctypes.data, out["inside"].ctypes.data)
         return out
 
+    def step_host(self, dt, pos, vel, pressure=None, divergence=None, pos_out=None, vel_out=None,
+                  pressure_out=None, divergence_out=None):
+        """One substep with the state in host arrays (float32, caller order): upload, advance,
+        download into the given outputs, one synchronisation (bbg_step_host)."""
+        def ptr(a, shape):
+            if a is None:
+                return None
+            assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] and a.size == int(np.prod(shape))
+            return a.ctypes.data
+        n = int(np.asarray(pos).shape[0])
+        N.call("bbg_step_host", self.h, float(dt), n, ptr(pos, (n, 3)), ptr(vel, (n, 3)), ptr(pressure, (n,)),
+               ptr(divergence, (n,)), ptr(pos_out, (n, 3)), ptr(vel_out, (n, 3)), ptr(pressure_out, (n,)),
+               ptr(divergence_out, (n,)), None)
+        self.n = n
+
     def energy(self):
         """FP64 totals of the state: mass, kinetic, potential, momentum (3)."""
         out = np.zeros(6)

@@ -210,6 +210,17 @@ bbg_status bbg_set_stream(bbg_solver s, void *cuda_stream);
 bbg_status bbg_synchronize(bbg_solver s);
 
 /* ----- stepping ----------------------------------------------------------- */
+/* One substep with the state in host memory, as a host that keeps its particles on the CPU
+ * calls it every step: positions and velocities (n each, xyz) uploaded, optionally the warm
+ * start's carried pressure and divergence (BBG_FIELD_PRESSURE / BBG_FIELD_DIVERGENCE,
+ * caller order), AdvanceTimeStep(dt), then the same fields downloaded into the *_out arrays
+ * that are not NULL.  Equivalent to bbg_upload_particles, bbg_set_field,
+ * bbg_advance_time_step, bbg_download and bbg_get_field in sequence, queued on the solver's
+ * stream with a single synchronisation at the end (stats as bbg_advance_time_step's). */
+bbg_status bbg_step_host(bbg_solver s, double dt, int n, const float *pos, const float *vel, const float *pressure,
+                         const float *divergence, float *pos_out, float *vel_out, float *pressure_out,
+                         float *divergence_out, bbg_step_stats *stats);
+
 /* Advance(dt) with the CFL substep loop (pcisph_solver3.cpp:67-89,
  * sph_solver3.cpp:69-93). */
 bbg_status bbg_advance(bbg_solver s, double dt, bbg_step_stats *stats);
