@@ -210,8 +210,8 @@ k_soa(int n, const float4 *__restrict__ pos, float *__restrict__ sx, float *__re
 
 // k_density with candidates taken two at a time: the even-aligned pairs of each 32-candidate
 // chunk load x, y, z as float2 from the structure-of-arrays copy and compute both squared
-// distances and kernel terms with f32x2 instructions; the membership test, the sums (one per
-// lane of the pair) and the member list are those of k_density.
+// distances and kernel terms with f32x2 instructions; the membership test, the running sum
+// in candidate order and the member list are those of k_density.
 __global__ void __launch_bounds__(kMaxTile, kDensityMinBlocks)
 k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
              const unsigned *__restrict__ start, const float *__restrict__ sx, const float *__restrict__ sy,
@@ -223,7 +223,7 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
     const float4 pi = pos[i];
     const unsigned cw = cell[i];
     const size_t n = (size_t)P.n;
-    float s0 = 0.f, s1 = 0.f;
+    float s0 = 0.f;
     int cnt = 0;      // bucket members, i included
     int listed = 0;   // members other than i
     const bool crowded = candidate_count(P.g, start, cw & ~kWide) > kMaxCandidates;
@@ -256,7 +256,7 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
                     const f2 dx = f2_sub(f2_pack(ax.x, ax.y), X);
                     const f2 dy = f2_sub(f2_pack(ay.x, ay.y), Y);
                     const f2 dz = f2_sub(f2_pack(az.x, az.y), Z);
-                    const f2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                    const f2 r2 = f2_fma(dz, dz, f2_fma(dx, dx, f2_mul(dy, dy)));
                     const f2 x = f2_fma(r2, NIH, ONE);
                     const f2 x3 = f2_mul(f2_mul(x, x), x);
                     float r0, r1, c0, c1;
@@ -267,8 +267,8 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
                         if (!m0 && r0 <= hi) m0 = std_member_exact(P, pi, make_float4(ax.x, ay.x, az.x, 0.f));
                         if (!m1 && r1 <= hi) m1 = std_member_exact(P, pi, make_float4(ax.y, ay.y, az.y, 0.f));
                     }
-                    s0 += m0 ? c0 : 0.f;
-                    s1 += m1 ? c1 : 0.f;
+                    s0 += m0 ? c0 : 0.f;   // one running sum in candidate order
+                    s0 += m1 ? c1 : 0.f;
                     m |= ((unsigned)m0 | ((unsigned)m1 << 1)) << (j - cb);
                 }
                 if (j < ce) single(j);
@@ -283,7 +283,7 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
             }
         });
     }
-    const float di = (s0 + s1) * P.std_c * P.mass;
+    const float di = s0 * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);
         if (p < 0.f) p *= P.neg_scale;
