@@ -197,15 +197,18 @@ k_density(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned
     if (cnt > kBucketCap) atomicAdd(&st->nbr_overflow, 1u);
 }
 
-// Structure-of-arrays copy of the positions for the packed density pass.
+// Positions regrouped for the packed density pass: slots 2k and 2k + 1 share a record of six
+// floats (x of both, y of both, z of both), so a pair's coordinates are three float2 loads
+// from one address.
 __global__ void __launch_bounds__(kThreads)
-k_soa(int n, const float4 *__restrict__ pos, float *__restrict__ sx, float *__restrict__ sy, float *__restrict__ sz) {
+k_soa(int n, const float4 *__restrict__ pos, float *__restrict__ rec) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pos[i];
-    sx[i] = p.x;
-    sy[i] = p.y;
-    sz[i] = p.z;
+    float *r = rec + 6 * (size_t)(i >> 1) + (i & 1);
+    r[0] = p.x;
+    r[2] = p.y;
+    r[4] = p.z;
 }
 
 // k_density with candidates taken two at a time: the even-aligned pairs of each 32-candidate
@@ -214,8 +217,8 @@ k_soa(int n, const float4 *__restrict__ pos, float *__restrict__ sx, float *__re
 // in candidate order and the member list are those of k_density.
 __global__ void __launch_bounds__(kMaxTile, kDensityMinBlocks)
 k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsigned *__restrict__ cell,
-             const unsigned *__restrict__ start, const float *__restrict__ sx, const float *__restrict__ sy,
-             const float *__restrict__ sz, float *__restrict__ rho, float *__restrict__ inv_rho,
+             const unsigned *__restrict__ start, const float *__restrict__ rec, float *__restrict__ rho,
+             float *__restrict__ inv_rho,
              float *__restrict__ press, int *__restrict__ nbr, ListEntry *__restrict__ list, int compute_pressure,
              StepState *st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -226,22 +229,29 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
     float s0 = 0.f;
     int cnt = 0;      // bucket members, i included
     int listed = 0;   // members other than i
-    const bool crowded = candidate_count(P.g, start, cw & ~kWide) > kMaxCandidates;
-    if (crowded) {
-        s0 = 1.f;
-        cnt = 1;
-        atomicAdd(&st->crowded, 1u);
-    } else {
+    // past kMaxCandidates in its 27 cells a particle is crowded: its rows stop being walked
+    // as soon as the running candidate count passes the cap (the work stays bounded), and
+    // it keeps only itself, as in k_density
+    bool crowded = false;
+    unsigned seen = 0;
+    {
         const f2 X = f2_pack(pi.x, pi.x), Y = f2_pack(pi.y, pi.y), Z = f2_pack(pi.z, pi.z);
         const f2 NIH = f2_pack(-P.inv_h2, -P.inv_h2), ONE = f2_pack(1.f, 1.f);
         const float lo = P.nb_lo, hi = P.nb_hi, ih2 = P.inv_h2;
         tile_rows(P.g, start, cw & ~kWide, [&](int, unsigned b, unsigned e) {
+            if (crowded) return;
+            seen += e - b;
+            if (seen > kMaxCandidates) {
+                crowded = true;
+                return;
+            }
             for (unsigned cb = b; cb < e; cb += 32u) {
                 const unsigned ce = min(e, cb + 32u);
                 unsigned m = 0u;
                 unsigned j = cb;
                 auto single = [&](unsigned q) {
-                    const float4 pj = make_float4(__ldg(&sx[q]), __ldg(&sy[q]), __ldg(&sz[q]), 0.f);
+                    const float *r = rec + 6 * (size_t)(q >> 1) + (q & 1u);
+                    const float4 pj = make_float4(__ldg(&r[0]), __ldg(&r[2]), __ldg(&r[4]), 0.f);
                     const float r2 = dist2(pi, pj);
                     const bool mem = r2 < lo || (r2 <= hi && std_member_exact(P, pi, pj));
                     const float x = 1.f - r2 * ih2;
@@ -250,9 +260,8 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
                 };
                 if (j & 1u) single(j++);
                 for (; j + 1u < ce; j += 2u) {
-                    const float2 ax = __ldg(reinterpret_cast<const float2 *>(sx + j));
-                    const float2 ay = __ldg(reinterpret_cast<const float2 *>(sy + j));
-                    const float2 az = __ldg(reinterpret_cast<const float2 *>(sz + j));
+                    const float2 *r = reinterpret_cast<const float2 *>(rec + 3 * (size_t)j);   // j even
+                    const float2 ax = __ldg(&r[0]), ay = __ldg(&r[1]), az = __ldg(&r[2]);
                     const f2 dx = f2_sub(f2_pack(ax.x, ax.y), X);
                     const f2 dy = f2_sub(f2_pack(ay.x, ay.y), Y);
                     const f2 dz = f2_sub(f2_pack(az.x, az.y), Z);
@@ -282,6 +291,12 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
                 }
             }
         });
+    }
+    if (crowded) {
+        s0 = 1.f;
+        cnt = 1;
+        listed = 0;
+        atomicAdd(&st->crowded, 1u);
     }
     const float di = s0 * P.std_c * P.mass;
     if (compute_pressure) {
@@ -734,11 +749,9 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
     const int t = B.tune.block;
     if (kDensityX2 && !kListRelative) {
-        float *sx = B.soa, *sy = B.soa + B.soa_stride, *sz = B.soa + 2 * B.soa_stride;
-        k_soa<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], sx, sy, sz);
-        k_density_x2<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, sx, sy, sz,
-                                                      B.rho, B.inv_rho, B.press, B.nbr, B.list, compute_pressure,
-                                                      B.st);
+        k_soa<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.soa);
+        k_density_x2<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.soa, B.rho,
+                                                      B.inv_rho, B.press, B.nbr, B.list, compute_pressure, B.st);
     } else {
         k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
                                                    B.press, B.nbr, B.list, compute_pressure, B.st);
