@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <random>
@@ -176,9 +177,32 @@ void fill_params(bbg_solver s) {
     P.max_err_ratio = (float)d.max_density_error_ratio;
 }
 
+// Host-side fault injection for tests, off unless the environment sets BBG_FAIL_ALLOC_AFTER:
+// the device allocation after that many successful ones (counted per process) fails as
+// cudaMalloc does when memory runs out.
+static long alloc_fault_budget() {
+    static const long budget = [] {
+        const char *e = getenv("BBG_FAIL_ALLOC_AFTER");
+        return e ? atol(e) : -1L;
+    }();
+    return budget;
+}
+static long alloc_count = 0;
+
 template <class T>
 bbg_status dalloc(T **p, size_t count) {
-    CK(cudaMalloc((void **)p, sizeof(T) * (count ? count : 1)));
+    const long budget = alloc_fault_budget();
+    if (budget >= 0 && __atomic_fetch_add(&alloc_count, 1, __ATOMIC_SEQ_CST) >= budget) {
+        *p = nullptr;
+        return fail(BBG_ERR_OUT_OF_MEMORY, "device allocation failed (injected by BBG_FAIL_ALLOC_AFTER)");
+    }
+    const cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // a failed allocation must not surface in a later call's launch check
+        *p = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? BBG_ERR_OUT_OF_MEMORY : BBG_ERR_CUDA,
+                    "device allocation of %zu bytes: %s", sizeof(T) * count, cudaGetErrorString(e));
+    }
     return BBG_OK;
 }
 
@@ -918,10 +942,14 @@ bbg_status bbg_create(const bbg_solver_desc *desc, int capacity, bbg_solver *out
     ALLOC(B.partials, scan_partials_needed(s->cells));
     ALLOC(B.st, 1); ALLOC(B.stage, 6 * n); ALLOC(B.red, 4);
 #undef ALLOC
-    if (!r && cudaMallocHost((void **)&s->h_st, sizeof(StepState)) != cudaSuccess)
+    if (!r && cudaMallocHost((void **)&s->h_st, sizeof(StepState)) != cudaSuccess) {
+        cudaGetLastError();
         r = fail(BBG_ERR_OUT_OF_MEMORY, "pinned allocation failed");
-    if (!r && cudaMallocHost((void **)&s->h_u, 64) != cudaSuccess)
+    }
+    if (!r && cudaMallocHost((void **)&s->h_u, 64) != cudaSuccess) {
+        cudaGetLastError();
         r = fail(BBG_ERR_OUT_OF_MEMORY, "pinned allocation failed");
+    }
     if (!r && cudaMemsetAsync(B.count, 0, sizeof(unsigned) * s->cells, s->stream) != cudaSuccess)
         r = fail(BBG_ERR_CUDA, "memset failed");
     if (!r && cudaMemsetAsync(B.st, 0, sizeof(StepState), s->stream) != cudaSuccess)

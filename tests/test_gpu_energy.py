@@ -49,3 +49,32 @@ def test_nonfinite_state_is_counted(gpu, small):
         assert st["nonfinite"] >= 1
         p, _ = s.download()
         assert np.isnan(p).any(axis=1).sum() == st["nonfinite"]
+
+
+def test_allocation_failures_are_reported(gpu, small):
+    """Allocation failure without a GPU fault: an injected failure at each point of the
+    solver's allocations (BBG_FAIL_ALLOC_AFTER, in a child process) and a request far past
+    the device's memory both come back as BBG_ERR_OUT_OF_MEMORY, and the process goes on."""
+    import os
+    import subprocess
+    import sys
+    sc, pos = small
+    code = ("import numpy as np, bubbles_gb300 as bb\n"
+            "from bubbles_gb300 import scenes\n"
+            "sc, pos = scenes.small_pcisph()\n"
+            "try:\n"
+            "    bb.Solver(sc, pos=pos).close()\n"
+            "    print('created')\n"
+            "except bb.BbgError as e:\n"
+            "    print('status', e.status)\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for k in (0, 4, 17):
+        env = dict(os.environ, BBG_FAIL_ALLOC_AFTER=str(k), PYTHONPATH=root)
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        assert out.returncode == 0, out.stderr[-2000:]
+        assert "status 3" in out.stdout, out.stdout
+    with pytest.raises(bb.BbgError) as e:
+        bb.Solver(sc, pos=pos, capacity=1 << 30)   # ~300 GB of particle state
+    assert e.value.status == 3
+    with bb.Solver(sc, pos=pos) as s:              # the device is still usable
+        assert s.advance_time_step(sc["dt"], stats=True)["nonfinite"] == 0
