@@ -173,11 +173,11 @@ def barrier(dist):
 
 
 def cpu_oracle_rate(scene, pos, vel, budget_s, threads, max_steps=50):
-    """Time the CPU oracle on substeps of (scene, pos, vel) until `budget_s`."""
+    """Time the CPU oracle on substeps of (scene, pos, vel) until `budget_s` (at least one)."""
     from oracle import oracle as O
     sim = O.OracleSim(scene, pos, vel, variant="f32", threads=threads)
     steps, iters, t = 0, 0, 0.0
-    while t < budget_s and steps < max_steps:
+    while steps < max_steps and (steps == 0 or t < budget_s):
         t0 = time.perf_counter()
         it, _ = sim.pcisph_substep(scene["dt"], scene["max_density_error_ratio"],
                                    scene["max_iterations"], O.PCISPH_TOLERANCE)
