@@ -835,6 +835,8 @@ def main():
                     help="substeps of FP64 mass/energy logging after the timed region (every 10); "
                          "default 100 for pcisph_4m, else none")
     ap.add_argument("--energy-log", default=None, help="JSONL file for the mass/energy records")
+    ap.add_argument("--warm-scale", type=float, default=None,
+                    help="start pressure = scale x estimate for warm starts (default: the library's, 0.9 learned)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
     ap.add_argument("--no-frames", action="store_true",
                     help="skip the particle-frame and seeding timings (frame writer / reader, emitters)")
@@ -852,6 +854,8 @@ def main():
     scene["pressure_init"] = {"plain": "zero", "warm": "previous", "learned": "learned"}[args.variant]
     if args.variant == "learned":
         scene["mlp"] = {"train_substeps": args.prep}
+    if args.warm_scale is not None:
+        scene["warm_scale"] = args.warm_scale
     if args.impl == "reference":
         run_reference(args, scene, pos)
     else:
