@@ -835,6 +835,8 @@ def main():
                     help="substeps of FP64 mass/energy logging after the timed region (every 10); "
                          "default 100 for pcisph_4m, else none")
     ap.add_argument("--energy-log", default=None, help="JSONL file for the mass/energy records")
+    ap.add_argument("--mlp", action="append", default=[], metavar="KEY=VALUE",
+                    help="learned warm start settings (bbg_mlp_desc fields, e.g. expectile=0.4)")
     ap.add_argument("--warm-scale", type=float, default=None,
                     help="start pressure = scale x estimate for warm starts (default: the library's, 0.9 learned)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
@@ -854,6 +856,9 @@ def main():
     scene["pressure_init"] = {"plain": "zero", "warm": "previous", "learned": "learned"}[args.variant]
     if args.variant == "learned":
         scene["mlp"] = {"train_substeps": args.prep}
+        for kv in args.mlp:
+            k, v = kv.split("=", 1)
+            scene["mlp"][k] = float(v) if "." in v or "e" in v else int(v)
     if args.warm_scale is not None:
         scene["warm_scale"] = args.warm_scale
     if args.impl == "reference":
