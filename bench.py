@@ -289,29 +289,39 @@ def launches_per_substep(scene, variant, iters):
     return 8 + extra + 3 * iters + pv
 
 
-def timed_substeps(g, dt, steps, stream, flush, events=True):
-    """K substeps (graph replay), L2 flushed before each outside the events."""
+def sample_substeps(first, total, k):
+    """k substep indices spread evenly over [first, total): the timed sample of the run."""
+    span = total - first
+    return [first + (i * span) // k for i in range(k)]
+
+
+def timed_event(stream, flush, fn):
+    """Device time (ms) of fn() on `stream`, L2 flushed before and outside the events."""
     import torch
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    iters, errs = [], []
-    flags = {"out_of_grid": 0, "crowded": 0, "not_converged": 0}
-    torch.cuda.synchronize()
-    for k in range(steps):
-        flush.zero_()
-        starts[k].record(stream)
-        g.advance_time_step(dt)
-        ends[k].record(stream)
-        st = g.stats()
-        iters.append(st["iterations"])
-        errs.append(st["max_density_error_ratio"])
-        flags["out_of_grid"] = max(flags["out_of_grid"], st["out_of_grid"])
-        flags["crowded"] = max(flags["crowded"], st["crowded"])
-        flags["not_converged"] += st["not_converged"]
-    torch.cuda.synchronize()
-    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    timed_substeps.flags = flags
-    return ms, iters, errs
+    flush.zero_()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b)
+
+
+class StepLog:
+    """Per-substep corrector statistics of one arm of the timed sample."""
+
+    def __init__(self):
+        self.ms, self.iters, self.errs = [], [], []
+        self.not_converged = self.out_of_grid = self.crowded = 0
+
+    def add(self, ms, st):
+        self.ms.append(ms)
+        self.iters.append(st["iterations"])
+        self.errs.append(st["max_density_error_ratio"])
+        self.not_converged += st["not_converged"]
+        self.out_of_grid = max(self.out_of_grid, st["out_of_grid"])
+        self.crowded = max(self.crowded, st["crowded"])
 
 
 def frame_io(bb, g, scene, n, device, reps=5):
@@ -535,6 +545,48 @@ def postprocess(bb, scene, final_pos, device):
     return out
 
 
+def sph_config1(bb, device, stream, advances=200):
+    """Config 1, the plain SPH dam break of 16,384 particles (SphSolver3, fixed dt 1e-3,
+    200 Advance calls of 7 CFL substeps each), on the device with CUDA events around the
+    Advance calls, beside the CPU oracle (the reference's SPH step restated, Jacobi order,
+    all host threads) on the first 5 Advance calls from the same start."""
+    import torch
+    from bubbles_gb300 import scenes
+    from oracle import oracle as O
+    sc, pos = scenes.sph_16k(seed=0)
+    g = bb.Solver(sc, pos=pos, device=device)
+    g.set_stream(stream)
+    for _ in range(3):
+        g.advance(sc["dt"])
+    g.upload(pos)
+    g.setup()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    substeps = 0
+    a.record(stream)
+    for _ in range(advances):
+        substeps += g.advance(sc["dt"])["substeps"]
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    g.close()
+    threads = os.cpu_count() or 1
+    o = O.OracleSim(sc, pos, variant="f32", threads=threads)
+    t0 = time.perf_counter()
+    cpu_sub = sum(o.advance_sph(sc["dt"]) for _ in range(5))
+    cpu_s = time.perf_counter() - t0
+    o.close()
+    n = len(pos)
+    return {"workload": sc["workload"], "particles": n, "advances": advances, "substeps": substeps,
+            "ms_per_advance": ms / advances, "us_per_substep": 1e3 * ms / substeps,
+            "particle_updates_per_s": n * substeps / (ms / 1e3),
+            "cpu": {"kind": "port", "cores": threads, "advances": 5, "substeps": cpu_sub,
+                    "particle_updates_per_s": n * cpu_sub / cpu_s},
+            "measured": "CUDA events on the solver's stream around the Advance calls (each reads its CFL "
+                        "count back to the host)"}
+
+
 def energy_log(g, scene, substeps, path=None, every=10):
     """FP64 mass and energy of the state every `every` substeps of a run after the timed
     region (device reductions, bbg_energy), as JSONL records; optionally written to `path`."""
@@ -571,6 +623,10 @@ def run_ours(args, scene, pos):
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     warm = variant != "plain"
+    learned = variant == "learned"
+    compare = warm and not args.no_plain
+    total = max(int(scene.get("steps", 0)), args.prep + args.warmup + args.steps)
+    samples = sample_substeps(args.prep + args.warmup, total, args.steps)
     with torch.cuda.stream(stream):
         tuned = None
         if not args.no_tuning:
@@ -578,10 +634,59 @@ def run_ours(args, scene, pos):
             tuned = autotune.load(args.config)
             if tuned is not None and scene.get("batch"):
                 scene = dict(scene, grid_spacing_scale=tuned["grid_spacing_scale"])
-        g = make_solver(bb, scene, pos, local)
-        if tuned is not None:
-            g.set_tuning(**tuned["tuning"])
-        g.set_stream(stream)
+
+        def solver(sc):
+            s = make_solver(bb, sc, pos, local)
+            if tuned is not None:
+                s.set_tuning(**tuned["tuning"])
+            s.set_stream(stream)
+            return s
+        g = solver(scene)
+        gp = solver(dict(scene, pressure_init="zero")) if compare else None
+        # host copies of a sampled substep's input state (pinned): the e2e step reads them,
+        # and every other timed arm is restored from them
+        pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        pr_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+        dv_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+        pos_o = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        vel_o = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        pr_o = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+        dv_o = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
+
+        def snapshot():
+            g.download(pos_h, vel_h)
+            if warm:
+                g.get(bb.FIELD_PRESSURE, out=pr_h)
+            if learned:
+                g.get(bb.FIELD_DIVERGENCE, out=dv_h)
+
+        def restore(s, carried):
+            s.upload(pos_h, vel_h)
+            if carried:
+                s.set(bb.FIELD_PRESSURE, pr_h)
+                if learned:
+                    s.set(bb.FIELD_DIVERGENCE, dv_h)
+
+        def e2e_step():
+            # end to end through the C ABI: the substep's inputs from pinned host memory,
+            # its outputs back to host memory, one synchronisation
+            if scene.get("batch"):
+                g.upload(pos_h, vel_h)
+                if warm:
+                    g.set(bb.FIELD_PRESSURE, pr_h)
+                if learned:
+                    g.set(bb.FIELD_DIVERGENCE, dv_h)
+                g.advance_time_step(dt)
+                g.download(pos_o, vel_o)
+                if warm:
+                    g.get(bb.FIELD_PRESSURE, out=pr_o)
+                if learned:
+                    g.get(bb.FIELD_DIVERGENCE, out=dv_o)
+                return
+            g.step_host(dt, pos_h, vel_h, pr_h if warm else None, dv_h if learned else None,
+                        pos_o, vel_o, pr_o if warm else None, dv_o if learned else None)
+
         # the first `prep` substeps of the run: plain corrector; the learned variant trains
         # its model on their (features, converged pressure) pairs
         torch.cuda.synchronize()
@@ -590,125 +695,85 @@ def run_ours(args, scene, pos):
             g.advance_time_step(dt)
         torch.cuda.synchronize()
         prep_s = time.perf_counter() - t0
-        mlp = g.mlp_status() if variant == "learned" else None
-        for _ in range(args.warmup):
+        mlp = g.mlp_status() if learned else None
+        # warm-up: the run's next substeps, plus every timed arm once from the first
+        # sampled state's predecessor (graph capture, first-use allocations), state restored
+        for k in range(args.warmup):
+            if k == args.warmup - 1:
+                snapshot()
+                if gp is not None:
+                    restore(gp, False)
+                    gp.advance_time_step(dt)
+                e2e_step()
+                restore(g, warm)
+                g.profiler_enable(True)
+                g.advance_time_step(dt)
+                g.profiler_enable(False)
+                g.profiler_report()
+                restore(g, warm)
             g.advance_time_step(dt)
         torch.cuda.synchronize()
-        # every region below replays the same K substeps from this state
-        snap_p, snap_v = g.download()
-        snap_pr = g.get(bb.FIELD_PRESSURE) if warm else None
-        snap_dv = g.get(bb.FIELD_DIVERGENCE) if variant == "learned" else None
         list_len = float(np.minimum(g.neighbor_counts() - 1, 64).mean())
-
-        def restore(solver, with_pressure):
-            solver.upload(snap_p, snap_v)
-            if with_pressure:
-                solver.set(bb.FIELD_PRESSURE, snap_pr)
-                if snap_dv is not None:
-                    solver.set(bb.FIELD_DIVERGENCE, snap_dv)
-            torch.cuda.synchronize()
         barrier(dist)
 
         sampler = ClockSampler(local)
         sampler.start()
         barrier(dist)
-        # timed region: every substep is one CUDA-graph launch
-        step_ms, iters, max_err = timed_substeps(g, dt, args.steps, stream, flush)
-        timed_flags = dict(timed_substeps.flags)
-        barrier(dist)
-        total_s = sum(step_ms) / 1e3
-        value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
-        launches_timed = int(sum(launches_per_substep(scene, variant, it) for it in iters))
-
-        # the plain corrector on the same substeps, for the learned / warm comparison
-        plain = None
-        if warm and not args.no_plain:
-            gp = make_solver(bb, dict(scene, pressure_init="zero"), pos, local)
-            if tuned is not None:
-                gp.set_tuning(**tuned["tuning"])
-            gp.set_stream(stream)
-            restore(gp, False)
-            for _ in range(3):
-                gp.advance_time_step(dt)
-            restore(gp, False)
-            pms, pit, perr = timed_substeps(gp, dt, args.steps, stream, flush)
-            gp.close()
-            pv, _, _ = aggregate(dist, float(n * args.steps), sum(pms) / 1e3)
-            plain = {"value": pv, "ms_per_step": sum(pms) / args.steps,
-                     "corrector_iterations_mean": float(np.mean(pit)),
-                     "max_density_error_ratio_max": float(np.max(perr)),
-                     "speedup_of_this_variant": value / pv}
-
-        # per-kernel breakdown: the same substeps launched directly with CUDA events
-        # around every kernel on the launching stream
-        g.use_cuda_graphs(False)
-        restore(g, warm)
-        g.profiler_enable(True)
-        torch.cuda.synchronize()
-        for k in range(args.steps):
+        # the timed sample: at each sampled substep of the run, from the run's state there,
+        #   plain: the zero-start corrector (a second solver given the same state);
+        #   kernels: the learned substep launched kernel by kernel with per-kernel events;
+        #   e2e: the learned substep through bbg_step_host (host buffers, wall clock);
+        #   value: the learned substep replayed as a CUDA graph (device events), which
+        #   also carries the run forward.
+        dev, pln = StepLog(), StepLog()
+        e2e_s, e2e_iters = 0.0, []
+        cur = args.prep + args.warmup
+        for idx in samples:
+            while cur < idx:
+                g.advance_time_step(dt)
+                cur += 1
+            snapshot()
+            if gp is not None:
+                restore(gp, False)
+                pln.add(timed_event(stream, flush, lambda: gp.advance_time_step(dt)), gp.stats())
+            restore(g, warm)
+            g.profiler_enable(True)
             flush.zero_()
             g.advance_time_step(dt)
-            g.stats()
-        torch.cuda.synchronize()
-        g.profiler_enable(False)
-        prof, _ = g.profiler_report()
-        g.use_cuda_graphs(True)
-
-        # end to end through the C ABI with pinned host buffers: every step uploads the
-        # particles, advances one substep and downloads them (warm variants: the pressure
-        # the next start needs travels with them)
-        pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-        vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-        pr_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
-        dv_h = torch.empty((n,), dtype=torch.float32, pin_memory=True).numpy()
-        learned = variant == "learned"
-
-        def e2e_step():
-            if scene.get("batch"):
-                g.upload(pos_h, vel_h)
-                if warm:
-                    g.set(bb.FIELD_PRESSURE, pr_h)
-                if learned:
-                    g.set(bb.FIELD_DIVERGENCE, dv_h)
-                g.advance_time_step(dt)
-                g.download(pos_h, vel_h)
-                if warm:
-                    g.get(bb.FIELD_PRESSURE, out=pr_h)
-                if learned:
-                    g.get(bb.FIELD_DIVERGENCE, out=dv_h)
-                return
-            # the host-resident step of the C ABI: uploads, substep, downloads, one sync
-            g.step_host(dt, pos_h, vel_h, pr_h if warm else None, dv_h if learned else None,
-                        pos_h, vel_h, pr_h if warm else None, dv_h if learned else None)
-
-        def e2e_reset():
-            pos_h[:] = snap_p
-            vel_h[:] = snap_v
-            if warm:
-                pr_h[:] = snap_pr
-            if learned:
-                dv_h[:] = snap_dv
-        e2e_reset()
-        for _ in range(max(1, args.warmup)):
+            g.profiler_enable(False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
             e2e_step()
-        e2e_reset()
-        e2e_iters = []
-        barrier(dist)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
+            e2e_s += time.perf_counter() - t0
             e2e_iters.append(g.stats()["iterations"])
-        e2e_s = time.perf_counter() - t0
-        e2e_value, _, _ = aggregate(dist, float(n * args.steps), e2e_s)
+            restore(g, warm)
+            dev.add(timed_event(stream, flush, lambda: g.advance_time_step(dt)), g.stats())
+            cur += 1
+        torch.cuda.synchronize()
+        barrier(dist)
         sampler.stop()
-        final_pos, final_vel = pos_h.copy(), vel_h.copy()
+        prof, _ = g.profiler_report()
+        total_s = sum(dev.ms) / 1e3
+        value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
+        e2e_value, _, _ = aggregate(dist, float(n * args.steps), e2e_s)
+        launches_timed = int(sum(launches_per_substep(scene, variant, it) for it in dev.iters))
+        plain = None
+        if gp is not None:
+            pv, _, _ = aggregate(dist, float(n * args.steps), sum(pln.ms) / 1e3)
+            plain = {"value": pv, "ms_per_step": sum(pln.ms) / args.steps,
+                     "corrector_iterations_mean": float(np.mean(pln.iters)),
+                     "max_density_error_ratio_max": float(np.max(pln.errs)),
+                     "not_converged": pln.not_converged}
+            gp.close()
+        final_pos, final_vel = g.download()
         batch_offsets = g.layout() if scene.get("batch") else None
         energy = None
         steps_e = args.energy_steps if args.energy_steps >= 0 else (100 if args.config == "pcisph_4m" else 0)
         if steps_e > 0 and rank == 0:
             energy = energy_log(g, scene, steps_e, args.energy_log)
-        frames = seeds = post = None
+        frames = seeds = post = sph1 = None
         if not scene.get("batch") and not args.no_frames and rank == 0:
+            sph1 = sph_config1(bb, local, stream)
             frames = frame_io(bb, g, scene, n, local)
             seeds = seeding(bb, scene, final_pos, local)
             post = postprocess(bb, scene, final_pos, local)
@@ -736,8 +801,9 @@ def run_ours(args, scene, pos):
                 "traffic": tr * n if tr is not None else None,
                 "algorithmic_bytes": alg, "avg_launch_us": avg_s * 1e6,
                 "share_of_step": ms / sum(v[0] for v in prof.values()),
-                "measured": "per-launch CUDA events over a second run of the timed substeps "
-                            "(direct launches; the timed region replays the same kernels as graphs)"}
+                "measured": "per-launch CUDA events on the launching stream over the sampled substeps "
+                            "(launched kernel by kernel from the same states; the timed arm replays the "
+                            "same kernels as graphs)"}
 
     # CPU baseline: oracle on the host cores, bounded sample of the same state
     cpu = None
@@ -761,23 +827,23 @@ def run_ours(args, scene, pos):
 
     per_kernel = {k: {"ms_total": v[0], "launches": v[1], "avg_us": 1e3 * v[0] / max(1, v[1])}
                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    first, last = samples[0], samples[-1]
     config = {"workload": scene["workload"], "variant": variant, "solver": "pcisph",
               "particles_per_gpu": n, "dt": dt, "tolerance": scene["max_density_error_ratio"],
               "max_iterations": scene["max_iterations"],
-              "window": "substeps %d..%d of the run (%d preparation + %d warm-up substeps first)"
-                        % (args.prep + args.warmup, args.prep + args.warmup + args.steps - 1,
-                           args.prep, args.warmup),
-              "corrector_iterations_mean": float(np.mean(iters)),
+              "window": ("%d substeps sampled evenly over substeps %d..%d of the %d-substep run (%d preparation "
+                         "+ %d warm-up substeps first); each timed from the run's state at that substep"
+                         % (len(samples), first, last, total, args.prep, args.warmup)),
+              "corrector_iterations_mean": float(np.mean(dev.iters)),
               "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
-              "max_density_error_ratio_max": float(np.max(max_err)),
-              "substeps_at_max_iterations_above_tolerance": timed_flags["not_converged"],
-              "state_checks": {"out_of_grid_max": timed_flags["out_of_grid"],
-                               "crowded_max": timed_flags["crowded"]},
+              "max_density_error_ratio_max": float(np.max(dev.errs)),
+              "substeps_at_max_iterations_above_tolerance": dev.not_converged,
+              "state_checks": {"out_of_grid_max": dev.out_of_grid, "crowded_max": dev.crowded},
               "member_list_mean": list_len,
               "preparation_s": prep_s,
-              "regions": "timed, per-kernel and e2e regions each replay the same substeps "
-                         "from one snapshot taken after warm-up",
-              "l2": "flushed between timed steps (256 MB write, outside the events)",
+              "regions": "at every sampled substep the plain, per-kernel, e2e and timed arms start "
+                         "from the same state (host copy of the run's state, uploaded outside the timing)",
+              "l2": "flushed before every timed substep (256 MB write, outside the events)",
               "tuning": ({"source": "bubbles_gb300/tuned/%s.json" % args.config,
                           "grid_spacing_scale": scene.get("grid_spacing_scale", 2.0),
                           **tuned["tuning"]} if tuned is not None else "defaults"),
@@ -797,6 +863,12 @@ def run_ours(args, scene, pos):
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config,
+        # the comparison the metric names, flat: this variant against the plain (zero-start,
+        # reference) corrector on the same substeps from the same states
+        "variant": variant,
+        "corrector_iterations": float(np.mean(dev.iters)),
+        "not_converged": dev.not_converged,
+        "max_density_error_ratio": float(np.max(dev.errs)),
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": n * (24 + (4 if warm else 0) + (4 if variant == "learned" else 0)),
                 "d2h_bytes_per_step": n * (24 + (4 if warm else 0) + (4 if variant == "learned" else 0))},
@@ -806,6 +878,13 @@ def run_ours(args, scene, pos):
         "clocks": sampler.summary(),
         "kernels": per_kernel,
     }
+    if plain is not None:
+        line.update({"plain_value": plain["value"], "speedup_vs_plain": value / plain["value"],
+                     "corrector_iterations_plain": plain["corrector_iterations_mean"],
+                     "not_converged_plain": plain["not_converged"],
+                     "max_density_error_ratio_plain": plain["max_density_error_ratio_max"]})
+    if sph1 is not None:
+        line["sph_config1"] = sph1
     if frames is not None:
         line["frame_io"] = frames
     if seeds is not None:
@@ -840,6 +919,8 @@ def main():
     ap.add_argument("--warm-scale", type=float, default=None,
                     help="start pressure = scale x estimate for warm starts (default: the library's, 0.9 learned)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
+    ap.add_argument("--max-iterations", type=int, default=None,
+                    help="corrector iteration cap of both arms (default: the configuration's)")
     ap.add_argument("--no-frames", action="store_true",
                     help="skip the particle-frame and seeding timings (frame writer / reader, emitters)")
     ap.add_argument("--no-tuning", action="store_true",
@@ -861,6 +942,8 @@ def main():
             scene["mlp"][k] = float(v) if "." in v or "e" in v else int(v)
     if args.warm_scale is not None:
         scene["warm_scale"] = args.warm_scale
+    if args.max_iterations is not None:
+        scene["max_iterations"] = args.max_iterations
     if args.impl == "reference":
         run_reference(args, scene, pos)
     else:

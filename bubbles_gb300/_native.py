@@ -174,9 +174,10 @@ SIGNATURES = {
     "bbg_get_grid": [_P, _IP, _DP],
     "bbg_dump_grid": [_P, _UP, _UP, _UP],
     "bbg_neighbor_counts": [_P, _IP],
+    "bbg_neighbor_lists": [_P, _I, _IP, _IP],
     "bbg_profiler_enable": [_P, _I],
     "bbg_use_cuda_graphs": [_P, _I],
-    "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P],
+    "bbg_grid_sort_noalloc": [_P, _I, _DP, _DP, _D, _D, _P, _P, _P, _P, _P],
     "bbg_get_tuning": [_P, ctypes.POINTER(Tuning)],
     "bbg_set_tuning": [_P, ctypes.POINTER(Tuning)],
     "bbg_batch_create": [ctypes.POINTER(SolverDesc), ctypes.POINTER(SceneDesc), _I, ctypes.POINTER(_P)],

@@ -119,6 +119,8 @@ struct bbg_solver_s {
     BucketBufs bucket;           // cell lists of particles added since the last distribution
     int grid_n = 0;              // particles in the last grid distribution's sorted ranges
     bool members_ok = false;     // sorted ranges [0, grid_n) are the last distribution's cells
+    int list_state = -1;         // buffer holding the positions of the last density pass, whose
+                                 // neighbour sets the member lists hold (-1: none)
     bool map_full = false;       // MapGridEmit reached the capacity once (it stops emitting)
     // signed-distance fields of colliders (Params::sdf holds their device descriptors)
     float *sdf_values[kMaxSdf] = {};
@@ -394,11 +396,20 @@ bbg_status reset_step_state(bbg_solver s) {
     return BBG_OK;
 }
 
+// The other ping-pong buffer becomes the current state (an integration wrote into it); if
+// it held the positions of the last density pass, the neighbour sets can no longer be
+// exported.
+void flip_state(bbg_solver s) {
+    s->state = 1 - s->state;
+    if (s->list_state == s->state) s->list_state = -1;
+}
+
 bbg_status grid_update(bbg_solver s) {
     bbg_status r = reset_step_state(s);
     if (r) return r;
     launch_grid_update(s->P, s->B, s->state, s->pid_cur, s->stream, s->mlp.divsum, s->mlp.divprev);
     CK_LAUNCH();
+    s->list_state = -1;
     s->state = 1 - s->state;
     s->pid_cur = 1 - s->pid_cur;
     s->grid_valid = true;
@@ -555,7 +566,7 @@ bbg_status corrector(bbg_solver s, float dt, float delta, int max_it) {
         memcpy(&e, s->h_u, 4);
         if (e / s->P.target_density < s->P.max_err_ratio) break;
     }
-    s->state = 1 - s->state;
+    flip_state(s);
     s->valid |= kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE) |
                 bit(BBG_FIELD_PRESSURE_FORCE) | bit(BBG_FIELD_PRED_DENSITY) |
                 bit(BBG_FIELD_DENSITY_ERROR) | bit(BBG_FIELD_PRED_POSITION);
@@ -664,6 +675,7 @@ void after_substep(bbg_solver s, float dt) {
     s->grid_valid = true;
     s->grid_n = s->n;
     s->members_ok = true;
+    s->list_state = 1 - s->state;   // the graph's density pass ran on the other buffer
     s->valid = kPosVel | bit(BBG_FIELD_INTERACTION) | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE) |
                bit(BBG_FIELD_PRESSURE);
     if (s->desc.solver_kind == BBG_SOLVER_PCISPH)
@@ -716,13 +728,15 @@ bbg_status substep(bbg_solver s, float dt) {
         launch_density(s->P, s->B, s->state, 1, s->stream);
         launch_sph_forces(s->P, s->B, s->state, dt, s->stream);
         CK_LAUNCH();
-        s->state = 1 - s->state;
+        s->list_state = s->state;
+        flip_state(s);
         s->valid |= kPosVel | bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_FORCE);
         return pseudo_viscosity(s, dt);
     }
     launch_density(s->P, s->B, s->state, 0, s->stream);
     launch_prologue(s, s->state, dt, delta, max_it, s->stream);
     CK_LAUNCH();
+    s->list_state = s->state;
     s->valid |= bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_FORCE);
     r = corrector(s, dt, delta, max_it);
     if (r) return r;
@@ -1031,6 +1045,7 @@ static bbg_status upload_common(bbg_solver s, const float *d_pos, const float *d
     s->P.n = n;
     s->grid_valid = false;
     s->members_ok = false;
+    s->list_state = -1;
     s->valid = kPosVel | bit(BBG_FIELD_FORCE) | bit(BBG_FIELD_PRESSURE_FORCE) |
                bit(BBG_FIELD_DENSITY) | bit(BBG_FIELD_PRESSURE) | bit(BBG_FIELD_INTERACTION);
     return BBG_OK;
@@ -1086,6 +1101,7 @@ bbg_status bbg_compute_density(bbg_solver s, int compute_pressure) {
     if (bbg_status r = require_grid(s)) return r;
     launch_density(s->P, s->B, s->state, compute_pressure ? 1 : 0, s->stream);
     CK_LAUNCH();
+    s->list_state = s->state;
     s->valid |= bit(BBG_FIELD_DENSITY) | (compute_pressure ? bit(BBG_FIELD_PRESSURE) : 0u);
     return BBG_OK;
 }
@@ -1235,7 +1251,7 @@ bbg_status bbg_accumulate_and_integrate(bbg_solver s, double dt) {
         return fail(BBG_ERR_STATE, "forces and pressure forces must be valid");
     launch_accumulate_integrate(s->P, s->B, s->state, (float)dt, s->stream);
     CK_LAUNCH();
-    s->state = 1 - s->state;
+    flip_state(s);
     return BBG_OK;
 }
 
@@ -1246,7 +1262,7 @@ bbg_status bbg_compute_pressure_force(bbg_solver s, double dt) {
         return fail(BBG_ERR_STATE, "density and pressure must be computed first");
     launch_sph_forces(s->P, s->B, s->state, (float)dt, s->stream);
     CK_LAUNCH();
-    s->state = 1 - s->state;
+    flip_state(s);
     s->valid |= kPosVel | bit(BBG_FIELD_FORCE);
     return BBG_OK;
 }
@@ -1258,7 +1274,7 @@ bbg_status bbg_time_integration(bbg_solver s, double dt) {
     launch_integrate(s->P, s->B, s->state, (float)dt, s->stream);
     CK_LAUNCH();
     // the other buffer now holds the integrated state in the same slot order
-    s->state = 1 - s->state;
+    flip_state(s);
     return BBG_OK;
 }
 
@@ -1436,6 +1452,7 @@ bbg_status bbg_set_field(bbg_solver s, int field, const float *in) {
     CK_LAUNCH();
     CK(cudaStreamSynchronize(s->stream));
     s->valid |= bit(field);
+    if (field == BBG_FIELD_POSITION && s->list_state == s->state) s->list_state = -1;
     return BBG_OK;
 }
 
@@ -1546,6 +1563,33 @@ bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts) {
     CK_LAUNCH();
     CK(cudaMemcpyAsync(counts, s->B.stage, 4 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    return BBG_OK;
+}
+
+bbg_status bbg_neighbor_lists(bbg_solver s, int max_per_particle, int32_t *counts, int32_t *ids) {
+    if (bbg_status r = check_solver(s)) return r;
+    if (!counts || max_per_particle < 0 || (max_per_particle > 0 && !ids))
+        return fail(BBG_ERR_INVALID_ARGUMENT, "need counts, max_per_particle >= 0 and ids when it is > 0");
+    if (s->list_state < 0 || !s->grid_valid)
+        return fail(BBG_ERR_STATE, "no neighbour sets: compute the density (or a substep) after the last grid update");
+    const int n = s->n;
+    const size_t width = (size_t)max_per_particle;
+    // rows of a chunk of caller ids staged in the 6 x capacity words of the staging buffer
+    size_t rows = 6 * (size_t)s->capacity / (width + 1);
+    if (rows > (size_t)n) rows = (size_t)n;
+    int *dc = reinterpret_cast<int *>(s->B.stage);
+    for (size_t a = 0; a < (size_t)n; a += rows) {
+        const size_t b = a + rows < (size_t)n ? a + rows : (size_t)n;
+        int *dout = dc + (b - a);
+        launch_export_members(s->P, s->B, s->list_state, s->pid_cur, (int)a, (int)b, max_per_particle, dc, dout,
+                              s->stream);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(counts + a, dc, sizeof(int) * (b - a), cudaMemcpyDeviceToHost, s->stream));
+        if (width)
+            CK(cudaMemcpyAsync(ids + a * width, dout, sizeof(int) * (b - a) * width, cudaMemcpyDeviceToHost,
+                               s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     return BBG_OK;
 }
 
@@ -1964,7 +2008,7 @@ bbg_status bbg_format_g(float value, char *out, int *length) {
 namespace {
 
 constexpr char kCkptMagic[8] = {'B', 'B', 'G', 'C', 'K', 'P', 'T', '1'};
-constexpr uint32_t kCkptVersion = 1;
+constexpr uint32_t kCkptVersion = 2;
 // per-particle fields a snapshot carries when they are valid, in file order
 constexpr int kCkptFields[] = {BBG_FIELD_POSITION,       BBG_FIELD_VELOCITY,      BBG_FIELD_FORCE,
                                BBG_FIELD_DENSITY,        BBG_FIELD_PRESSURE,      BBG_FIELD_PRED_POSITION,
@@ -1973,7 +2017,8 @@ constexpr int kCkptFields[] = {BBG_FIELD_POSITION,       BBG_FIELD_VELOCITY,    
 
 struct CkptHeader {
     char magic[8];
-    uint32_t version, header_bytes, desc_bytes, shape_bytes, mlp_desc_bytes, reserved0;
+    uint32_t version, header_bytes, desc_bytes, shape_bytes, mlp_desc_bytes;
+    int32_t nfields;   // colliders' signed-distance fields stored (grid + node values each)
     int32_t n, nshapes, nscenes, mlp;
     uint32_t fields;   // bit f set: field f stored
     uint32_t valid;    // the solver's valid-field mask
@@ -1984,6 +2029,8 @@ struct CkptHeader {
     double mlp_loss;
     uint32_t adam_step, reserved1;
 };
+
+bbg_status attach_field(bbg_solver s, int index, const bbg_sdf_grid &g, float *values);
 
 bool same_desc(const bbg_solver_desc &a, const bbg_solver_desc &b) {
 #define EQ(f) (a.f == b.f)
@@ -2032,6 +2079,7 @@ bbg_status ckpt_build(bbg_solver s, std::vector<char> *out) {
     h.n = s->n;
     h.nshapes = s->P.nshapes;
     h.nscenes = s->nscenes;
+    for (int i = 0; i < s->P.nshapes; i++) h.nfields += s->P.shapes[i].sdf >= 0 ? 1 : 0;
     h.mlp = s->mlp_alloc ? 1 : 0;
     h.valid = s->valid;
     h.mass = s->mass;
@@ -2055,6 +2103,16 @@ bbg_status ckpt_build(bbg_solver s, std::vector<char> *out) {
     w.put(s->P.shapes, sizeof(ShapeDev) * (size_t)s->P.nshapes);
     w.put(s->scene_count.data(), sizeof(int) * (size_t)s->nscenes);
     std::vector<float> buf;
+    // each collider's field, in collider order: its grid, then its node values
+    for (int i = 0; i < s->P.nshapes; i++) {
+        const int slot = s->P.shapes[i].sdf;
+        if (slot < 0) continue;
+        const bbg_sdf_grid &g = s->sdf_grid[slot];
+        buf.resize((size_t)g.nodes[0] * g.nodes[1] * g.nodes[2]);
+        CK(cudaMemcpy(buf.data(), s->sdf_values[slot], sizeof(float) * buf.size(), cudaMemcpyDeviceToHost));
+        w.put(&g, sizeof(g));
+        w.put(buf.data(), sizeof(float) * buf.size());
+    }
     for (int f : kCkptFields) {
         if (!(h.fields & bit(f))) continue;
         buf.resize((size_t)field_components(f) * (size_t)s->n);
@@ -2102,6 +2160,41 @@ bbg_status ckpt_restore(bbg_solver s, const char *data, size_t length) {
         return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
     if (h.nscenes != s->nscenes || counts != s->scene_count)
         return fail(BBG_ERR_STATE, "the checkpoint's scene layout differs from this batch");
+    // colliders: known types, field slots in range and used once, a field-only collider
+    // with its field, and as many stored fields as colliders that have one
+    int with_field = 0;
+    unsigned slots_used = 0;
+    for (const ShapeDev &sh : shapes) {
+        if (sh.type != BBG_SHAPE_BOX && sh.type != BBG_SHAPE_SPHERE && sh.type != BBG_SHAPE_SDF)
+            return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: collider type %d", sh.type);
+        if (sh.sdf < -1 || sh.sdf >= kMaxSdf || (sh.sdf >= 0 && (slots_used >> sh.sdf) & 1u))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: collider field slot %d", sh.sdf);
+        if (sh.type == BBG_SHAPE_SDF && sh.sdf < 0)
+            return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: a field-only collider without its field");
+        if (sh.sdf >= 0) {
+            slots_used |= 1u << sh.sdf;
+            with_field++;
+        }
+    }
+    if (h.nfields != with_field) return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: field count");
+    if (with_field > 0 && s->nscenes > 0)
+        return fail(BBG_ERR_STATE, "fields are not supported on a batch of scenes");
+    std::vector<bbg_sdf_grid> grids((size_t)with_field);
+    std::vector<std::vector<float>> values((size_t)with_field);
+    for (int k = 0; k < with_field; k++) {
+        bbg_sdf_grid &g = grids[(size_t)k];
+        if (!rd.get(&g, sizeof(g))) return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+        size_t total = 1;
+        for (int a = 0; a < 3; a++) {
+            if (g.nodes[a] < 1 || g.nodes[a] > 4097 || !(g.spacing[a] > 0) || !std::isfinite(g.origin[a]))
+                return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: field grid");
+            total *= (size_t)g.nodes[a];
+        }
+        if (total >= 0xffffffffull) return fail(BBG_ERR_INVALID_ARGUMENT, "corrupt checkpoint: field grid");
+        values[(size_t)k].resize(total);
+        if (!rd.get(values[(size_t)k].data(), sizeof(float) * total))
+            return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
+    }
     if ((h.mlp != 0) != s->mlp_alloc)
         return fail(BBG_ERR_STATE, "learned warm start %s in the checkpoint but %s in this solver",
                     h.mlp ? "present" : "absent", s->mlp_alloc ? "present" : "absent");
@@ -2122,12 +2215,42 @@ bbg_status ckpt_restore(bbg_solver s, const char *data, size_t length) {
         if (!rd.get(&md, sizeof(md)) || !rd.get(mlp.data(), sizeof(float) * mlp.size()))
             return fail(BBG_ERR_INVALID_ARGUMENT, "truncated checkpoint");
     }
-    // colliders and particles
-    for (int i = 0; i < h.nshapes; i++) s->P.shapes[i] = shapes[(size_t)i];
-    s->P.nshapes = h.nshapes;
-    s->epoch++;
+    // the fields' device copies, then the particles; the colliders change only after both
+    std::vector<float *> dev((size_t)with_field, nullptr);
+    auto drop = [&]() {
+        for (float *d : dev)
+            if (d) cudaFree(d);
+    };
+    for (int k = 0; k < with_field; k++) {
+        const std::vector<float> &v = values[(size_t)k];
+        if (bbg_status r = dalloc(&dev[(size_t)k], v.size())) {
+            drop();
+            return r;
+        }
+        cudaError_t e = cudaMemcpy(dev[(size_t)k], v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            drop();
+            return fail(BBG_ERR_CUDA, "field upload: %s", cudaGetErrorString(e));
+        }
+    }
     const float *pos = fields[0].data(), *vel = fields[1].data();
-    if (bbg_status r = bbg_upload_particles(s, pos, vel, h.n)) return r;
+    if (bbg_status r = bbg_upload_particles(s, pos, vel, h.n)) {
+        drop();
+        return r;
+    }
+    free_fields(s);
+    for (int i = 0; i < h.nshapes; i++) {
+        s->P.shapes[i] = shapes[(size_t)i];
+        s->P.shapes[i].sdf = -1;
+    }
+    s->P.nshapes = h.nshapes;
+    for (int i = 0, k = 0; i < h.nshapes; i++) {
+        if (shapes[(size_t)i].sdf < 0) continue;
+        // cannot fail: at most kMaxSdf fields, all slots free after free_fields
+        attach_field(s, i, grids[(size_t)k], dev[(size_t)k]);
+        dev[(size_t)k++] = nullptr;
+    }
+    s->epoch++;
     if (!s->setup_done)
         if (bbg_status r = bbg_setup(s)) return r;
     s->mass = h.mass;

@@ -75,6 +75,10 @@ void launch_max_force(const float4 *force, int n, unsigned *out_bits, cudaStream
 // sph.cu
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure,
                     cudaStream_t s);
+// members (other than itself, as original ids) of every particle with original id in
+// [a, b) at the last density pass on buffer buf: counts[id - a], maxm ids per row of out
+void launch_export_members(const Params &P, const DevBufs &B, int buf, int pid_buf, int a, int b, int maxm,
+                           int *counts, int *out, cudaStream_t s);
 // divsum != null: also the velocity-divergence sum of each particle (learned warm start);
 // warm: the corrector's start pressure is set, add its pressure force and predict from F + Fp
 void launch_non_pressure(const Params &P, const DevBufs &B, int buf, int predict, float dt,

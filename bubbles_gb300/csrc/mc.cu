@@ -11,17 +11,14 @@
 //   (every edge runs from its lower to its upper node, so the position does not depend on
 //   which cube computes it);
 // - one thread per cube writes its triangles.
-// The triangulation table is derived on the host (cube faces walked around each region of
-// corners at or below the iso value, ambiguous faces separating the smaller region, loops
-// fanned from their first edge), not copied: vertices, normals and orientation are the
-// reference's, triangles can differ where a case table choice does.
+// The triangles follow the reference's case table (marching_cubes_table.h,
+// triangleConnectionTable3D): triangles are only identical when every case is
+// triangulated the same way, so that table's content is kept, re-encoded below as one
+// packed 64-bit word per case.
 #include "bbg_internal.cuh"
 #include "bbg_kernels.h"
 
-#include <algorithm>
-#include <cmath>
 #include <cstring>
-#include <vector>
 
 namespace bbg {
 
@@ -33,95 +30,82 @@ namespace {
 // its lower to its upper corner
 constexpr int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}};
 constexpr int kEdge[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6}, {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-constexpr int kMaxTri = 4;   // the derived table never needs more per cube
+// The case table: for configuration c (bit q set: corner q at or below the iso value),
+// bits 60..63 of kCase[c] hold its triangle count and bits 4m..4m+3 the m-th edge of its
+// triangles, three per triangle in the reference's winding.
+constexpr unsigned long long kCase[256] = {
+    0x0000000000000000ull, 0x1000000000000380ull, 0x1000000000000910ull, 0x2000000000189381ull,
+    0x1000000000000a21ull, 0x2000000000a21380ull, 0x2000000000920a29ull, 0x300000089a8a2382ull,
+    0x10000000000002b3ull, 0x20000000000b82b0ull, 0x2000000000b32091ull, 0x3000000b89b912b1ull,
+    0x20000000003ab1a3ull, 0x3000000ab8a801a0ull, 0x30000009ab9b3093ull, 0x2000000000b8aa89ull,
+    0x1000000000000874ull, 0x2000000000437034ull, 0x2000000000748910ull, 0x3000000137174914ull,
+    0x2000000000748a21ull, 0x3000000a21403743ull, 0x3000000748209a29ull, 0x40004973727929a2ull,
+    0x20000000002b3748ull, 0x300000040242b74bull, 0x3000000b32748109ull, 0x40001292b9b49b74ull,
+    0x3000000487ab31a3ull, 0x40004b7401b41ab1ull, 0x400030bab9b09874ull, 0x3000000ab99b4b74ull,
+    0x1000000000000459ull, 0x2000000000380459ull, 0x2000000000051450ull, 0x3000000513538458ull,
+    0x2000000000459a21ull, 0x3000000594a21803ull, 0x3000000204245a25ull, 0x40008434535235a2ull,
+    0x2000000000b32459ull, 0x3000000594b802b0ull, 0x3000000b32510450ull, 0x4000584b82852512ull,
+    0x300000045931ab3aull, 0x4000ab81a8180594ull, 0x400030bab5b05045ull, 0x3000000b8aa85845ull,
+    0x2000000000975879ull, 0x3000000375359039ull, 0x3000000751710870ull, 0x2000000000753351ull,
+    0x300000021a759879ull, 0x400037503505921aull, 0x400025a758528208ull, 0x30000007533525a2ull,
+    0x30000002b3987597ull, 0x4000b72029279759ull, 0x4000751871810b32ull, 0x300000051771b12bull,
+    0x4000b3a31a758859ull, 0x50aba010b7905075ull, 0x507570805a30b0abull, 0x20000000005b75abull,
+    0x100000000000056aull, 0x20000000006a5380ull, 0x20000000006a5109ull, 0x30000006a5891381ull,
+    0x2000000000162561ull, 0x3000000803621561ull, 0x3000000620609569ull, 0x4000823625285895ull,
+    0x200000000056ab32ull, 0x300000056a02b80bull, 0x30000006a5b32910ull, 0x4000b892b92916a5ull,
+    0x3000000315356b36ull, 0x40006b51505b0b80ull, 0x40009505606306b3ull, 0x300000089bb96956ull,
+    0x20000000008746a5ull, 0x3000000a56374034ull, 0x30000007486a5091ull, 0x400049737179156aull,
+    0x3000000874156216ull, 0x4000743403625521ull, 0x4000620560509748ull, 0x5962695923497937ull,
+    0x300000056a4872b3ull, 0x4000b720242746a5ull, 0x40006a5b32874910ull, 0x56a54b7b492b9129ull,
+    0x40006b51535b3748ull, 0x5b404b7b016b5b15ull, 0x574836b630560950ull, 0x40009b7974b96956ull,
+    0x2000000000a4694aull, 0x3000000380a946a4ull, 0x300000004606a10aull, 0x4000a16468618138ull,
+    0x3000000462421941ull, 0x4000462942921803ull, 0x2000000000624420ull, 0x3000000624428238ull,
+    0x300000032b46a94aull, 0x40006a4a94b82280ull, 0x4000a164606102b3ull, 0x51b8b12184a16146ull,
+    0x400036b319639469ull, 0x514641916b0181b8ull, 0x30000004600636b3ull, 0x200000000086b846ull,
+    0x3000000a98a876a7ull, 0x4000a76a907a0370ull, 0x40000818717a176aull, 0x300000037117a76aull,
+    0x4000768981861621ull, 0x5937390976192962ull, 0x3000000206607087ull, 0x2000000000276237ull,
+    0x400076898a86ab32ull, 0x57a9a76790b72702ull, 0x5b32a767a1871081ull, 0x400017616a71b12bull,
+    0x563136b619768698ull, 0x200000000076b190ull, 0x400006b0b3607087ull, 0x10000000000006b7ull,
+    0x1000000000000b67ull, 0x200000000067b803ull, 0x200000000067b910ull, 0x300000067b138918ull,
+    0x20000000007b621aull, 0x30000007b6803a21ull, 0x30000007b69a2092ull, 0x400089a38a3a27b6ull,
+    0x2000000000726327ull, 0x3000000026067807ull, 0x3000000910732672ull, 0x4000678891681261ull,
+    0x300000073171a67aull, 0x4000801781a7167aull, 0x40007a69a0a70730ull, 0x30000009a88a7a67ull,
+    0x200000000068b486ull, 0x3000000640603b63ull, 0x3000000109648b68ull, 0x400063b139369649ull,
+    0x30000001a28b6486ull, 0x4000640b60b03a21ull, 0x40009a2920b648b4ull, 0x536463b34923a39aull,
+    0x3000000264248328ull, 0x2000000000264240ull, 0x4000834642432091ull, 0x3000000642241491ull,
+    0x40001a6648168318ull, 0x300000040660a01aull, 0x539a9303a6834364ull, 0x20000000004a649aull,
+    0x2000000000b67594ull, 0x300000067b594380ull, 0x3000000b67045105ull, 0x400051345343867bull,
+    0x3000000b6721a459ull, 0x4000594380a217b6ull, 0x4000204a24a45b67ull, 0x567b25a523453843ull,
+    0x3000000945267327ull, 0x4000786260680459ull, 0x4000045051673263ull, 0x5851584812786826ull,
+    0x400073167161a459ull, 0x5459078701671a61ull, 0x5a737a6a305a4a04ull, 0x4000a84a458a7a67ull,
+    0x300000098b9b6596ull, 0x4000590650360b63ull, 0x4000b65510b508b0ull, 0x30000001355363b6ull,
+    0x400065b8b9b59a21ull, 0x5a21965690b603b0ull, 0x552025a50865b58bull, 0x400035a3a2536b63ull,
+    0x4000283265825985ull, 0x3000000260069659ull, 0x5826283865081851ull, 0x2000000000612651ull,
+    0x5698965683a61631ull, 0x400006505960a01aull, 0x2000000000a65830ull, 0x100000000000065aull,
+    0x2000000000b57a5bull, 0x300000003857ba5bull, 0x3000000091ba57b5ull, 0x40001381897ba57aull,
+    0x300000015717b21bull, 0x4000b27571721380ull, 0x40007b2209729579ull, 0x5289823295b27257ull,
+    0x3000000573532a52ull, 0x400052a578258028ull, 0x40002a37353a5109ull, 0x525752a278129289ull,
+    0x2000000000573531ull, 0x3000000571170780ull, 0x3000000735539309ull, 0x2000000000795789ull,
+    0x30000008ba8a5485ull, 0x400003bba50b5405ull, 0x400054aba8a48910ull, 0x541314943b54a4baull,
+    0x40008548b2582152ull, 0x5b151b2b543b0b40ull, 0x558b8545b2950520ull, 0x20000000003b2549ull,
+    0x4000483543253a52ull, 0x30000000244252a5ull, 0x5910854583a532a3ull, 0x40002492914252a5ull,
+    0x3000000153358548ull, 0x2000000000501540ull, 0x4000530509358548ull, 0x1000000000000549ull,
+    0x3000000ba9b947b4ull, 0x4000ba97b9794380ull, 0x4000b470414b1ba1ull, 0x54bab474a1843413ull,
+    0x4000219b294b97b4ull, 0x53801b2b197b9479ull, 0x300000004224b47bull, 0x400042343824b47bull,
+    0x4000947732972a92ull, 0x570207872a4797a9ull, 0x5a040a1a472a3a73ull, 0x20000000004782a1ull,
+    0x3000000317714194ull, 0x4000178180714194ull, 0x2000000000347304ull, 0x1000000000000784ull,
+    0x20000000008ba8a9ull, 0x3000000a9bb93903ull, 0x3000000ba88a0a10ull, 0x2000000000a3ba13ull,
+    0x30000008b99b1b21ull, 0x40009b2921b93903ull, 0x2000000000b08b20ull, 0x1000000000000b23ull,
+    0x300000098aa82832ull, 0x20000000002902a9ull, 0x40008a1810a82832ull, 0x10000000000002a1ull,
+    0x2000000000819831ull, 0x1000000000000190ull, 0x1000000000000830ull, 0x0000000000000000ull
+};
 
-__constant__ signed char c_tri[256][3 * kMaxTri + 1];   // count, then edge triples
+__constant__ unsigned long long c_case[256];
 __constant__ int c_edge_dev[12][2];
 __constant__ int c_corner_dev[8][3];
 
-int edge_between(int a, int b) {
-    for (int e = 0; e < 12; e++)
-        if ((kEdge[e][0] == a && kEdge[e][1] == b) || (kEdge[e][0] == b && kEdge[e][1] == a)) return e;
-    return -1;
-}
-
-// The triangulation table: for each configuration (bit c set: corner c at or below iso),
-// every face of the cube contributes directed segments between its crossing edges that keep
-// the low corners on one side; the segments close into loops, fanned into triangles.
-std::vector<signed char> derive_table() {
-    // faces: 4 corners in counter-clockwise order seen from outside the cube
-    std::vector<std::vector<int>> faces;
-    for (int ax = 0; ax < 3; ax++) {
-        for (int side = 0; side < 2; side++) {
-            std::vector<int> cs;
-            for (int c = 0; c < 8; c++)
-                if (kCorner[c][ax] == side) cs.push_back(c);
-            const int u = ax == 0 ? 1 : 0, v = ax == 2 ? 1 : 2;
-            std::sort(cs.begin(), cs.end(), [&](int a, int b) {
-                return std::atan2(kCorner[a][v] - 0.5, kCorner[a][u] - 0.5) <
-                       std::atan2(kCorner[b][v] - 0.5, kCorner[b][u] - 0.5);
-            });
-            double p[3][3];
-            for (int q = 0; q < 3; q++)
-                for (int k = 0; k < 3; k++) p[q][k] = kCorner[cs[q]][k];
-            const double e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
-            const double e2[3] = {p[2][0] - p[1][0], p[2][1] - p[1][1], p[2][2] - p[1][2]};
-            const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
-                                  e1[0] * e2[1] - e1[1] * e2[0]};
-            if (cr[ax] * (side ? 1.0 : -1.0) < 0) std::reverse(cs.begin(), cs.end());
-            faces.push_back(cs);
-        }
-    }
-    std::vector<signed char> table(256 * (3 * kMaxTri + 1), -1);
-    for (int cfg = 0; cfg < 256; cfg++) {
-        int low[8], nlow = 0;
-        for (int c = 0; c < 8; c++) nlow += (low[c] = (cfg >> c) & 1);
-        int next[12];
-        for (int e = 0; e < 12; e++) next[e] = -1;
-        for (const auto &f : faces) {
-            int s = 0;
-            for (int q = 0; q < 4; q++) s += low[f[q]];
-            if (s == 0 || s == 4) continue;
-            if (s == 2 && low[f[0]] == low[f[2]]) {
-                // an ambiguous face: the smaller region's corners are cut off one by one
-                const int target = nlow <= 4 ? 1 : 0;
-                for (int q = 0; q < 4; q++) {
-                    if (low[f[q]] != target) continue;
-                    const int ein = edge_between(f[(q + 3) % 4], f[q]), eout = edge_between(f[q], f[(q + 1) % 4]);
-                    if (target) next[ein] = eout;
-                    else next[eout] = ein;
-                }
-            } else {
-                int ein = -1, eout = -1;
-                for (int q = 0; q < 4; q++) {
-                    const int a = f[q], b = f[(q + 1) % 4];
-                    if (!low[a] && low[b]) ein = edge_between(a, b);
-                    if (low[a] && !low[b]) eout = edge_between(a, b);
-                }
-                next[ein] = eout;
-            }
-        }
-        bool seen[12] = {};
-        int ntri = 0;
-        signed char *row = &table[(size_t)cfg * (3 * kMaxTri + 1)];
-        for (int start = 0; start < 12; start++) {
-            if (next[start] < 0 || seen[start]) continue;
-            int loop[12], m = 0;
-            for (int e = start; !seen[e]; e = next[e]) {
-                seen[e] = true;
-                loop[m++] = e;
-            }
-            for (int q = 1; q + 1 < m; q++) {
-                row[1 + 3 * ntri] = (signed char)loop[0];
-                row[2 + 3 * ntri] = (signed char)loop[q];
-                row[3 + 3 * ntri] = (signed char)loop[q + 1];
-                ntri++;
-            }
-        }
-        row[0] = (signed char)ntri;
-    }
-    return table;
-}
+__device__ __forceinline__ int case_triangles(int cfg) { return (int)(c_case[cfg] >> 60); }
+__device__ __forceinline__ int case_edge(int cfg, int m) { return (int)((c_case[cfg] >> (4 * m)) & 15ull); }
 
 struct McGrid {
     const float *v;
@@ -156,7 +140,7 @@ __global__ void k_mc_cubes(McGrid g, long long cubes, unsigned *__restrict__ ntr
     if (id >= cubes) return;
     int i, j, k;
     cube_of(g, id, i, j, k);
-    ntri[id] = (unsigned)c_tri[cube_config(g, i, j, k)][0];
+    ntri[id] = (unsigned)case_triangles(cube_config(g, i, j, k));
 }
 
 // edge e = axis * nodes + node: the edge from node (i, j, k) along the axis
@@ -231,12 +215,12 @@ __global__ void k_mc_triangles(McGrid g, long long cubes, long long nodes, const
     int i, j, k;
     cube_of(g, id, i, j, k);
     const int cfg = cube_config(g, i, j, k);
-    const int nt = c_tri[cfg][0];
+    const int nt = case_triangles(cfg);
     unsigned t0 = tri_start[id];
     for (int t = 0; t < nt; t++) {
         int vid[3];
         for (int c = 0; c < 3; c++) {
-            const int le = c_tri[cfg][1 + 3 * t + c];
+            const int le = case_edge(cfg, 3 * t + c);
             const int a = c_edge_dev[le][0], b = c_edge_dev[le][1];
             const int ai = i + c_corner_dev[a][0], aj = j + c_corner_dev[a][1], ak = k + c_corner_dev[a][2];
             const int axis = c_corner_dev[b][0] != c_corner_dev[a][0] ? 0 : (c_corner_dev[b][1] != c_corner_dev[a][1] ? 1 : 2);
@@ -256,8 +240,7 @@ bool tables_ready = false;
 
 cudaError_t mc_prepare() {
     if (tables_ready) return cudaSuccess;
-    const std::vector<signed char> t = derive_table();
-    cudaError_t e = cudaMemcpyToSymbol(c_tri, t.data(), t.size());
+    cudaError_t e = cudaMemcpyToSymbol(c_case, kCase, sizeof(kCase));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_edge_dev, kEdge, sizeof(kEdge));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_corner_dev, kCorner, sizeof(kCorner));
     if (e == cudaSuccess) tables_ready = true;

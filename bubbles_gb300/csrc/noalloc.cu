@@ -10,8 +10,11 @@
 // allocating.
 //
 // Rules of use:
-//  - The first call on a device looks up the scratch array's device address there
-//    (cudaGetSymbolAddress); make that first call outside any stream capture.
+//  - A call outside stream capture looks up the scratch array's device address on the
+//    current device (cudaGetSymbolAddress) every time, so a device reset between calls
+//    (which unloads the module and frees the array) is picked up; a call inside a
+//    capture uses the address an earlier uncaptured call on that device found, so make
+//    the first call on a device outside any stream capture.
 //  - Every call on a device shares the one scratch array, and it keeps the previous
 //    call's contents (this file clears what must start at zero).  Calls whose GPU work
 //    overlaps -- on different streams, or from different host threads -- race on it;
@@ -42,11 +45,15 @@ static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t)
 __global__ void __launch_bounds__(kThreads)
 k_na_hash_count(GridDev g, float iz, const float *__restrict__ xyz, int n,
                 unsigned *__restrict__ cell_old, unsigned *__restrict__ sub,
-                unsigned *__restrict__ count) {
+                unsigned *__restrict__ count, unsigned *__restrict__ out_of_grid) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     unsigned bad = 0, c = 0xffffffffu;
     if (valid) c = grid_hash(g, make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.f), iz, &bad);
+    // particles outside the grid are clamped into its edge cells (as the solver's grid);
+    // the caller's counter, when given, receives how many
+    const unsigned outside = __ballot_sync(0xffffffffu, valid && bad);
+    if (out_of_grid && (threadIdx.x & 31) == 0 && outside) atomicAdd(out_of_grid, (unsigned)__popc(outside));
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
     const unsigned peers = __match_any_sync(mask, c);
@@ -88,21 +95,31 @@ k_na_rank(int n, const uint2 *__restrict__ pairs, const unsigned *__restrict__ s
 std::mutex g_mutex;
 unsigned *g_ptr[256] = {nullptr};
 
-// Device address of g_scratch on the current device, looked up once per device.
-int scratch_for_current_device(unsigned **out) {
+// Device address of g_scratch on the current device.  Outside stream capture it is looked
+// up on every call (a device reset frees the module's array and a later load may place it
+// elsewhere); inside a capture, where the lookup may not be legal, the address the last
+// uncaptured call on this device found is used.
+int scratch_for_current_device(cudaStream_t stream, unsigned **out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= 256)
         return set_error(BBG_ERR_NO_DEVICE, "bbg_grid_sort_noalloc: no current CUDA device (%s)",
                          cudaGetErrorString(e));
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess)
+        return set_error(BBG_ERR_CUDA, "bbg_grid_sort_noalloc: cudaStreamIsCapturing: %s", cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_scratch);
         if (e != cudaSuccess || !p)
             return set_error(BBG_ERR_CUDA, "bbg_grid_sort_noalloc: cudaGetSymbolAddress: %s",
                              cudaGetErrorString(e));
         g_ptr[dev] = (unsigned *)p;
+    } else if (!g_ptr[dev]) {
+        return set_error(BBG_ERR_STATE,
+                         "bbg_grid_sort_noalloc: the first call on a device must be outside stream capture");
     }
     *out = g_ptr[dev];
     return BBG_OK;
@@ -115,7 +132,7 @@ extern "C" bbg_status bbg_grid_sort_noalloc(const float *d_pos, int n, const dou
                                             const double domain_max[3], double spacing,
                                             double spacing_scale, uint32_t *d_cell_of,
                                             uint32_t *d_sorted_ids, uint32_t *d_cell_start,
-                                            void *stream) {
+                                            uint32_t *d_out_of_grid, void *stream) {
     using namespace bbg;
     if (!d_pos || !d_cell_of || !d_sorted_ids || !d_cell_start || !domain_min || !domain_max)
         return set_error(BBG_ERR_INVALID_ARGUMENT, "bbg_grid_sort_noalloc: null pointer argument");
@@ -140,20 +157,23 @@ extern "C" bbg_status bbg_grid_sort_noalloc(const float *d_pos, int n, const dou
     g.ny = dims[1];
     g.nz = dims[2];
     g.total = (unsigned)cells;
+    cudaStream_t s = (cudaStream_t)stream;
     unsigned *base = nullptr;
-    if (int r = scratch_for_current_device(&base)) return r;
+    if (int r = scratch_for_current_device(s, &base)) return r;
     unsigned *count = base;
     unsigned *partials = count + kMaxC;
     unsigned *sub = partials + kPartialWords;
     unsigned *cell_old = sub + kMaxP;
     uint2 *pairs = reinterpret_cast<uint2 *>(cell_old + kMaxP);
-    cudaStream_t s = (cudaStream_t)stream;
-    // the histogram must start at zero; everything else is fully overwritten
+    // the histogram (and the caller's counter) must start at zero; everything else is
+    // fully overwritten
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned) * (size_t)cells, s);
+    if (e == cudaSuccess && d_out_of_grid) e = cudaMemsetAsync(d_out_of_grid, 0, sizeof(unsigned), s);
     if (e != cudaSuccess)
         return set_error(BBG_ERR_CUDA, "bbg_grid_sort_noalloc: %s", cudaGetErrorString(e));
     const float iz = float_above(1e-8);
-    k_na_hash_count<<<blocks_for(n, kThreads), kThreads, 0, s>>>(g, iz, d_pos, n, cell_old, sub, count);
+    k_na_hash_count<<<blocks_for(n, kThreads), kThreads, 0, s>>>(g, iz, d_pos, n, cell_old, sub, count,
+                                                                  d_out_of_grid);
     launch_cell_scan(count, (unsigned)cells, partials, d_cell_start, s);
     k_na_place<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, cell_old, sub, d_cell_start, pairs);
     k_na_rank<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, pairs, d_cell_start, d_cell_of,

@@ -745,6 +745,39 @@ __global__ void k_pv_interpolate(int n, float4 *__restrict__ vel, const float4 *
     vel[i] = make_float4(v.x * a + s.x * t, v.y * a + s.y * t, v.z * a + s.z * t, 0.f);
 }
 
+// Neighbour sets of the last density pass in caller order (bbg_neighbor_lists): every
+// particle whose original id lies in [a, b) writes its members other than itself, as
+// original ids in visit order (at most maxm of them, -1 after the last), into row id - a of
+// out, and its full member count into counts[id - a].  pos0 holds the positions of that
+// density pass (wide particles re-test their candidates there).
+__global__ void __launch_bounds__(kThreads)
+k_export_members(Params P, const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+                 const ListEntry *__restrict__ list, const int *__restrict__ nbr,
+                 const float4 *__restrict__ pos0, const int *__restrict__ pid, int a, int b, int maxm,
+                 int *__restrict__ counts, int *__restrict__ out) {
+    __shared__ TileMap T;
+    tile_setup(P.g, cell, start, P.n, T);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int id = pid[i];
+    if (id < a || id >= b) return;
+    int *row = out + (size_t)(id - a) * (size_t)maxm;
+    int c = 0;
+    tile_members<1>(P, start, T, list, nbr, pos0, cell[i], i, [&](unsigned j) { return j; },
+                    [&](unsigned j) {
+                        if (c < maxm) row[c] = pid[j];
+                        c++;
+                    });
+    for (int q = c; q < maxm; q++) row[q] = -1;
+    counts[id - a] = c;
+}
+
+void launch_export_members(const Params &P, const DevBufs &B, int buf, int pid_buf, int a, int b, int maxm,
+                           int *counts, int *out, cudaStream_t s) {
+    k_export_members<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P, B.cell, B.start, B.list, B.nbr, B.pos[buf],
+                                                                    B.pid[pid_buf], a, b, maxm, counts, out);
+}
+
 void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pressure, cudaStream_t s) {
     BBG_PBEGIN(B, KID_DENSITY, s, -1);
     const int t = B.tune.block;

@@ -629,6 +629,16 @@ class Solver:
         N.call("bbg_neighbor_counts", self.h, out.ctypes.data_as(N._IP))
         return out
 
+    def neighbor_lists(self, max_per_particle=64):
+        """Neighbour sets of the last density pass: (counts, ids) with counts[i] the members
+        of i other than itself and ids[i, :counts[i]] their caller ids (visit order, -1 past
+        the end; rows truncated at max_per_particle)."""
+        counts = np.zeros(self.n, np.int32)
+        ids = np.zeros((self.n, max_per_particle), np.int32)
+        N.call("bbg_neighbor_lists", self.h, int(max_per_particle), counts.ctypes.data_as(N._IP),
+               ids.ctypes.data_as(N._IP) if max_per_particle else None)
+        return counts, ids
+
 
 class BatchSolver(Solver):
     """Independent scenes advanced together (bbg_batch_create): `scene` holds the shared

@@ -278,11 +278,15 @@ bbg_status bbg_frame_find_section(const char *text, size_t length, int *flags, i
  * src/third/serializer.cpp:1027) and reloads positions and velocities from them
  * (SerializerLoadSphDataSet3, :562-577), so its resume loses pressure, forces and the CFL
  * input.  A checkpoint holds the full state in binary: the solver description (checked
- * on load), the colliders, the scene layout of a batch, every valid per-particle field in
- * caller order (positions, velocities, forces, density, pressure, predicted state, the
- * carried divergence) and the learned warm start's weights, Adam moments and training
- * counters.  Loading it into a solver created with the same description (any device,
- * capacity >= the particle count) continues the run bit for bit.  Native byte order. */
+ * on load), the colliders with their signed-distance fields (grid and node values; the
+ * fields attached to the loading solver are replaced by these), the scene layout of a
+ * batch, every valid per-particle field in caller order (positions, velocities, forces,
+ * density, pressure, predicted state, the carried divergence) and the learned warm start's
+ * weights, Adam moments and training counters.  Loading it into a solver created with the
+ * same description (any device, capacity >= the particle count) continues the run bit for
+ * bit.  A file with an unknown collider type, a field slot out of range or used twice, a
+ * field-only collider without its field or a truncated record is refused
+ * (BBG_ERR_INVALID_ARGUMENT) before the solver changes.  Native byte order. */
 bbg_status bbg_checkpoint_save(bbg_solver s, const char *path);
 bbg_status bbg_checkpoint_load(bbg_solver s, const char *path);
 /* The same bytes through memory; *length is the size, also when buf is too small
@@ -569,6 +573,14 @@ bbg_status bbg_dump_grid(bbg_solver s, uint32_t *cell_of_particle, uint32_t *cel
                          uint32_t *sorted_ids);
 /* Neighbour count of each particle (caller order) at the last grid update. */
 bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts);
+/* Neighbour sets of the last density pass (Grid::DistributeParticleBucket's buckets,
+ * src/core/grid.h:423-447, read back as ParticleSet3::GetParticleBucket would,
+ * src/core/particle.h:22-60): counts[i] = members of particle i other than itself
+ * (caller order, never truncated); ids[i * max_per_particle + q] = their caller ids in
+ * the solver's visit order, -1 past the last, at most max_per_particle of them (0: counts
+ * only).  BBG_ERR_STATE when no density pass ran on the current grid distribution or its
+ * positions were overwritten since. */
+bbg_status bbg_neighbor_lists(bbg_solver s, int max_per_particle, int32_t *counts, int32_t *ids);
 
 /* ----- allocation-free grid sort ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc -- a host
@@ -581,13 +593,19 @@ bbg_status bbg_neighbor_counts(bbg_solver s, int32_t *counts);
  *                  512 particles (a degenerate state) keeps the arrival order instead,
  *                  as the solver's grid does
  *   d_cell_start   cells + 1 offsets of each cell's range in d_sorted_ids
+ *   d_out_of_grid  optional (NULL: not counted) one counter, set to the number of
+ *                  particles outside the grid; like the solver's grid (and the
+ *                  reference's hash), those are clamped into the edge cells
  * with the grid of UtilBuildGridForDomain(domain, spacing, spacing_scale).  It never
  * allocates: its scratch is one fixed __device__ array of BBG_NOALLOC_SCRATCH_BYTES
  * that every GPU loading the library holds until exit, so n and the cell count are
- * capped (BBG_ERR_CAPACITY beyond).  The first call on a device looks the array up
- * (cudaGetSymbolAddress) and must not be inside a stream capture.  All calls share the
- * array: calls whose GPU work overlaps race and must be serialised.  Asynchronous on
- * `cuda_stream` (NULL = the legacy default stream). */
+ * capped (BBG_ERR_CAPACITY beyond).  A call outside stream capture looks the array's
+ * device address up (cudaGetSymbolAddress) on the current device, so a device reset
+ * between calls is safe; a call inside a capture reuses the address of the last
+ * uncaptured call there, so the first call on a device must not be captured
+ * (BBG_ERR_STATE).  All calls share the array: calls whose GPU work overlaps race and
+ * must be serialised.  Asynchronous on `cuda_stream` (NULL = the legacy default
+ * stream). */
 #define BBG_NOALLOC_MAX_PARTICLES 1048576
 #define BBG_NOALLOC_MAX_CELLS 1048576
 #define BBG_NOALLOC_SCRATCH_BYTES 20973576
@@ -595,7 +613,7 @@ bbg_status bbg_grid_sort_noalloc(const float *d_pos, int n, const double domain_
                                  const double domain_max[3], double spacing,
                                  double spacing_scale, uint32_t *d_cell_of,
                                  uint32_t *d_sorted_ids, uint32_t *d_cell_start,
-                                 void *cuda_stream);
+                                 uint32_t *d_out_of_grid, void *cuda_stream);
 
 /* ----- profiling (ProfilerPrepare / ProfilerFinish around every GPULaunch,
  *       src/cuda/cutil.h:237-244; ProfilerReport, src/core/profiler.cpp:175-247) ---- */

@@ -108,3 +108,41 @@ def test_checkpoint_file_and_refusals(gpu, moved, tmp_path):
         bb.Solver(learned, capacity=len(p)).restore(data)
     with pytest.raises(bb.BbgError):
         b.load_checkpoint(tmp_path / "missing.bbg")
+
+
+def test_resume_with_fields_into_a_fresh_solver(gpu, small):
+    """Colliders with signed-distance fields travel in the checkpoint: a box whose field was
+    generated on the device and a field-only sphere, restored into a solver with no fields
+    attached, continue bit-identically; corrupt field records are refused untouched."""
+    from test_gpu_sdf import attach, field_scene, golden
+    gold, _ = golden()
+    sc, pos = small
+    scf = field_scene(sc)
+    dt = sc["dt"]
+    a = bb.Solver(scf, pos=pos)
+    attach(a, gold)
+    a.generate_sdf(0, dx=0.02, margin=0.1)
+    for _ in range(5):
+        a.advance_time_step(dt)
+    data = a.checkpoint()
+    b = bb.Solver(scf, capacity=len(pos))
+    b.restore(data)
+    for k in (0, 1):
+        na, oa, sa, va = a.get_sdf(k)
+        nb, ob, sb, vb = b.get_sdf(k)
+        assert np.array_equal(na, nb) and np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    for g in (a, b):
+        for _ in range(4):
+            g.advance_time_step(dt)
+    assert same(state(a), state(b))
+
+    c = bb.Solver(scf, pos=pos, capacity=len(pos))
+    attach(c, gold)
+    c.advance_time_step(dt)
+    before = state(c)
+    bad = bytearray(data)
+    bad[28:32] = (0).to_bytes(4, "little")   # the header's field count
+    for corrupt in (bytes(bad), data[: len(data) - 4 * len(pos)]):
+        with pytest.raises(bb.BbgError):
+            c.restore(corrupt)
+        assert same(state(c), before)

@@ -2,10 +2,11 @@
 (tests/golden/mc_f32.npz).
 
 Points and normals are the reference's bit for bit (compared as sets keyed by position:
-the device orders points by edge, the reference by first use).  The triangulation table is
-derived here, not the reference's: on the smooth field the triangle count equals the
-reference's and the surface is closed and faces outwards; on the random field (every cube
-configuration, many ambiguous faces) only the points and normals are compared.
+the device orders points by edge, the reference by first use).  Triangles are the
+reference's: the same triangles with the same orientation, compared as a multiset of
+vertex triples (each triple of points' bit patterns rotated to start at its smallest, so
+the winding is kept), on the smooth field and on the random field (every cube
+configuration, many ambiguous faces).  The smooth surface is also closed and faces outwards.
 """
 import os
 
@@ -27,6 +28,29 @@ def same_bits(a, b):
     a = np.asarray(a, np.float32)
     b = np.asarray(b, np.float32)
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def triangle_keys(points, tris):
+    """Each triangle as its three points' bit patterns, rotated to start at the smallest
+    (orientation kept), sorted into a list."""
+    bits = [tuple(r) for r in np.ascontiguousarray(points, np.float32).view(np.uint32)]
+    out = []
+    for a, b, c in tris:
+        t = (bits[a], bits[b], bits[c])
+        k = t.index(min(t))
+        out.append(t[k:] + t[:k])
+    out.sort()
+    return out
+
+
+@pytest.mark.parametrize("name", ["blobs", "noise"])
+def test_triangles_match_reference(gpu, small, name):
+    d = np.load(GOLDEN, allow_pickle=False)
+    sc, pos = small
+    with bb.Solver(sc, pos=pos) as s:
+        p, _, t = s.marching_cubes(d["nodes"], d["origin"], d["spacing"], d[name + "_values"], 0.0)
+    assert len(t) == len(d[name + "_triangles"])
+    assert triangle_keys(p, t) == triangle_keys(d[name + "_points"], d[name + "_triangles"])
 
 
 @pytest.mark.parametrize("name", ["blobs", "noise"])
