@@ -587,6 +587,53 @@ def sph_config1(bb, device, stream, advances=200):
                         "count back to the host)"}
 
 
+def batched_config4(bb, device, stream, flush, samples=10, prep=200):
+    """Config 4, 64 dam breaks of uneven sizes in one batch (3.7 M particles), learned warm
+    start against the plain corrector: `prep` plain substeps (the MLP trains on them), then
+    `samples` substeps spread evenly over the rest of the 500-substep run, each timed from
+    the run's state with both correctors (CUDA events, L2 flushed before each)."""
+    from bubbles_gb300 import autotune, scenes
+    sc, pos = scenes.config("batched_64", seed=0)
+    tuned = autotune.load("batched_64")
+    if tuned is not None:
+        sc = dict(sc, grid_spacing_scale=tuned["grid_spacing_scale"])
+    scl = dict(sc, pressure_init="learned", mlp={"train_substeps": prep})
+    scp = dict(sc, pressure_init="zero")
+    g, gp = make_solver(bb, scl, pos, device), make_solver(bb, scp, pos, device)
+    for s_ in (g, gp):
+        if tuned is not None:
+            s_.set_tuning(**tuned["tuning"])
+        s_.set_stream(stream)
+    dt, n = sc["dt"], sum(len(p) for p in pos)
+    for _ in range(prep):
+        g.advance_time_step(dt)
+    learned, plain = StepLog(), StepLog()
+    cur = prep
+    for idx in sample_substeps(prep + 5, sc["steps"], samples):
+        while cur < idx:
+            g.advance_time_step(dt)
+            cur += 1
+        p, v = g.download()
+        pr, dv = g.get(bb.FIELD_PRESSURE), g.get(bb.FIELD_DIVERGENCE)
+        gp.upload(p, v)
+        plain.add(timed_event(stream, flush, lambda: gp.advance_time_step(dt)), gp.stats())
+        g.upload(p, v)
+        g.set(bb.FIELD_PRESSURE, pr)
+        g.set(bb.FIELD_DIVERGENCE, dv)
+        learned.add(timed_event(stream, flush, lambda: g.advance_time_step(dt)), g.stats())
+        cur += 1
+    g.close()
+    gp.close()
+    lv, pv = n * samples / (sum(learned.ms) / 1e3), n * samples / (sum(plain.ms) / 1e3)
+    return {"workload": sc["workload"], "particles": n, "samples": samples,
+            "window": "substeps %d..%d of the %d-substep run" % (prep + 5, sc["steps"] - 1, sc["steps"]),
+            "learned_value": lv, "plain_value": pv, "speedup_vs_plain": lv / pv,
+            "corrector_iterations_learned_slowest_scene": float(np.mean(learned.iters)),
+            "corrector_iterations_plain_slowest_scene": float(np.mean(plain.iters)),
+            "not_converged_learned": learned.not_converged, "not_converged_plain": plain.not_converged,
+            "unit": UNIT, "measured": "CUDA events on the launching stream, one substep per sample from the run's state"}
+
+
 def energy_log(g, scene, substeps, path=None, every=10):
     """FP64 mass and energy of the state every `every` substeps of a run after the timed
     region (device reductions, bbg_energy), as JSONL records; optionally written to `path`."""
@@ -635,13 +682,18 @@ def run_ours(args, scene, pos):
             if tuned is not None and scene.get("batch"):
                 scene = dict(scene, grid_spacing_scale=tuned["grid_spacing_scale"])
 
+        overrides = {k: int(v) for k, v in (kv.split("=", 1) for kv in args.tune)}
+
         def solver(sc):
             s = make_solver(bb, sc, pos, local)
             if tuned is not None:
                 s.set_tuning(**tuned["tuning"])
+            if overrides:
+                s.set_tuning(**overrides)
             s.set_stream(stream)
             return s
         g = solver(scene)
+        tuning_used = g.tuning()
         gp = solver(dict(scene, pressure_init="zero")) if compare else None
         # host copies of a sampled substep's input state (pinned): the e2e step reads them,
         # and every other timed arm is restored from them
@@ -771,13 +823,15 @@ def run_ours(args, scene, pos):
         steps_e = args.energy_steps if args.energy_steps >= 0 else (100 if args.config == "pcisph_4m" else 0)
         if steps_e > 0 and rank == 0:
             energy = energy_log(g, scene, steps_e, args.energy_log)
-        frames = seeds = post = sph1 = None
+        frames = seeds = post = sph1 = batch4 = None
         if not scene.get("batch") and not args.no_frames and rank == 0:
-            sph1 = sph_config1(bb, local, stream)
             frames = frame_io(bb, g, scene, n, local)
             seeds = seeding(bb, scene, final_pos, local)
             post = postprocess(bb, scene, final_pos, local)
         g.close()
+        if not scene.get("batch") and not args.no_frames and rank == 0:
+            sph1 = sph_config1(bb, local, stream)
+            batch4 = batched_config4(bb, local, stream, flush)
 
     if rank != 0:
         barrier(dist)
@@ -844,9 +898,9 @@ def run_ours(args, scene, pos):
               "regions": "at every sampled substep the plain, per-kernel, e2e and timed arms start "
                          "from the same state (host copy of the run's state, uploaded outside the timing)",
               "l2": "flushed before every timed substep (256 MB write, outside the events)",
-              "tuning": ({"source": "bubbles_gb300/tuned/%s.json" % args.config,
-                          "grid_spacing_scale": scene.get("grid_spacing_scale", 2.0),
-                          **tuned["tuning"]} if tuned is not None else "defaults"),
+              "tuning": dict({"source": ("bubbles_gb300/tuned/%s.json" % args.config) if tuned is not None
+                              else "defaults",
+                              "grid_spacing_scale": scene.get("grid_spacing_scale", 2.0)}, **tuning_used),
               "parallelism": "replicas" if world > 1 else "single gpu"}
     if variant == "warm":
         config["warm_start"] = "previous substep's pressure x 0.5, monotone corrector update"
@@ -856,7 +910,9 @@ def run_ours(args, scene, pos):
         config["mlp"] = {"trained_substeps": mlp["trained_substeps"], "adam_steps": mlp["adam_steps"],
                          "last_training_loss": mlp["last_loss"],
                          "training": "online during the %d preparation substeps" % args.prep}
+    config["iterations_per_sample"] = [int(x) for x in dev.iters]
     if plain is not None:
+        plain["iterations_per_sample"] = [int(x) for x in pln.iters]
         config["plain_same_window"] = plain
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -885,6 +941,8 @@ def run_ours(args, scene, pos):
                      "max_density_error_ratio_plain": plain["max_density_error_ratio_max"]})
     if sph1 is not None:
         line["sph_config1"] = sph1
+    if batch4 is not None:
+        line["batched_config4"] = batch4
     if frames is not None:
         line["frame_io"] = frames
     if seeds is not None:
@@ -919,6 +977,8 @@ def main():
     ap.add_argument("--warm-scale", type=float, default=None,
                     help="start pressure = scale x estimate for warm starts (default: the library's, 0.9 learned)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-corrector comparison")
+    ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
+                    help="launch tuning override after the tuned file (bbg_tuning fields, e.g. block_size=64)")
     ap.add_argument("--max-iterations", type=int, default=None,
                     help="corrector iteration cap of both arms (default: the configuration's)")
     ap.add_argument("--no-frames", action="store_true",

@@ -94,3 +94,44 @@ def test_batch_learned_warm_start_runs(gpu):
         assert st["max_density_error_ratio"] < 0.01
     assert g.mlp_status()["trained_substeps"] == 4
     g.close()
+
+
+def test_batched_64_scenes_against_oracle(gpu):
+    """Config 4 (64 dam breaks of uneven sizes in one batch): after 30 substeps, one substep
+    of four scenes -- the smallest, the largest and two from the middle -- against the FP32
+    oracle (the reference algorithm) run on each scene alone from the batch's state: the
+    same corrector iterations, the tolerance met, positions within the rounding of the
+    scene's translation into the packed domain (4 ulps of the packed coordinate) plus
+    1e-5 x spacing."""
+    import os
+    from oracle import oracle as O
+    sc, pos = scenes.config("batched_64", seed=0)
+    boxes = sc["boxes"]
+    g = bb.BatchSolver(sc, boxes, pos)
+    for _ in range(30):
+        g.advance_time_step(sc["dt"])
+    ps, vs = g.download_scenes()
+    g.advance_time_step(sc["dt"])
+    its, errs = g.scene_stats()
+    nxt, _ = g.download_scenes()
+    off = g.layout()
+    g.close()
+    order = np.argsort([len(p) for p in pos])
+    picks = [int(order[0]), int(order[-1]), int(order[len(order) // 2]), int(order[len(order) // 3])]
+    threads = os.cpu_count() or 1
+    for k in picks:
+        lo, hi = boxes[k]
+        ext = tuple(float(b - a) for a, b in zip(lo, hi))
+        center = tuple(float(a + b) / 2 for a, b in zip(lo, hi))
+        one = dict(sc, domain_min=tuple(lo), domain_max=tuple(hi), batch=False,
+                   colliders=[{"type": "box", "size": ext, "center": center, "reverse": True}])
+        o = O.OracleSim(one, ps[k], vs[k], variant="f32", threads=threads)
+        it_o, _ = o.pcisph_substep(sc["dt"], sc["max_density_error_ratio"], sc["max_iterations"],
+                                   O.PCISPH_TOLERANCE)
+        want = o.get(O.POSITION)
+        o.close()
+        assert its[k] == it_o, (k, its[k], it_o)
+        assert errs[k] < sc["max_density_error_ratio"]
+        packed = np.abs(want + off[k][None, :]).astype(np.float32)
+        allowed = 4.0 * np.spacing(packed).astype(np.float64) + 1e-5 * sc["spacing"]
+        assert np.all(np.abs(nxt[k] - want) <= allowed), (k, float(np.max(np.abs(nxt[k] - want) - allowed)))

@@ -8,14 +8,20 @@ oracle (the reference CPU path restated, all host threads) -- pass by pass:
   - neighbour sets: every particle's members, as sets (not only their number), equal to
     the oracle's buckets (src/core/grid.h:423-447);
   - density: relative 1e-5 per particle (all summands positive);
-  - non-pressure force (from identical density), pressure of one corrector pass and the
-    pressure force (from identical p, rho*): |error_i| <= 1e-5 x the sum of the
-    magnitudes of particle i's summands -- the FP32 error bound of a sum with
-    cancellation, per particle;
+  - non-pressure force (from identical density) and pressure of one corrector pass:
+    |error_i| <= 1e-5 x the sum of the magnitudes of particle i's summands -- the FP32
+    error bound of a sum with cancellation, per particle;
+  - pressure force (from identical p, rho*): the same with each summand's conditioned
+    magnitude.  A summand c (1 - d/h)^2 is computed from a distance d that carries its own
+    rounding, and 1 - d/h cancels near the kernel radius: its first-order error is
+    c x (x + 2 d/h) eps <= c x (x + 2) eps with x = 1 - d/h, so the bound is
+    1e-5 x sum_j c_j x_j (x_j + 2) (a few times the summand far inside the kernel; near
+    the kernel radius, where (1 - d/h)^2 is tiny, the conditioning term dominates);
   - predictions, accumulation and integration with colliders: bit-exact from identical
     inputs;
   - a whole tolerance-mode substep (src/equations/pcisph_equations3.cpp:218-256): the
-    same number of corrector iterations and positions within 1e-5 x spacing.
+    same number of corrector iterations and positions within 1e-5 x spacing or 2 ulps of
+    the coordinate, whichever is larger (an FP32 coordinate cannot be closer than its ulp).
 
 Every case prints the per-particle relative error percentiles (p50, p99, max), and
 appends them as one JSON line to $BBG_PARITY_REPORT when that is set.
@@ -181,7 +187,11 @@ def test_substep_parity_full_size(gpu, name, seed, substeps):
     o.predict_pressure_force()
     a = np.abs(pg.astype(np.float64)) / (rs_g.astype(np.float64) ** 2)
     kg = m * m * 45.0 / (np.pi * h ** 4)
-    s_pf = pair_sum(x, rows, lambda i, j, r: kg * (a[i] + a[j]) * np.clip(1 - r / h, 0, None) ** 2)
+
+    def conditioned(i, j, r):
+        xk = np.clip(1 - r / h, 0, None)
+        return kg * (a[i] + a[j]) * xk * (xk + 2.0)
+    s_pf = pair_sum(x, rows, conditioned)
     fp_g, fp_o = g.get(bb.FIELD_PRESSURE_FORCE), o.get(O.PRESSURE_FORCE)
     dfp = np.linalg.norm(fp_g - fp_o, axis=1)
     rep["pressure_force_err_over_summands"] = percentiles(dfp / np.maximum(s_pf, 1e-30))
@@ -215,14 +225,18 @@ def test_substep_parity_full_size(gpu, name, seed, substeps):
     rep["substep"] = {"iterations_gpu": st["iterations"], "iterations_oracle": it_o,
                       "max_err_gpu": st["max_density_error_ratio"], "max_err_oracle": err_o}
     pg3, vg3 = g.download()
-    dx = np.linalg.norm(pg3 - o.get(O.POSITION), axis=1) / h0
+    po3 = o.get(O.POSITION)
+    dxyz = np.abs(pg3.astype(np.float64) - po3)
+    allowed = np.maximum(RTOL * h0, 2.0 * np.spacing(np.abs(po3).astype(np.float32)).astype(np.float64))
+    dx = np.linalg.norm(pg3 - po3, axis=1) / h0
     rep["substep"]["position_err_over_spacing"] = percentiles(dx)
+    rep["substep"]["position_err_over_allowed"] = percentiles((dxyz / allowed).max(axis=1))
     rep["substep"]["density_rel"] = percentiles(np.abs(g.get(bb.FIELD_DENSITY) - o.get(O.DENSITY)) / o.get(O.DENSITY))
     g.close()
     o.close()
     checks["substep_iterations"] = st["iterations"] == it_o
     checks["substep_max_error"] = abs(st["max_density_error_ratio"] - err_o) <= 1e-4
-    checks["substep_positions"] = dx.max() <= RTOL
+    checks["substep_positions"] = bool(np.all(dxyz <= allowed))
     rep["checks"] = {k: bool(v) for k, v in checks.items()}
     report(rep)
     assert all(checks.values()), [k for k, v in checks.items() if not v]
