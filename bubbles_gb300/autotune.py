@@ -7,6 +7,8 @@ same substeps (replayed as CUDA graphs from that state) for candidate settings:
     block walks): 64, 128, 256;
   * members whose neighbour records a thread requests together, separately for the
     non-pressure, predicted-density and pressure-force passes: 2, 4, 8;
+  * whether the density pass leaves out the neighbour cells and rows each particle's
+    sphere cannot reach (bitwise the same results): 0, 1;
   * for batches only, the grid cell as a multiple of the particle spacing: 2 (the kernel
     radius), 2.5, 3 -- any cell at least the kernel radius keeps every neighbour inside
     the 27 cells, and a batch has no reference grid to match.  A single scene keeps the
@@ -30,6 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED_DIR = os.path.join(HERE, "tuned")
 BLOCKS = (64, 128, 256)
 BATCHES = (2, 4, 8)
+PRUNES = (0, 1)
 CELL_SCALES = (2.0, 2.5, 3.0)
 
 
@@ -82,8 +85,8 @@ def tune_launches(g, dt, snap, steps, warm, log):
     best = dict(g.tuning())
     best_t = time_substeps(g, dt, snap, steps, warm)
     log.append({"tuning": dict(best), "seconds": best_t})
-    for key, values in (("block_size", BLOCKS), ("batch_pf", BATCHES), ("batch_pd", BATCHES),
-                        ("batch_np", BATCHES)):
+    for key, values in (("block_size", BLOCKS), ("prune", PRUNES), ("batch_pf", BATCHES),
+                        ("batch_pd", BATCHES), ("batch_np", BATCHES)):
         for v in values:
             if v == best[key]:
                 continue
@@ -134,8 +137,9 @@ def main():
     ap.add_argument("--prep", type=int, default=100)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
-    res = tune(args.config, args.prep, args.steps, args.variant)
+    res = tune(args.config, args.prep, args.steps, args.variant, args.seed)
     out = args.out or tuned_path(args.config)
     os.makedirs(os.path.dirname(out), exist_ok=True)
     with open(out, "w") as f:

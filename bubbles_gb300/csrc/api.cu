@@ -156,6 +156,16 @@ void fill_params(bbg_solver s) {
     P.nb_lo = lo;
     P.nb_hi = hi;
     P.h2mz = (float)T;
+    // margin of the density pass's reach test: far above the rounding of positions and cell
+    // faces (64 ulps of the largest grid coordinate) and the reference hash's 1e-4 nudge of
+    // particles on the grid's bounds
+    float cmax = 0.f;
+    const int dn[3] = {P.g.nx, P.g.ny, P.g.nz};
+    for (int k = 0; k < 3; k++) {
+        const float top = P.g.minp[k] + (float)dn[k] * P.g.len[k];
+        cmax = fmaxf(cmax, fmaxf(fmaxf(fabsf(P.g.bmin[k]), fabsf(P.g.bmax[k])), fmaxf(fabsf(P.g.minp[k]), fabsf(top))));
+    }
+    P.prune_m = fmaxf(fmaxf(1e-3f * P.h, 1.5e-4f), 64.f * cmax * 1.1920929e-7f);
     const double kPi = 3.14159265358979323846;
     const float h3 = P.h2 * P.h, h4 = P.h2 * P.h2, h5 = P.h2 * h3;
     P.std_c = (float)(315.0 / (64.0 * kPi * (double)h3));
@@ -1889,6 +1899,7 @@ bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t) {
     t->batch_np = s->B.tune.batch_np;
     t->batch_pd = s->B.tune.batch_pd;
     t->batch_pf = s->B.tune.batch_pf;
+    t->prune = s->B.tune.prune;
     return BBG_OK;
 }
 
@@ -1899,11 +1910,13 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
         return fail(BBG_ERR_INVALID_ARGUMENT, "block size must be 64, 128 or 256");
     for (int b : {t->batch_np, t->batch_pd, t->batch_pf})
         if (b != 2 && b != 4 && b != 8) return fail(BBG_ERR_INVALID_ARGUMENT, "gather batches must be 2, 4 or 8");
+    if (t->prune != 0 && t->prune != 1) return fail(BBG_ERR_INVALID_ARGUMENT, "prune must be 0 or 1");
     CK(cudaStreamSynchronize(s->stream));
     s->B.tune.block = t->block_size;
     s->B.tune.batch_np = t->batch_np;
     s->B.tune.batch_pd = t->batch_pd;
     s->B.tune.batch_pf = t->batch_pf;
+    s->B.tune.prune = t->prune;
     s->epoch++;   // captured graphs hold the old launch shapes
     return BBG_OK;
 }

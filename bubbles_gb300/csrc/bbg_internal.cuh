@@ -69,6 +69,7 @@ struct Params {
     float nb_lo;     // r^2 < nb_lo => IsWithinStd holds for sure
     float nb_hi;     // r^2 > nb_hi => IsWithinStd fails for sure
     float h2mz;      // h^2 - iz: W_std(r) > 0 <=> r^2 < h2mz (to FP32 rounding)
+    float prune_m;   // margin of the density pass's reach test (far above position rounding)
     float std_c;     // 315 / (64 pi h^3)
     float spiky_dw_c;   // 45 / (pi h^4)
     float spiky_d2w_c;  // 90 / (pi h^5)

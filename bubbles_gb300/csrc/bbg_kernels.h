@@ -14,6 +14,7 @@ struct Tuning {
     int batch_np = 4;      // non-pressure pass (two records per member)
     int batch_pd = 4;      // predicted-density pass
     int batch_pf = 4;      // pressure-force pass
+    int prune = 1;         // density pass: walk only the cells each particle's sphere reaches
 };
 
 // Device buffers of one solver (all sized for `capacity` particles / grid cells).

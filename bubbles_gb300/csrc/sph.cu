@@ -36,6 +36,12 @@ constexpr int kThreads = kTile;
 // a few spilled registers for occupancy, 8 for the others).  Kernels are compiled for
 // blocks of up to kMaxTile threads with the same register budget.
 constexpr int kNbrMinBlocks = BBG_NBR_MIN_BLOCKS * kTile / kMaxTile;
+#ifndef BBG_PD_MIN_BLOCKS
+#define BBG_PD_MIN_BLOCKS 16
+#endif
+// the predicted-density pass fits 32 registers without spilling (gather batch 4): full
+// occupancy for its latency-bound gathers
+constexpr int kPdMinBlocks = BBG_PD_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kPfMinBlocks = BBG_PF_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kDensityMinBlocks = 12 * kTile / kMaxTile;
 #ifndef BBG_DENSITY_MASK
@@ -220,7 +226,7 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
              const unsigned *__restrict__ start, const float *__restrict__ rec, float *__restrict__ rho,
              float *__restrict__ inv_rho,
              float *__restrict__ press, int *__restrict__ nbr, ListEntry *__restrict__ list, int compute_pressure,
-             StepState *st) {
+             StepState *st, int prune) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
@@ -238,9 +244,9 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
         const f2 X = f2_pack(pi.x, pi.x), Y = f2_pack(pi.y, pi.y), Z = f2_pack(pi.z, pi.z);
         const f2 NIH = f2_pack(-P.inv_h2, -P.inv_h2), ONE = f2_pack(1.f, 1.f);
         const float lo = P.nb_lo, hi = P.nb_hi, ih2 = P.inv_h2;
-        tile_rows(P.g, start, cw & ~kWide, [&](int, unsigned b, unsigned e) {
+        tile_rows_pruned(P, start, pi, cw & ~kWide, prune != 0, [&](int, unsigned b, unsigned e, unsigned whole) {
             if (crowded) return;
-            seen += e - b;
+            seen += whole;   // the work cap counts the 27 cells' candidates, walked or not
             if (seen > kMaxCandidates) {
                 crowded = true;
                 return;
@@ -440,7 +446,7 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
 // predicted positions, with the density error stored (tolerance mode) and reduced to
 // max |err| and sum |err| for iteration k; also p / rho*^2 for the pressure force.
 template <int NB>
-__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
+__global__ void __launch_bounds__(kMaxTile, kPdMinBlocks)
 k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
                const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
@@ -784,7 +790,8 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
     if (kDensityX2 && !kListRelative) {
         k_soa<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P.n, B.pos[buf], B.soa);
         k_density_x2<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.soa, B.rho,
-                                                      B.inv_rho, B.press, B.nbr, B.list, compute_pressure, B.st);
+                                                      B.inv_rho, B.press, B.nbr, B.list, compute_pressure, B.st,
+                                                      B.tune.prune);
     } else {
         k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
                                                    B.press, B.nbr, B.list, compute_pressure, B.st);

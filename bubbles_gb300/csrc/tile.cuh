@@ -125,6 +125,63 @@ __device__ __forceinline__ void tile_candidates(const GridDev &g, const unsigned
     }
 }
 
+// The rows of tile_rows for the density pass of particle i (position pi): f(r, b, e, whole)
+// with whole the row's candidate count and [b, e) the part of it walked.  With `prune`, a
+// row whose cells lie farther than the kernel radius from pi in y and z is not walked, and
+// the cell below or above in x is left out of a row when pi's sphere cannot reach it: a
+// member j of that cell would satisfy x-distance >= (the distance from pi to its cell's face)
+// and x-distance < sqrt(h^2 - dy^2 - dz^2), with dy, dz the y-z distances to the row's
+// cells.  Distances are reduced (and the radius enlarged) by the margin P.prune_m, far above
+// the rounding of positions and cell faces, so the walked candidates hold every member; they
+// are the row's own candidates in the row's order, so the members and their order are the
+// unpruned walk's.  A particle outside its own cell by more than the margin (clamped into
+// the grid) walks whole rows.
+template <class F>
+__device__ __forceinline__ void tile_rows_pruned(const Params &P, const unsigned *__restrict__ start, float4 pi,
+                                                 unsigned c, bool prune, F &&f) {
+    const GridDev &g = P.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
+    const int cz = (int)(c / plane);
+    const unsigned rem = c - (unsigned)cz * plane;
+    const int cy = (int)(rem / (unsigned)nx);
+    const int cx = (int)(rem - (unsigned)cy * (unsigned)nx);
+    const int x0 = cx > 0 ? cx - 1 : 0;
+    const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+    const int z0 = cz > 0 ? cz - 1 : 0, z1 = cz + 1 < nz ? cz + 1 : nz - 1;
+    const int y0 = cy > 0 ? cy - 1 : 0, y1 = cy + 1 < ny ? cy + 1 : ny - 1;
+    const float m = P.prune_m, hm = P.h + m, hm2 = hm * hm;
+    // offsets of pi in its cell: the distances to the faces of the cells below and above
+    const float ux = pi.x - (g.minp[0] + (float)cx * g.len[0]);
+    const float uy = pi.y - (g.minp[1] + (float)cy * g.len[1]);
+    const float uz = pi.z - (g.minp[2] + (float)cz * g.len[2]);
+    prune = prune && ux >= -m && ux <= g.len[0] + m && uy >= -m && uy <= g.len[1] + m && uz >= -m &&
+            uz <= g.len[2] + m;
+    const float ax_lo = ux - m, ax_hi = g.len[0] - ux - m;
+    const float dy_lo = fmaxf(uy - m, 0.f), dy_hi = fmaxf(g.len[1] - uy - m, 0.f);
+    const float dz_lo = fmaxf(uz - m, 0.f), dz_hi = fmaxf(g.len[2] - uz - m, 0.f);
+    for (int z = z0; z <= z1; ++z) {
+        const float dz = z < cz ? dz_lo : (z > cz ? dz_hi : 0.f);
+        for (int y = y0; y <= y1; ++y) {
+            const float dy = y < cy ? dy_lo : (y > cy ? dy_hi : 0.f);
+            const unsigned row = (unsigned)y * (unsigned)nx + (unsigned)z * plane;
+            const unsigned fb = __ldg(&start[row + (unsigned)x0]), fe = __ldg(&start[row + (unsigned)x1 + 1u]);
+            unsigned b = fb, e = fe;
+            if (prune) {
+                const float r2 = hm2 - (dy * dy + dz * dz);
+                if (r2 <= 0.f) {
+                    e = fb;   // out of reach
+                } else {
+                    if (x0 < cx && ax_lo > 0.f && ax_lo * ax_lo >= r2) b = __ldg(&start[row + (unsigned)cx]);
+                    if (x1 > cx && ax_hi > 0.f && ax_hi * ax_hi >= r2) e = __ldg(&start[row + (unsigned)cx + 1u]);
+                    if (e < b) e = b;
+                }
+            }
+            f((z - cz + 1) * 3 + (y - cy + 1), b, e, fe - fb);
+        }
+    }
+}
+
 // Number of candidates in the 27 cells of cell c.
 __device__ __forceinline__ unsigned candidate_count(const GridDev &g, const unsigned *__restrict__ start,
                                                     unsigned c) {

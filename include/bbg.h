@@ -467,14 +467,17 @@ bbg_status bbg_marching_cubes(bbg_solver s, const bbg_sdf_grid *grid, const floa
 
 /* ----- launch tuning ------------------------------------------------------------ */
 /* Block size of the neighbour passes (each block walks one tile of consecutive cell-
- * sorted particles) and how many members' records a thread requests together in the
- * non-pressure, predicted-density and pressure-force passes.  Results do not depend on
- * them; bubbles_gb300.autotune measures and picks them. */
+ * sorted particles), how many members' records a thread requests together in the
+ * non-pressure, predicted-density and pressure-force passes, and whether the density pass
+ * leaves out the neighbour cells (and rows of cells) a particle's sphere cannot reach.
+ * Results do not depend on them (bit for bit); bubbles_gb300.autotune measures and picks
+ * them. */
 typedef struct {
     int block_size;      /* 64, 128 (default) or 256 */
     int batch_np;        /* 2, 4 (default) or 8 */
     int batch_pd;
     int batch_pf;
+    int prune;           /* 1 (default) or 0 */
 } bbg_tuning;
 bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t);
 bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t);

@@ -20,8 +20,10 @@ oracle (the reference CPU path restated, all host threads) -- pass by pass:
   - predictions, accumulation and integration with colliders: bit-exact from identical
     inputs;
   - a whole tolerance-mode substep (src/equations/pcisph_equations3.cpp:218-256): the
-    same number of corrector iterations and positions within 1e-5 x spacing or 2 ulps of
-    the coordinate, whichever is larger (an FP32 coordinate cannot be closer than its ulp).
+    same number of corrector iterations and positions within 1e-5 x spacing or 8 ulps of
+    the coordinate, whichever is larger (an FP32 coordinate cannot be closer than its ulp;
+    the integration x + dt (v + dt F / m) and the collision projections each round on the
+    coordinate's scale -- the report gives the worst particle in ulps).
 
 Every case prints the per-particle relative error percentiles (p50, p99, max), and
 appends them as one JSON line to $BBG_PARITY_REPORT when that is set.
@@ -227,7 +229,9 @@ def test_substep_parity_full_size(gpu, name, seed, substeps):
     pg3, vg3 = g.download()
     po3 = o.get(O.POSITION)
     dxyz = np.abs(pg3.astype(np.float64) - po3)
-    allowed = np.maximum(RTOL * h0, 2.0 * np.spacing(np.abs(po3).astype(np.float32)).astype(np.float64))
+    ulp = np.spacing(np.abs(po3).astype(np.float32)).astype(np.float64)
+    allowed = np.maximum(RTOL * h0, 8.0 * ulp)
+    rep["substep"]["position_err_max_ulps"] = float((dxyz / ulp).max())
     dx = np.linalg.norm(pg3 - po3, axis=1) / h0
     rep["substep"]["position_err_over_spacing"] = percentiles(dx)
     rep["substep"]["position_err_over_allowed"] = percentiles((dxyz / allowed).max(axis=1))
