@@ -16,6 +16,8 @@ its warm-start MLP online on their (features, converged pressure) pairs.  After
              velocities (and the carried pressure for warm starts) from pinned memory,
              one substep, download them, every step
   roofline   dominant kernel: algorithmic bytes per launch / its average duration
+  kernel_bounds  every neighbour pass against its HBM bound and its issue-rate bound
+             (warp instructions from the committed ncu summary / duration / issue slots)
   cpu_baseline  the CPU oracle (restatement of the reference's CPU path) on the box's
              host cores, on a bounded sample of the same workload
   config.plain_same_window  the plain (zero-start) corrector timed on the same substeps
@@ -72,15 +74,39 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(workload_key):
-    """Per-particle DRAM bytes per launch from the committed ncu summary (or None)."""
+def load_profile_figures(workload_key, tag):
+    """Per-particle figures of each kernel from the committed ncu summary: lines
+    `<tag>: <kernel> <value>` (DRAM bytes per launch, warp instructions per launch)."""
     path = os.path.join(ROOT, "profiles", "%s_ncu.md" % workload_key)
     out = {}
     if os.path.exists(path):
         for line in open(path):
             parts = line.split()
-            if len(parts) == 3 and parts[0] == "traffic_bytes_per_particle:":
+            if len(parts) == 3 and parts[0] == tag + ":":
                 out[parts[1]] = float(parts[2])
+    return out
+
+
+def load_traffic(workload_key):
+    """Per-particle DRAM bytes per launch from the committed ncu summary."""
+    return load_profile_figures(workload_key, "traffic_bytes_per_particle")
+
+
+def kernel_bounds(prof, table, n, peak, inst_table, sm_count, sm_mhz):
+    """Each neighbour pass against both of its bounds: algorithmic HBM bytes / duration as a
+    fraction of the measured copy bandwidth, and warp instructions (ncu count per particle,
+    scaled to the launch) / duration as a fraction of the SMs' issue rate (4 schedulers per
+    SM, one warp instruction each per cycle, at the median SM clock sampled under load)."""
+    out = {}
+    for k, (ms, cnt) in prof.items():
+        if k not in table or cnt == 0:
+            continue
+        avg_s = ms / cnt / 1e3
+        e = {"avg_launch_us": avg_s * 1e6, "hbm_frac": table[k] * n / avg_s / 1e9 / peak}
+        if k in inst_table and sm_mhz:
+            e["issue_frac"] = inst_table[k] * n / avg_s / (sm_count * 4 * sm_mhz * 1e6)
+        e["bound"] = "issue" if e.get("issue_frac", 0.0) > e["hbm_frac"] else "hbm"
+        out[k] = e
     return out
 
 
@@ -914,6 +940,7 @@ def run_ours(args, scene, pos):
     if plain is not None:
         plain["iterations_per_sample"] = [int(x) for x in pln.iters]
         config["plain_same_window"] = plain
+    clocks = sampler.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
@@ -931,8 +958,12 @@ def run_ours(args, scene, pos):
         "roofline": roof,
         "cpu_baseline": cpu,
         "gpu_launches": launches_timed,
-        "clocks": sampler.summary(),
+        "clocks": clocks,
         "kernels": per_kernel,
+        "kernel_bounds": kernel_bounds(prof, table, n, peak,
+                                       load_profile_figures(args.config, "warp_instructions_per_particle"),
+                                       torch.cuda.get_device_properties(local).multi_processor_count,
+                                       clocks.get("sm_mhz")),
     }
     if plain is not None:
         line.update({"plain_value": plain["value"], "speedup_vs_plain": value / plain["value"],

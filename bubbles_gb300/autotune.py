@@ -9,6 +9,10 @@ same substeps (replayed as CUDA graphs from that state) for candidate settings:
     non-pressure, predicted-density and pressure-force passes: 2, 4, 8;
   * whether the density pass leaves out the neighbour cells and rows each particle's
     sphere cannot reach (bitwise the same results): 0, 1;
+  * particles per thread of the predicted-density and pressure-force passes: 1, 2;
+  * for batches, how the corrector passes cover the scenes: one block per tile of every
+    scene (0), one block per tile of the scenes still iterating, from a work list rebuilt
+    every iteration (1), or persistent blocks over that work list (2);
   * for batches only, the grid cell as a multiple of the particle spacing: 2 (the kernel
     radius), 2.5, 3 -- any cell at least the kernel radius keeps every neighbour inside
     the 27 cells, and a batch has no reference grid to match.  A single scene keeps the
@@ -33,6 +37,8 @@ TUNED_DIR = os.path.join(HERE, "tuned")
 BLOCKS = (64, 128, 256)
 BATCHES = (2, 4, 8)
 PRUNES = (0, 1)
+PPTS = (1, 2)
+WORKLISTS = (0, 1, 2)
 CELL_SCALES = (2.0, 2.5, 3.0)
 
 
@@ -85,8 +91,11 @@ def tune_launches(g, dt, snap, steps, warm, log):
     best = dict(g.tuning())
     best_t = time_substeps(g, dt, snap, steps, warm)
     log.append({"tuning": dict(best), "seconds": best_t})
-    for key, values in (("block_size", BLOCKS), ("prune", PRUNES), ("batch_pf", BATCHES),
-                        ("batch_pd", BATCHES), ("batch_np", BATCHES)):
+    knobs = [("block_size", BLOCKS), ("prune", PRUNES), ("batch_pf", BATCHES), ("batch_pd", BATCHES),
+             ("batch_np", BATCHES), ("particles_per_thread", PPTS)]
+    if isinstance(g, BatchSolver):
+        knobs.append(("batch_worklist", WORKLISTS))
+    for key, values in knobs:
         for v in values:
             if v == best[key]:
                 continue

@@ -112,6 +112,7 @@ struct bbg_solver_s {
     ShapeDev *d_box = nullptr;
     SceneState *d_sst = nullptr;
     unsigned short *d_scene = nullptr;
+    int *d_wl = nullptr;   // batch work list: scene first / last slots, segment offsets and tiles, counters
     FrameBufs frame;             // particle-frame writer buffers (allocated on first use)
     FrameReadBufs fread;         // frame reader buffers (grown on use)
     EmitBufs emit;               // emitter buffers (grown on use)
@@ -276,13 +277,14 @@ bbg_status free_all(bbg_solver s) {
     free_frame(s);
     if (s->d_stage2) cudaFree(s->d_stage2);
     s->d_stage2 = nullptr;
-    void *batch[] = {s->d_zb, s->d_box, s->d_sst, s->d_scene};
+    void *batch[] = {s->d_zb, s->d_box, s->d_sst, s->d_scene, s->d_wl};
     for (void *p : batch)
         if (p) cudaFree(p);
     s->d_zb = nullptr;
     s->d_box = nullptr;
     s->d_sst = nullptr;
     s->d_scene = nullptr;
+    s->d_wl = nullptr;
     DevBufs &B = s->B;
     void *ptrs[] = {B.pos[0], B.pos[1], B.vel[0], B.vel[1], B.pid[0], B.pid[1], B.slot, B.force,
                     B.xstar, B.pforce, B.smoothed, B.rho, B.press, B.rhostar, B.derr, B.cell,
@@ -1794,6 +1796,9 @@ bbg_status bbg_batch_create(const bbg_solver_desc *desc, const bbg_scene_desc *s
     if (!r) r = dalloc(&s->d_box, (size_t)count);
     if (!r) r = dalloc(&s->d_sst, (size_t)count);
     if (!r) r = dalloc(&s->d_scene, (size_t)total);
+    if (!r) r = dalloc(&s->d_wl, 4 * (size_t)count + 3);
+    if (!r && cudaMemset(s->d_wl, 0, sizeof(int) * (4 * (size_t)count + 3)) != cudaSuccess)
+        r = fail(BBG_ERR_CUDA, "batch upload failed");
     if (!r && cudaMemcpy(s->d_zb, zb.data(), sizeof(float) * count, cudaMemcpyHostToDevice) != cudaSuccess)
         r = fail(BBG_ERR_CUDA, "batch upload failed");
     if (!r && cudaMemcpy(s->d_box, boxes.data(), sizeof(ShapeDev) * count, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -1809,6 +1814,12 @@ bbg_status bbg_batch_create(const bbg_solver_desc *desc, const bbg_scene_desc *s
     s->P.scene_box = s->d_box;
     s->P.scene_st = s->d_sst;
     s->P.scene = s->d_scene;
+    s->P.scene_first = s->d_wl;
+    s->P.scene_last = s->d_wl + count;
+    s->P.wl_off = s->d_wl + 2 * (size_t)count;        // count + 1 entries
+    s->P.wl_tile = s->d_wl + 3 * (size_t)count + 1;
+    s->P.wl_ctr = s->d_wl + 4 * (size_t)count + 1;    // 2 entries
+    update_worklist_grid(s->B);
     s->epoch++;
     *out = s;
     return BBG_OK;
@@ -1900,6 +1911,8 @@ bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t) {
     t->batch_pd = s->B.tune.batch_pd;
     t->batch_pf = s->B.tune.batch_pf;
     t->prune = s->B.tune.prune;
+    t->particles_per_thread = s->B.tune.ppt;
+    t->batch_worklist = s->B.tune.worklist;
     return BBG_OK;
 }
 
@@ -1911,12 +1924,19 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
     for (int b : {t->batch_np, t->batch_pd, t->batch_pf})
         if (b != 2 && b != 4 && b != 8) return fail(BBG_ERR_INVALID_ARGUMENT, "gather batches must be 2, 4 or 8");
     if (t->prune != 0 && t->prune != 1) return fail(BBG_ERR_INVALID_ARGUMENT, "prune must be 0 or 1");
+    if (t->particles_per_thread != 1 && t->particles_per_thread != 2)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "particles_per_thread must be 1 or 2");
+    if (t->batch_worklist < 0 || t->batch_worklist > 2)
+        return fail(BBG_ERR_INVALID_ARGUMENT, "batch_worklist must be 0, 1 or 2");
     CK(cudaStreamSynchronize(s->stream));
     s->B.tune.block = t->block_size;
     s->B.tune.batch_np = t->batch_np;
     s->B.tune.batch_pd = t->batch_pd;
     s->B.tune.batch_pf = t->batch_pf;
     s->B.tune.prune = t->prune;
+    s->B.tune.ppt = t->particles_per_thread;
+    s->B.tune.worklist = t->batch_worklist;
+    if (s->nscenes > 0) update_worklist_grid(s->B);
     s->epoch++;   // captured graphs hold the old launch shapes
     return BBG_OK;
 }

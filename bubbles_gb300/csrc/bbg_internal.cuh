@@ -88,6 +88,12 @@ struct Params {
     const ShapeDev *scene_box;      // container box of each scene
     SceneState *scene_st;           // per-scene corrector state (reset each substep)
     unsigned short *scene;          // scene of each sorted slot (density pass)
+    // batch corrector work list: the tiles that hold particles of scenes whose corrector
+    // still runs, rebuilt before every iteration and taken by persistent blocks
+    int *scene_first, *scene_last;  // lowest / highest sorted slot of each scene
+    int *wl_off;                    // nscenes + 1 offsets of the scenes' tile segments
+    int *wl_tile;                   // first tile of each scene's segment
+    int *wl_ctr;                    // next work item of the two persistent passes
     int has_sdf;                    // some collider has a signed-distance field
     SdfDev sdf[kMaxSdf];
 };
@@ -594,6 +600,11 @@ __device__ __forceinline__ void predict_particle(const Params &P, float dt, floa
 __device__ __forceinline__ unsigned warp_max_u(unsigned v) { return __reduce_max_sync(0xffffffffu, v); }
 
 __device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }

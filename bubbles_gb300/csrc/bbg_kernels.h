@@ -14,7 +14,11 @@ struct Tuning {
     int batch_np = 4;      // non-pressure pass (two records per member)
     int batch_pd = 4;      // predicted-density pass
     int batch_pf = 4;      // pressure-force pass
-    int prune = 1;         // density pass: walk only the cells each particle's sphere reaches
+    int prune = 0;         // density pass: walk only the cells each particle's sphere reaches (1)
+    int ppt = 1;           // particles per thread of the predicted-density and pressure-force passes (1, 2)
+    int worklist = 1;      // batch corrector: 0 all tiles, 1 a block per listed tile, 2 persistent blocks
+    int wl_grid_pd = 0;    // batch: resident blocks of the persistent predicted-density and
+    int wl_grid_pf = 0;    // pressure-force passes for this shape (update_worklist_grid)
 };
 
 // Device buffers of one solver (all sized for `capacity` particles / grid cells).
@@ -88,6 +92,9 @@ void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_fir
                           float dt_over_m, cudaStream_t s);
 void launch_pack_acoef(const Params &P, const DevBufs &B, int buf, cudaStream_t s);
 // clamp_total: warm-started corrector (the total pressure, not the increment, is clamped)
+// batch: resident blocks of the persistent corrector passes for B.tune's launch shape
+// (set outside stream capture: creation and bbg_set_tuning)
+void update_worklist_grid(DevBufs &B);
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
                          cudaStream_t s, int clamp_total = 0);
 // mode 0: pressure force, then the next prediction or (converged) integration;

@@ -18,6 +18,8 @@
 // The iteration decision is read from device memory (max error of each iteration), so
 // the host launches max_iterations x 2 kernels without synchronising; kernels of
 // iterations after convergence return immediately.
+#include <climits>
+
 #include "bbg_kernels.h"
 #include "tile.cuh"
 
@@ -442,25 +444,20 @@ __global__ void k_pack_acoef(int n, float4 *pos, const float *__restrict__ press
     reinterpret_cast<float *>(&pos[i])[3] = press[i] / (d * d);
 }
 
-// PredictPressureFor (pcisph_equations3.cpp:60-90) over the step-start neighbour set at
-// predicted positions, with the density error stored (tolerance mode) and reduced to
-// max |err| and sum |err| for iteration k; also p / rho*^2 for the pressure force.
+// PredictPressureFor (pcisph_equations3.cpp:60-90) of particle i over the step-start
+// neighbour set at predicted positions, with the density error stored (tolerance mode);
+// also p / rho*^2 for the pressure force.  Returns |err| (0 for a particle not updated)
+// and, in a batch, its scene (-2 once that scene met the tolerance before iteration k).
 template <int NB>
-__global__ void __launch_bounds__(kMaxTile, kPdMinBlocks)
-k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
-               const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-               const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
-               float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
-               float delta, int clamp_total) {
-    // k < 0: iteration index from the device counter (the graph's WHILE loop only runs
-    // unconverged iterations); k >= 0: host-launched sequence, skip after convergence.
-    if (k < 0) k = st->iter;
-    else if (converged_before(P, st, k)) return;
-    __shared__ TileMap T;
-    tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ float pred_density_one(const Params &P, float4 *pos, const float4 *__restrict__ xstar,
+                                                  const unsigned *__restrict__ cell,
+                                                  const unsigned *__restrict__ start, const TileMap &T,
+                                                  const ListEntry *__restrict__ list,
+                                                  const int *__restrict__ nbr, float *__restrict__ press,
+                                                  float *__restrict__ rhostar, float *__restrict__ derr, int k,
+                                                  float delta, int clamp_total, int i, int &sc) {
     float aerr = 0.f;
-    int sc = -1;   // batch: scene of particle i while its corrector still runs
+    sc = -1;   // batch: scene of particle i while its corrector still runs
     if (i < P.n && P.nscenes > 0) {
         sc = P.scene[i];
         if (scene_converged_before(P, sc, k)) sc = -2;
@@ -468,7 +465,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
     if (i < P.n && sc != -2) {
         const float4 xi = xstar[i];
         float sum = 1.f;   // the particle itself: W_std(0) / (315 / (64 pi h^3))
-        tile_members<NB>(
+        tile_members<NB, true>(
             P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&xstar[j]); },
             [&](const float4 xj) {
                 const float r2 = dist2(xi, xj);
@@ -500,11 +497,35 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
         reinterpret_cast<float *>(&pos[i])[3] = p / (density * density);   // pos.w = p / rho*^2
         aerr = fabsf(err);
     }
-    // block reduction: max |err| (exact as bits of non-negative floats), sum |err| in FP64
+    return aerr;
+}
+
+// Per-scene maximum and sum of |err| of one warp's particles (lanes grouped by scene: one
+// group per warp except at the boundaries between scenes).  All lanes call it.  Sums: FP32
+// over the 32 lanes, FP64 from there on.
+__device__ __forceinline__ void scene_error_reduce(const Params &P, int sc, float aerr, int k) {
+    const int lane = threadIdx.x & 31;
+    const double s = (double)warp_sum_f(aerr);
+    const unsigned grp = __match_any_sync(0xffffffffu, sc);
+    const unsigned gm = __reduce_max_sync(grp, __float_as_uint(aerr));
+    if (sc >= 0) {
+        if ((__ffs(grp) - 1) == lane && gm) atomicMax(&P.scene_st[sc].err_bits[k], gm);
+        if (grp == 0xffffffffu) {
+            if (lane == 0) atomicAdd(&P.scene_st[sc].err_sum[k], s);
+        } else {
+            atomicAdd(&P.scene_st[sc].err_sum[k], (double)aerr);
+        }
+    }
+}
+
+// Block reduction of max |err| (exact as bits of non-negative floats) and sum |err| into
+// iteration k's totals: FP32 within a warp (at most 32 x particles-per-thread terms), FP64
+// across warps and blocks.  All threads call it.
+__device__ __forceinline__ void error_reduce(StepState *st, float amax, float asum, int k) {
     __shared__ unsigned smax[kMaxTile / 32];
     __shared__ double ssum[kMaxTile / 32];
-    const unsigned m = warp_max_u(__float_as_uint(aerr));
-    const double s = warp_sum_d((double)aerr);
+    const unsigned m = warp_max_u(__float_as_uint(amax));
+    const double s = (double)warp_sum_f(asum);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) { smax[wid] = m; ssum[wid] = s; }
     __syncthreads();
@@ -515,42 +536,128 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
         if (bm) atomicMax(&st->err_bits[k], bm);
         atomicAdd(&st->err_sum[k], bs);
     }
-    if (P.nscenes > 0) {
-        // per-scene maxima: lanes grouped by scene (one group per warp except at the
-        // boundaries between scenes)
-        const unsigned grp = __match_any_sync(0xffffffffu, sc);
-        const unsigned gm = __reduce_max_sync(grp, __float_as_uint(aerr));
-        if (sc >= 0) {
-            if ((__ffs(grp) - 1) == lane && gm) atomicMax(&P.scene_st[sc].err_bits[k], gm);
-            if (grp == 0xffffffffu) {
-                if (lane == 0) atomicAdd(&P.scene_st[sc].err_sum[k], s);
-            } else {
-                atomicAdd(&P.scene_st[sc].err_sum[k], (double)aerr);
-            }
-        }
-    }
 }
 
-// PredictPressureForceFor (pcisph_equations3.cpp:114-155) at the current positions,
-// then either the next prediction or AccumulateForcesFor + TimeIntegrationFor.
-template <int NB>
-__global__ void __launch_bounds__(kMaxTile, kPfMinBlocks)
-k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-                 const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
-                 const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
-                 float4 *__restrict__ pforce,
-                 float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
-                 float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
-                 float dt_over_m, int mode) {
-    if (k < 0) k = st->iter;
-    else if (converged_before(P, st, k)) return;
-    bool last = mode == 0 && ((k == max_it - 1) ||
-                fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
+// k < 0: iteration index from the device counter (the graph's WHILE loop only runs
+// unconverged iterations); k >= 0: host-launched sequence, skip after convergence.
+__device__ __forceinline__ bool corrector_iteration(const Params &P, const StepState *st, int &k) {
+    if (k < 0) {
+        k = st->iter;
+        return true;
+    }
+    return !converged_before(P, st, k);
+}
+
+// Work item w of the batch's list: the tile (segment of the scene found by binary search
+// over the segment offsets).
+__device__ __forceinline__ int worklist_tile(const Params &P, int w) {
+    int lo = 0, hi = P.nscenes;   // wl_off[lo] <= w < wl_off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&P.wl_off[mid]) <= w) lo = mid;
+        else hi = mid;
+    }
+    return __ldg(&P.wl_tile[lo]) + (w - __ldg(&P.wl_off[lo]));
+}
+
+// Number of work items, at most the number of tiles (of `slots` slots).
+__device__ __forceinline__ int worklist_total(const Params &P, int slots) {
+    const int tiles = (P.n + slots - 1) / slots;
+    const int total = __ldg(&P.wl_off[P.nscenes]);
+    return total < tiles ? total : tiles;
+}
+
+// Next work item of a persistent block (counter c; two shared slots alternate so that one
+// barrier per item keeps the slot being read apart from the one being written).
+__device__ __forceinline__ int worklist_next(int *ctr, int *slot, int &parity) {
+    if (threadIdx.x == 0) slot[parity] = atomicAdd(ctr, 1);
+    __syncthreads();
+    const int w = slot[parity];
+    parity ^= 1;
+    return w;
+}
+
+// First slot of the block's tile of `slots` slots: the block's own, or with a batch work
+// list (wl) the tile of work item blockIdx.x; -1 for a block past the list's end.
+__device__ __forceinline__ int block_tile(const Params &P, int wl, int slots) {
+    if (!wl) return blockIdx.x * slots;
+    if ((int)blockIdx.x >= worklist_total(P, slots)) return -1;
+    return worklist_tile(P, blockIdx.x) * slots;
+}
+
+// One block per tile (all tiles, or the work list's) of PPT x blockDim slots; thread t
+// takes slots t, t + blockDim, ... (PPT particles per thread).
+template <int NB, int PPT>
+__global__ void __launch_bounds__(kMaxTile, kPdMinBlocks)
+k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
+               const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+               const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
+               float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
+               float delta, int clamp_total, int wl) {
+    if (!corrector_iteration(P, st, k)) return;
+    const int s0 = block_tile(P, wl, PPT * blockDim.x);
+    if (s0 < 0 || s0 >= P.n) return;
     __shared__ TileMap T;
-    tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned fbits = 0;
-    bool bad = false;   // integrated position or velocity not finite
+    float amax = 0.f, asum = 0.f;
+#pragma unroll 1
+    for (int u = 0; u < PPT; u++) {
+        const int su = s0 + u * blockDim.x;
+        tile_setup_at(P.g, cell, start, su < P.n ? su : s0, T);
+        int sc;
+        const float aerr = pred_density_one<NB>(P, pos, xstar, cell, start, T, list, nbr, press, rhostar, derr,
+                                                k, delta, clamp_total, su + threadIdx.x, sc);
+        amax = fmaxf(amax, aerr);
+        asum += aerr;
+        if (P.nscenes > 0) scene_error_reduce(P, sc, aerr, k);
+    }
+    error_reduce(st, amax, asum, k);
+}
+
+// Batch: persistent blocks over the work list of the tiles whose scenes still run
+// (launch_worklist), the same per-particle work as k_pred_density.
+template <int NB>
+__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
+k_pred_density_wl(Params P, float4 *pos, const float4 *__restrict__ xstar,
+                  const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+                  const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
+                  float *__restrict__ rhostar, float *__restrict__ derr, StepState *st, int k,
+                  float delta, int clamp_total) {
+    if (!corrector_iteration(P, st, k)) return;
+    __shared__ TileMap T;
+    __shared__ int slot[2];
+    int parity = 0;
+    const int total = worklist_total(P, blockDim.x);
+    float amax = 0.f, asum = 0.f;   // this thread's particles (a few tiles): FP32 partial sum
+    for (;;) {
+        const int w = worklist_next(&P.wl_ctr[0], slot, parity);
+        if (w >= total) break;
+        const int s0 = worklist_tile(P, w) * blockDim.x;
+        if (s0 < 0 || s0 >= P.n) continue;   // never for a list built by k_worklist
+        tile_setup_at(P.g, cell, start, s0, T);
+        int sc;
+        const float aerr = pred_density_one<NB>(P, pos, xstar, cell, start, T, list, nbr, press, rhostar, derr,
+                                                k, delta, clamp_total, s0 + threadIdx.x, sc);
+        amax = fmaxf(amax, aerr);
+        asum += aerr;
+        scene_error_reduce(P, sc, aerr, k);
+    }
+    error_reduce(st, amax, asum, k);
+}
+
+// PredictPressureForceFor (pcisph_equations3.cpp:114-155) of particle i at the current
+// positions, then either the next prediction or AccumulateForcesFor + TimeIntegrationFor.
+// `last`: iteration k ends the corrector (single scene); batches decide per scene.
+template <int NB>
+__device__ __forceinline__ void pressure_force_one(const Params &P, const float4 *__restrict__ pos,
+                                                   const float4 *__restrict__ vel,
+                                                   const unsigned *__restrict__ cell,
+                                                   const unsigned *__restrict__ start, const TileMap &T,
+                                                   const ListEntry *__restrict__ list,
+                                                   const int *__restrict__ nbr, float4 *__restrict__ force,
+                                                   float4 *__restrict__ pforce, float4 *__restrict__ xstar,
+                                                   float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                                                   int k, int max_it, float dt, float dt_over_m, int mode,
+                                                   bool last, int i, unsigned &fbits, bool &bad) {
     bool active = i < P.n;
     if (active && P.nscenes > 0) {
         // batch: each scene stops at its own convergence
@@ -559,47 +666,190 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
         last = mode == 0 && ((k == max_it - 1) ||
                              fdv(__uint_as_float(P.scene_st[sc].err_bits[k]), P.target_density) < P.max_err_ratio);
     }
-    if (active) {
-        const float4 pi = pos[i];
-        const float ai = pi.w;   // p_i / rho*_i^2
-        float tx = 0.f, ty = 0.f, tz = 0.f;
-        const float kg = P.m2 * P.spiky_dw_c;
-        tile_members<NB>(
-            P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&pos[j]); },
-            [&](const float4 pj) {   // pj.w = p_j / rho*_j^2
-                const float r2 = dist2(pi, pj);
-                const float inv_d = rsqrtf(r2);
-                const float d = r2 > 0.f ? r2 * inv_d : 0.f;   // coincident particles: distance 0
-                // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
-                if (d - P.h <= -P.iz && d >= P.iz) {
-                    const float x = 1.f - d * P.inv_h;
-                    const float c = kg * (ai + pj.w) * x * x * inv_d;
-                    tx += (pj.x - pi.x) * c;
-                    ty += (pj.y - pi.y) * c;
-                    tz += (pj.z - pi.z) * c;
-                }
-            });
-        const v3 fp = V(-tx, -ty, -tz);
-        pforce[i] = F4(fp);
-        const v3 f = V(force[i]);
-        if (last) {
-            const v3 ft = vadd(f, fp);
-            force[i] = F4(ft);
-            v3 x = V(pi), v = V(vel[i]);
-            integrate_particle(P, dt, ft, &x, &v);
-            pos_out[i] = F4(x);
-            vel_out[i] = F4(v);
-            fbits = __float_as_uint(vlen(ft));
-            bad = !finite_state(x, v);
-        } else if (mode != 1) {
-            v3 xs;
-            predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
-            xstar[i] = F4(xs);
-        }
+    if (!active) return;
+    const float4 pi = pos[i];
+    const float ai = pi.w;   // p_i / rho*_i^2
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+    const float kg = P.m2 * P.spiky_dw_c;
+    tile_members<NB>(
+        P, start, T, list, nbr, pos, cell[i], i, [&](unsigned j) { return __ldg(&pos[j]); },
+        [&](const float4 pj) {   // pj.w = p_j / rho*_j^2
+            const float r2 = dist2(pi, pj);
+            const float inv_d = rsqrtf(r2);
+            const float d = r2 > 0.f ? r2 * inv_d : 0.f;   // coincident particles: distance 0
+            // IsWithinSpiky(d, h) and d > 0 && !IsZero(d)
+            if (d - P.h <= -P.iz && d >= P.iz) {
+                const float x = 1.f - d * P.inv_h;
+                const float c = kg * (ai + pj.w) * x * x * inv_d;
+                tx += (pj.x - pi.x) * c;
+                ty += (pj.y - pi.y) * c;
+                tz += (pj.z - pi.z) * c;
+            }
+        });
+    const v3 fp = V(-tx, -ty, -tz);
+    pforce[i] = F4(fp);
+    const v3 f = V(force[i]);
+    if (last) {
+        const v3 ft = vadd(f, fp);
+        force[i] = F4(ft);
+        v3 x = V(pi), v = V(vel[i]);
+        integrate_particle(P, dt, ft, &x, &v);
+        pos_out[i] = F4(x);
+        vel_out[i] = F4(v);
+        fbits = max(fbits, __float_as_uint(vlen(ft)));
+        bad = bad || !finite_state(x, v);
+    } else if (mode != 1) {
+        v3 xs;
+        predict_particle(P, dt, dt_over_m, f, fp, V(pi), V(vel[i]), &xs);
+        xstar[i] = F4(xs);
+    }
+}
+
+__device__ __forceinline__ bool corrector_ends(const Params &P, const StepState *st, int k, int max_it, int mode) {
+    return mode == 0 && ((k == max_it - 1) ||
+                         fdv(__uint_as_float(st->err_bits[k]), P.target_density) < P.max_err_ratio);
+}
+
+template <int NB, int PPT>
+__global__ void __launch_bounds__(kMaxTile, kPfMinBlocks)
+k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                 const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+                 const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+                 float4 *__restrict__ pforce,
+                 float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
+                 float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt,
+                 float dt_over_m, int mode, int wl) {
+    if (!corrector_iteration(P, st, k)) return;
+    const bool last = corrector_ends(P, st, k, max_it, mode);
+    const int s0 = block_tile(P, wl, PPT * blockDim.x);
+    if (s0 < 0 || s0 >= P.n) return;
+    __shared__ TileMap T;
+    unsigned fbits = 0;
+    bool bad = false;   // integrated position or velocity not finite
+#pragma unroll 1
+    for (int u = 0; u < PPT; u++) {
+        const int su = s0 + u * blockDim.x;
+        tile_setup_at(P.g, cell, start, su < P.n ? su : s0, T);
+        pressure_force_one<NB>(P, pos, vel, cell, start, T, list, nbr, force, pforce, xstar, pos_out, vel_out,
+                               k, max_it, dt, dt_over_m, mode, last, su + threadIdx.x, fbits, bad);
     }
     fbits = warp_max_u(fbits);
     if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
     count_nonfinite(bad, st);
+}
+
+// Batch: persistent blocks over the same work list as k_pred_density_wl.
+template <int NB>
+__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
+k_pressure_force_wl(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                    const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
+                    const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
+                    float4 *__restrict__ pforce, float4 *__restrict__ xstar, float4 *__restrict__ pos_out,
+                    float4 *__restrict__ vel_out, StepState *st, int k, int max_it, float dt, float dt_over_m,
+                    int mode) {
+    if (!corrector_iteration(P, st, k)) return;
+    __shared__ TileMap T;
+    __shared__ int slot[2];
+    int parity = 0;
+    const int total = worklist_total(P, blockDim.x);
+    unsigned fbits = 0;
+    bool bad = false;
+    for (;;) {
+        const int w = worklist_next(&P.wl_ctr[1], slot, parity);
+        if (w >= total) break;
+        const int s0 = worklist_tile(P, w) * blockDim.x;
+        if (s0 < 0 || s0 >= P.n) continue;   // never for a list built by k_worklist
+        tile_setup_at(P.g, cell, start, s0, T);
+        pressure_force_one<NB>(P, pos, vel, cell, start, T, list, nbr, force, pforce, xstar, pos_out, vel_out, k,
+                               max_it, dt, dt_over_m, mode, false, s0 + threadIdx.x, fbits, bad);
+    }
+    fbits = warp_max_u(fbits);
+    if ((threadIdx.x & 31) == 0 && fbits) atomicMax(&st->max_force_bits, fbits);
+    count_nonfinite(bad, st);
+}
+
+// Batch: first and last sorted slot of every scene (both arrays preset to 0x7f7f7f7f / -1).
+// The layout keeps each scene's slots contiguous and the scenes in order (containers
+// stacked along z, the slowest axis of the cell order, two empty cells apart).
+__global__ void __launch_bounds__(kThreads)
+k_scene_slots(Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int s = P.scene[i];
+    if (i == 0 || P.scene[i - 1] != s) atomicMin(&P.scene_first[s], i);
+    if (i == P.n - 1 || P.scene[i + 1] != s) atomicMax(&P.scene_last[s], i);
+}
+
+// Exclusive block scan (sum, or max with identity INT_MIN) of one int per thread; *total
+// gets the whole block's result.  All threads call it; sh holds 32 ints.
+template <bool MAX>
+__device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    const int id = MAX ? INT_MIN : 0;
+    auto op = [](int a, int b) { return MAX ? (a > b ? a : b) : a + b; };
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = op(x, y);
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < nw ? sh[lane] : id;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t = op(t, y);
+        }
+        sh[lane] = t;
+    }
+    __syncthreads();
+    const int before = __shfl_up_sync(0xffffffffu, x, 1);
+    const int r = op(wid > 0 ? sh[wid - 1] : id, lane > 0 ? before : id);
+    *total = sh[nw - 1];
+    __syncthreads();
+    return r;
+}
+
+// Batch work list of corrector iteration k (k < 0: the device counter): for every scene
+// whose corrector still runs, the segment of tiles (of `tile` slots) holding its slots,
+// without the tiles an earlier segment already holds; a scene that met the tolerance gets
+// an empty segment.  Resets the persistent passes' counters.  One block.
+__global__ void __launch_bounds__(1024)
+k_worklist(Params P, const StepState *st, int k, int tile) {
+    __shared__ int sh[32];
+    if (k < 0) k = st->iter;
+    int carry_tile = -1;   // last tile of the segments so far
+    int carry_off = 0;     // work items so far
+    for (int c = 0; c < P.nscenes; c += blockDim.x) {
+        const int s = c + threadIdx.x;
+        int ta = 0, tb = -1;
+        if (s < P.nscenes) {
+            const int f = P.scene_first[s], l = P.scene_last[s];
+            if (l >= f && l >= 0 && !scene_converged_before(P, s, k)) {
+                ta = f / tile;
+                tb = l / tile;
+            }
+        }
+        int chunk_max, chunk_sum;
+        const int before = block_scan_excl<true>(tb, sh, &chunk_max);
+        const int prev = max(carry_tile, before);
+        if (ta <= prev) ta = prev + 1;
+        const int len = tb >= ta ? tb - ta + 1 : 0;
+        const int off = block_scan_excl<false>(len, sh, &chunk_sum);
+        if (s < P.nscenes) {
+            P.wl_off[s] = carry_off + off;
+            P.wl_tile[s] = ta;
+        }
+        carry_tile = max(carry_tile, chunk_max);
+        carry_off += chunk_sum;
+    }
+    if (threadIdx.x == 0) {
+        P.wl_off[P.nscenes] = carry_off;
+        P.wl_ctr[0] = 0;
+        P.wl_ctr[1] = 0;
+    }
 }
 
 // End of one corrector iteration in the graph-driven loop: stop when the density error
@@ -796,6 +1046,12 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
         k_density<<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start, B.rho, B.inv_rho,
                                                    B.press, B.nbr, B.list, compute_pressure, B.st);
     }
+    if (P.nscenes > 0 && P.n > 0) {
+        // batch: each scene's slot range (the scene of every slot was set just above)
+        cudaMemsetAsync(P.scene_first, 0x7f, sizeof(int) * (size_t)P.nscenes, s);
+        cudaMemsetAsync(P.scene_last, 0xff, sizeof(int) * (size_t)P.nscenes, s);
+        k_scene_slots<<<blocks_for(P.n, kThreads), kThreads, 0, s>>>(P);
+    }
     BBG_PEND(B, s);
 }
 
@@ -837,20 +1093,75 @@ void launch_predict_first(const Params &P, const DevBufs &B, int buf, int is_fir
     BBG_PEND(B, s);
 }
 
+// Resident blocks of a persistent kernel: every SM filled to the kernel's occupancy.
+template <class K>
+static int persistent_blocks(K kernel, int threads) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+}
+
+template <int NB>
+static int pd_grid(int t) { return persistent_blocks(k_pred_density_wl<NB>, t); }
+template <int NB>
+static int pf_grid(int t) { return persistent_blocks(k_pressure_force_wl<NB>, t); }
+
+void update_worklist_grid(DevBufs &B) {
+    const int t = B.tune.block;
+    B.tune.wl_grid_pd = B.tune.batch_pd == 2 ? pd_grid<2>(t) : B.tune.batch_pd == 8 ? pd_grid<8>(t) : pd_grid<4>(t);
+    B.tune.wl_grid_pf = B.tune.batch_pf == 2 ? pf_grid<2>(t) : B.tune.batch_pf == 8 ? pf_grid<8>(t) : pf_grid<4>(t);
+}
+
+// Particles per thread of the per-tile corrector passes (1 with tile-relative lists,
+// whose entries are decoded against the block's own tile).
+static int corrector_ppt(const DevBufs &B) { return kListRelative ? 1 : (B.tune.ppt == 2 ? 2 : 1); }
+
+// Slots per tile of the corrector passes: the block, times the particles per thread for
+// the per-tile kernels.
+static int corrector_tile(const DevBufs &B) {
+    return B.tune.block * (B.tune.worklist == 2 ? 1 : corrector_ppt(B));
+}
+
+void launch_worklist(const Params &P, const DevBufs &B, int k, cudaStream_t s) {
+    k_worklist<<<1, 1024, 0, s>>>(P, B.st, k, corrector_tile(B));
+}
+
 void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, float delta,
                          cudaStream_t s, int clamp_total) {
     BBG_PBEGIN(B, KID_PRED_DENSITY, s, k);
     const int t = B.tune.block;
-#define PD_LAUNCH(NB)                                                                                  \
-    k_pred_density<NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.xstar, B.cell, B.start, B.list, \
-                                                        B.nbr, B.press, B.rhostar, B.derr, B.st, k, delta, \
-                                                        clamp_total)
-    switch (B.tune.batch_pd) {
-        case 2: PD_LAUNCH(2); break;
-        case 8: PD_LAUNCH(8); break;
-        default: PD_LAUNCH(4); break;
-    }
+    const int wl = P.nscenes > 0 ? B.tune.worklist : 0;
+    if (wl) launch_worklist(P, B, k, s);   // batch: the tiles of the scenes still running
+    if (wl == 2) {
+        // persistent blocks over the work list
+#define PD_LAUNCH(NB)                                                                               \
+    k_pred_density_wl<NB><<<B.tune.wl_grid_pd > 0 ? B.tune.wl_grid_pd : pd_grid<NB>(t), t, 0, s>>>(  \
+        P, B.pos[buf], B.xstar, B.cell, B.start, B.list, B.nbr, B.press, B.rhostar, B.derr, B.st, k, \
+        delta, clamp_total)
+        switch (B.tune.batch_pd) {
+            case 2: PD_LAUNCH(2); break;
+            case 8: PD_LAUNCH(8); break;
+            default: PD_LAUNCH(4); break;
+        }
 #undef PD_LAUNCH
+    } else {
+        const int ppt = corrector_ppt(B);
+#define PD_LAUNCH(NB, PPT)                                                                              \
+    k_pred_density<NB, PPT><<<blocks_for(P.n, t * PPT), t, 0, s>>>(P, B.pos[buf], B.xstar, B.cell, B.start, \
+                                                                   B.list, B.nbr, B.press, B.rhostar,      \
+                                                                   B.derr, B.st, k, delta, clamp_total, wl)
+        switch (B.tune.batch_pd * 10 + ppt) {
+            case 21: PD_LAUNCH(2, 1); break;
+            case 81: PD_LAUNCH(8, 1); break;
+            case 22: PD_LAUNCH(2, 2); break;
+            case 42: PD_LAUNCH(4, 2); break;
+            case 82: PD_LAUNCH(8, 2); break;
+            default: PD_LAUNCH(4, 1); break;
+        }
+#undef PD_LAUNCH
+    }
     BBG_PEND(B, s);
 }
 
@@ -867,17 +1178,37 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
                            float dt_over_m, cudaStream_t s, int mode) {
     BBG_PBEGIN(B, KID_PRESSURE_FORCE, s, k);
     const int t = B.tune.block;
-#define PF_LAUNCH(NB)                                                                                \
-    k_pressure_force<NB><<<blocks_for(P.n, t), t, 0, s>>>(P, B.pos[buf], B.vel[buf], B.cell, B.start,  \
-                                                          B.list, B.nbr, B.force, B.pforce, B.xstar,   \
-                                                          B.pos[1 - buf], B.vel[1 - buf], B.st, k,     \
-                                                          max_it, dt, dt_over_m, mode)
-    switch (B.tune.batch_pf) {
-        case 2: PF_LAUNCH(2); break;
-        case 8: PF_LAUNCH(8); break;
-        default: PF_LAUNCH(4); break;
-    }
+    const int wl = P.nscenes > 0 ? B.tune.worklist : 0;
+    // batch: the work list launch_pred_density built for iteration k (built here when the
+    // pass runs on its own)
+    if (wl && mode == 1) launch_worklist(P, B, k, s);
+    if (wl == 2) {
+#define PF_LAUNCH(NB)                                                                                   \
+    k_pressure_force_wl<NB><<<B.tune.wl_grid_pf > 0 ? B.tune.wl_grid_pf : pf_grid<NB>(t), t, 0, s>>>(    \
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,           \
+        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, mode)
+        switch (B.tune.batch_pf) {
+            case 2: PF_LAUNCH(2); break;
+            case 8: PF_LAUNCH(8); break;
+            default: PF_LAUNCH(4); break;
+        }
 #undef PF_LAUNCH
+    } else {
+        const int ppt = corrector_ppt(B);
+#define PF_LAUNCH(NB, PPT)                                                                             \
+    k_pressure_force<NB, PPT><<<blocks_for(P.n, t * PPT), t, 0, s>>>(                                   \
+        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,           \
+        B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, mode, wl)
+        switch (B.tune.batch_pf * 10 + ppt) {
+            case 21: PF_LAUNCH(2, 1); break;
+            case 81: PF_LAUNCH(8, 1); break;
+            case 22: PF_LAUNCH(2, 2); break;
+            case 42: PF_LAUNCH(4, 2); break;
+            case 82: PF_LAUNCH(8, 2); break;
+            default: PF_LAUNCH(4, 1); break;
+        }
+#undef PF_LAUNCH
+    }
     BBG_PEND(B, s);
 }
 

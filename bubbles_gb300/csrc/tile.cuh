@@ -57,13 +57,13 @@ __device__ __forceinline__ unsigned short list_code(unsigned j, unsigned base) {
 constexpr bool kListRelative = true;
 #endif
 
-// The tile's 9 range starts from the grid (all threads of the block must call it; a
-// no-op with absolute list entries).
-__device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
-                                           const unsigned *__restrict__ start, int n, TileMap &T) {
+// The 9 range starts of the tile whose first slot is s0, from the grid (all threads of the
+// block must call it; a no-op with absolute list entries).
+__device__ __forceinline__ void tile_setup_at(const GridDev &g, const unsigned *__restrict__ cell,
+                                              const unsigned *__restrict__ start, int s0, TileMap &T) {
     if (!kListRelative) return;
+    __syncthreads();   // a previous tile of the same block may still read T
     if (threadIdx.x < 9) {
-        const int s0 = blockIdx.x * blockDim.x;
         const int r = threadIdx.x;
         const long long plane = (long long)g.nx * g.ny;
         const long long off = (long long)(r % 3 - 1) * g.nx + (long long)(r / 3 - 1) * plane;
@@ -73,6 +73,13 @@ __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__r
         T.lo[r] = (int)__ldg(&start[c0]);
     }
     __syncthreads();
+}
+
+// The range starts of the block's own tile (slots blockIdx.x * blockDim.x on).
+__device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
+                                           const unsigned *__restrict__ start, int n, TileMap &T) {
+    (void)n;
+    tile_setup_at(g, cell, start, blockIdx.x * blockDim.x, T);
 }
 
 // The 9 row ranges of the 27 neighbour cells of cell c in z, y, x order: f(r, b, e) for
@@ -226,7 +233,7 @@ __device__ __forceinline__ void tile_candidates_coded(const GridDev &g, const un
 // records are requested before any is used (entries past the end fetch particle i
 // itself and are not used).  Wide particles re-test their candidates with the
 // exact membership test at the step-start positions pos0.
-template <int NB = kGatherBatch, class Fetch, class Use>
+template <int NB = kGatherBatch, bool SPLIT = false, class Fetch, class Use>
 __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__restrict__ start,
                                              const TileMap &T, const ListEntry *__restrict__ list,
                                              const int *__restrict__ nbr, const float4 *__restrict__ pos0,
@@ -243,12 +250,25 @@ __device__ __forceinline__ void tile_members(const Params &P, const unsigned *__
     }
     const int cnt = __ldg(&nbr[i]) - 1;   // members other than i
     const size_t n = (size_t)P.n;
-    const ListEntry *l = list + i;
-    for (int q = 0; q < cnt; q += NB) {
+    const ListEntry *l = list + i;        // entry q + k of the group at l + k * n
+    // SPLIT: whole groups without per-member predicates, then the partial group (a second
+    // copy of `use`: measured faster for the small predicted-density body only)
+    const int full = SPLIT ? cnt - cnt % NB : 0;
+    int q = 0;
+    for (; q < full; q += NB, l += NB * n) {
         unsigned j[NB];
 #pragma unroll
-        for (int k = 0; k < NB; k++)
-            j[k] = q + k < cnt ? list_slot(T, __ldg(&l[(size_t)(q + k) * n])) : (unsigned)i;
+        for (int k = 0; k < NB; k++) j[k] = list_slot(T, __ldg(l + k * n));
+        decltype(fetch(0u)) d[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) d[k] = fetch(j[k]);
+#pragma unroll
+        for (int k = 0; k < NB; k++) use(d[k]);
+    }
+    for (; q < cnt; q += NB, l += NB * n) {   // predicated groups (with SPLIT: the last one)
+        unsigned j[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) j[k] = q + k < cnt ? list_slot(T, __ldg(l + k * n)) : (unsigned)i;
         decltype(fetch(0u)) d[NB];
 #pragma unroll
         for (int k = 0; k < NB; k++) d[k] = fetch(j[k]);

@@ -477,7 +477,11 @@ typedef struct {
     int batch_np;        /* 2, 4 (default) or 8 */
     int batch_pd;
     int batch_pf;
-    int prune;           /* 1 (default) or 0 */
+    int prune;           /* 0 (default: measured faster on GB300) or 1 */
+    int particles_per_thread;  /* predicted-density and pressure-force passes: 1 (default) or 2 */
+    int batch_worklist;  /* batches: 0 one block per tile of every scene, 1 (default) one block
+                            per tile of the scenes whose corrector still runs (a work list
+                            rebuilt every iteration), 2 persistent blocks over that list */
 } bbg_tuning;
 bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t);
 bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t);

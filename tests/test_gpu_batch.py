@@ -85,6 +85,29 @@ def test_batch_scenes_converge_independently(gpu):
     g.close()
 
 
+@pytest.mark.parametrize("tuning", [dict(batch_worklist=0), dict(batch_worklist=1, particles_per_thread=2),
+                                    dict(batch_worklist=2, block_size=64)])
+def test_batch_work_lists_do_not_change_results(gpu, tuning):
+    """The corrector passes over every scene's tiles, over a work list of the tiles of the
+    scenes still iterating (one block per tile, or persistent blocks taking tiles from it):
+    bitwise the same substeps, per-scene iterations and errors as the default."""
+    sc, boxes, pos = small_batch()
+    ga = bb.BatchSolver(sc, boxes, pos)
+    gb = bb.BatchSolver(sc, boxes, pos)
+    gb.set_tuning(**tuning)
+    for _ in range(4):
+        ga.advance_time_step(sc["dt"])
+        gb.advance_time_step(sc["dt"])
+        ia, ea = ga.scene_stats()
+        ib, eb = gb.scene_stats()
+        assert np.array_equal(ia, ib) and np.array_equal(ea, eb)
+    pa, va = ga.download()
+    pb, vb = gb.download()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    ga.close()
+    gb.close()
+
+
 def test_batch_learned_warm_start_runs(gpu):
     sc, boxes, pos = small_batch()
     scl = dict(sc, pressure_init="learned", mlp={"train_substeps": 4, "batch": 1024})
@@ -96,44 +119,67 @@ def test_batch_learned_warm_start_runs(gpu):
     g.close()
 
 
+def packed_frame(sc, boxes):
+    """The batch's packed domain and each scene's container in it, by the layout rule of
+    bbg_batch_create: scenes stacked along z, each container's min corner on a cell
+    boundary, two empty cells between consecutive containers (the same double arithmetic)."""
+    import math
+    from bubbles_gb300.solver import desc_from_scene
+    d = desc_from_scene(dict(sc, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0)))
+    cell = d.target_spacing * d.grid_spacing_scale
+    xmax = ymax = z = 0.0
+    offsets, containers = [], []
+    for lo, hi in boxes:
+        ext = [float(b) - float(a) for a, b in zip(lo, hi)]
+        xmax, ymax = max(xmax, ext[0]), max(ymax, ext[1])
+        offsets.append((-float(lo[0]), -float(lo[1]), z - float(lo[2])))
+        containers.append({"type": "box", "size": tuple(ext), "reverse": True,
+                           "center": (0.5 * ext[0], 0.5 * ext[1], z + 0.5 * ext[2])})
+        z = math.ceil((z + ext[2]) / cell) * cell + 2.0 * cell
+    dmax = (math.ceil(xmax / cell) * cell, math.ceil(ymax / cell) * cell, z - 2.0 * cell)
+    return (0.0, 0.0, 0.0), dmax, np.asarray(offsets), containers
+
+
 def test_batched_64_scenes_against_oracle(gpu):
     """Config 4 (64 dam breaks of uneven sizes in one batch): after 30 substeps, one substep
     of four scenes -- the smallest, the largest and two from the middle -- against the FP32
-    oracle (the reference algorithm) run on each scene alone from the batch's state: the
-    same corrector iterations, the tolerance met, and positions within 16 ulps of the packed
-    coordinate plus 1e-5 x spacing.  The batch computes in the packed domain, where scenes
-    stacked along z sit at |z| up to ~12 (ulp ~1e-6); relative positions there carry that
-    absolute rounding, so a scene matches the same scene computed at its own origin only to
-    a few ulps of its packed coordinates."""
+    oracle (the reference algorithm) run on each scene alone in the batch's packed frame
+    (the packed domain's grid, the scene's container where the batch puts it, the scene's
+    particles at their packed coordinates): the same corrector iterations, the tolerance
+    met, the same maximum density error, and positions within 1e-5 x spacing or 8 ulps of
+    the coordinate, the bound of the single-scene parity tests.  The frame makes the
+    arithmetic the batch's own: scenes are independent, so each one is the reference step
+    of that scene alone."""
     import os
     from oracle import oracle as O
     sc, pos = scenes.config("batched_64", seed=0)
     boxes = sc["boxes"]
+    dmin, dmax, offsets, containers = packed_frame(sc, boxes)
     g = bb.BatchSolver(sc, boxes, pos)
+    assert np.array_equal(g.layout(), offsets)
     for _ in range(30):
         g.advance_time_step(sc["dt"])
-    ps, vs = g.download_scenes()
+    ps, vs = bb.Solver.download(g)          # packed coordinates, scene after scene
     g.advance_time_step(sc["dt"])
     its, errs = g.scene_stats()
-    nxt, _ = g.download_scenes()
-    off = g.layout()
+    nxt, _ = bb.Solver.download(g)
     g.close()
+    first = np.concatenate([[0], np.cumsum([len(p) for p in pos])])
     order = np.argsort([len(p) for p in pos])
     picks = [int(order[0]), int(order[-1]), int(order[len(order) // 2]), int(order[len(order) // 3])]
     threads = os.cpu_count() or 1
+    h0 = sc["spacing"]
     for k in picks:
-        lo, hi = boxes[k]
-        ext = tuple(float(b - a) for a, b in zip(lo, hi))
-        center = tuple(float(a + b) / 2 for a, b in zip(lo, hi))
-        one = dict(sc, domain_min=tuple(lo), domain_max=tuple(hi), batch=False,
-                   colliders=[{"type": "box", "size": ext, "center": center, "reverse": True}])
-        o = O.OracleSim(one, ps[k], vs[k], variant="f32", threads=threads)
-        it_o, _ = o.pcisph_substep(sc["dt"], sc["max_density_error_ratio"], sc["max_iterations"],
-                                   O.PCISPH_TOLERANCE)
+        a, b = first[k], first[k + 1]
+        one = dict(sc, domain_min=dmin, domain_max=dmax, batch=False, colliders=[containers[k]])
+        o = O.OracleSim(one, ps[a:b], vs[a:b], variant="f32", threads=threads)
+        it_o, err_o = o.pcisph_substep(sc["dt"], sc["max_density_error_ratio"], sc["max_iterations"],
+                                       O.PCISPH_TOLERANCE)
         want = o.get(O.POSITION)
         o.close()
         assert its[k] == it_o, (k, its[k], it_o)
         assert errs[k] < sc["max_density_error_ratio"]
-        packed = np.abs(want + off[k][None, :]).astype(np.float32)
-        allowed = 16.0 * np.spacing(packed).astype(np.float64) + 1e-5 * sc["spacing"]
-        assert np.all(np.abs(nxt[k] - want) <= allowed), (k, float(np.max(np.abs(nxt[k] - want) - allowed)))
+        assert abs(errs[k] - err_o) <= 1e-4, (k, errs[k], err_o)
+        allowed = np.maximum(1e-5 * h0, 8.0 * np.spacing(np.abs(want).astype(np.float32)).astype(np.float64))
+        d = np.abs(nxt[a:b].astype(np.float64) - want)
+        assert np.all(d <= allowed), (k, float(np.max(d / allowed)))

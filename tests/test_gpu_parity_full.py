@@ -22,8 +22,12 @@ oracle (the reference CPU path restated, all host threads) -- pass by pass:
   - a whole tolerance-mode substep (src/equations/pcisph_equations3.cpp:218-256): the
     same number of corrector iterations and positions within 1e-5 x spacing or 8 ulps of
     the coordinate, whichever is larger (an FP32 coordinate cannot be closer than its ulp;
-    the integration x + dt (v + dt F / m) and the collision projections each round on the
-    coordinate's scale -- the report gives the worst particle in ulps).
+    the integration x + dt (v + dt F / m) rounds on the coordinate's scale -- the report
+    gives the worst particle in ulps).  A particle in contact with a collider gets 2 ulps
+    of the collider frame's scale instead when that is larger: its normal coordinate can
+    land within an ulp of the surface, the projection then fires on one side only, and it
+    rounds every coordinate in the collider's frame (a box measures from its corner, so a
+    coordinate near 0 moves by an ulp of the box's half extent).
 
 Every case prints the per-particle relative error percentiles (p50, p99, max), and
 appends them as one JSON line to $BBG_PARITY_REPORT when that is set.
@@ -91,6 +95,28 @@ def pair_sum(x, rows, term):
         r = np.linalg.norm(x[jj] - x[ii], axis=2)
         out[a:b] = np.sum(np.where(ok, term(ii, jj, r), 0.0), axis=1)
     return out
+
+
+def collider_frame(sc, *positions):
+    """The largest coordinate of the colliders' frames (corner or centre + radius), and
+    which particles lie within a particle radius (+ 1e-4) of a collider surface in any of
+    the given position arrays."""
+    r = sc["spacing"] + 1e-4
+    scale, contact = 0.0, np.zeros(len(positions[0]), bool)
+    for c in sc.get("colliders", []):
+        t = np.asarray(c.get("center", (0.0, 0.0, 0.0)), np.float64)
+        if c["type"] == "box":
+            half = np.asarray(c["size"], np.float64) / 2
+            scale = max(scale, float(np.max(np.abs(t) + half)))
+            for x in positions:
+                gap = half[None, :] - np.abs(np.asarray(x, np.float64) - t[None, :])
+                contact |= gap.min(axis=1) <= r if c.get("reverse") else gap.max(axis=1) >= -r
+        else:
+            scale = max(scale, float(np.max(np.abs(t)) + c["radius"]))
+            for x in positions:
+                d = np.linalg.norm(np.asarray(x, np.float64) - t[None, :], axis=1) - c["radius"]
+                contact |= np.abs(d) <= r
+    return scale, contact
 
 
 def moving_state(name, seed, substeps):
@@ -231,11 +257,30 @@ def test_substep_parity_full_size(gpu, name, seed, substeps):
     dxyz = np.abs(pg3.astype(np.float64) - po3)
     ulp = np.spacing(np.abs(po3).astype(np.float32)).astype(np.float64)
     allowed = np.maximum(RTOL * h0, 8.0 * ulp)
+    # a particle in contact with a collider may be projected on one side only (its normal
+    # coordinate lies within an ulp of the surface), and the projection rounds every
+    # coordinate in the collider's frame (box.cpp:111-172 measures from a box corner)
+    scale, contact = collider_frame(sc, pg3, po3)
+    allowed[contact] = np.maximum(allowed[contact], 2.0 * float(np.spacing(np.float32(2.0 * scale))))
+    rep["substep"]["collider_contacts"] = int(contact.sum())
     rep["substep"]["position_err_max_ulps"] = float((dxyz / ulp).max())
     dx = np.linalg.norm(pg3 - po3, axis=1) / h0
     rep["substep"]["position_err_over_spacing"] = percentiles(dx)
     rep["substep"]["position_err_over_allowed"] = percentiles((dxyz / allowed).max(axis=1))
     rep["substep"]["density_rel"] = percentiles(np.abs(g.get(bb.FIELD_DENSITY) - o.get(O.DENSITY)) / o.get(O.DENSITY))
+    # the particles farthest from their bound, with the fields that decide their positions
+    over = (dxyz / allowed).max(axis=1)
+    worst = np.argsort(over)[-4:][::-1]
+    fields = {"force": (bb.FIELD_FORCE, O.FORCE), "pressure_force": (bb.FIELD_PRESSURE_FORCE, O.PRESSURE_FORCE),
+              "pressure": (bb.FIELD_PRESSURE, O.PRESSURE), "pred_density": (bb.FIELD_PRED_DENSITY, O.PRED_DENSITY)}
+    got = {k: (g.get(a), o.get(b)) for k, (a, b) in fields.items()}
+    vo3 = o.get(O.VELOCITY)
+    rep["substep"]["worst"] = [
+        {"particle": int(w), "over_allowed": float(over[w]), "start": p[w].tolist(), "start_vel": v[w].tolist(),
+         "gpu": pg3[w].tolist(), "oracle": po3[w].tolist(), "gpu_vel": vg3[w].tolist(), "oracle_vel": vo3[w].tolist(),
+         **{k + "_gpu": np.asarray(a[w]).tolist() for k, (a, b) in got.items()},
+         **{k + "_oracle": np.asarray(b[w]).tolist() for k, (a, b) in got.items()}}
+        for w in worst]
     g.close()
     o.close()
     checks["substep_iterations"] = st["iterations"] == it_o
