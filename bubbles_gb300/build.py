@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I", INCLUDE,
              "-I", CSRC]
 
-CU_SOURCES = ["grid.cu", "sph.cu", "mlp.cu", "frame.cu", "emit.cu", "sdf.cu", "mesh.cu", "boundary.cu", "surface.cu", "mc.cu", "api.cu", "noalloc.cu"]
+CU_SOURCES = ["grid.cu", "sph.cu", "mlp.cu", "frame.cu", "emit.cu", "sdf.cu", "mesh.cu", "boundary.cu", "surface.cu", "mc.cu", "api.cu", "api_batch.cu", "api_io.cu", "api_emit.cu", "api_post.cu", "noalloc.cu"]
 CXX_SOURCES = ["host_math.cpp"]
 
 
