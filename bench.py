@@ -305,14 +305,17 @@ def cpu_sample(scene, pos, vel, depth):
             "a %d-layer slab of the block" % depth)
 
 
-def launches_per_substep(scene, variant, iters):
-    """Kernels one graph-launched PCISPH substep runs: 6 for the grid rebuild (hash and
-    count, 3 scan kernels, place, rank and gather), density, non-pressure, 3 per corrector
-    iteration (predicted density, pressure force, loop control), plus the warm start (one
-    kernel; learned: features and the MLP); 2 more when pseudo-viscosity is active."""
+def launches_per_substep(scene, variant, iters, worklist=1):
+    """Kernels one graph-launched PCISPH substep runs: 5 for the grid rebuild (hash and
+    count, 2 scan kernels, place, rank and gather), 2 for density (the pair-record copy and
+    the pass), non-pressure, 3 per corrector iteration (predicted density, pressure force,
+    loop control), plus the warm start (one kernel; learned: features and the MLP); 2 more
+    when pseudo-viscosity is active.  A batch adds the scenes' slot ranges and, with a work
+    list, its rebuild before each iteration."""
     pv = 2 if scene.get("pseudo_viscosity", 10.0) * scene["dt"] > 0.1 else 0
     extra = {"plain": 0, "warm": 1, "learned": 2}[variant]
-    return 8 + extra + 3 * iters + pv
+    batch = (1 + (iters if worklist else 0)) if scene.get("batch") else 0
+    return 8 + extra + 3 * iters + pv + batch
 
 
 def sample_substeps(first, total, k):
@@ -834,7 +837,8 @@ def run_ours(args, scene, pos):
         total_s = sum(dev.ms) / 1e3
         value, tmax, _ = aggregate(dist, float(n * args.steps), total_s)
         e2e_value, _, _ = aggregate(dist, float(n * args.steps), e2e_s)
-        launches_timed = int(sum(launches_per_substep(scene, variant, it) for it in dev.iters))
+        launches_timed = int(sum(launches_per_substep(scene, variant, it, tuning_used.get("batch_worklist", 1))
+                                 for it in dev.iters))
         plain = None
         if gp is not None:
             pv, _, _ = aggregate(dist, float(n * args.steps), sum(pln.ms) / 1e3)
@@ -960,6 +964,8 @@ def run_ours(args, scene, pos):
         "gpu_launches": launches_timed,
         "clocks": clocks,
         "kernels": per_kernel,
+        # a batch's corrector passes run over the unconverged scenes' tiles only, while
+        # the fractions count every particle: for batches they overstate those passes
         "kernel_bounds": kernel_bounds(prof, table, n, peak,
                                        load_profile_figures(args.config, "warp_instructions_per_particle"),
                                        torch.cuda.get_device_properties(local).multi_processor_count,

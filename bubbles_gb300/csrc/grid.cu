@@ -6,7 +6,8 @@
 //   1. hash + count:  cell id of every particle (exact reference hash) and its arrival
 //                     index inside the cell, one atomic per distinct cell per warp
 //                     (__match_any_sync aggregation);
-//   2. scan:          exclusive scan of the per-cell counts -> cell start offsets;
+//   2. scan:          exclusive scan of the per-cell counts -> cell start offsets (tile
+//                     totals, then each tile's scan plus the sum of the tiles before it);
 //   3. place:         (original id, old slot) written into its cell's range;
 //   4. rank + gather: each particle's final slot is its cell start plus its rank by
 //                     original id inside the cell, which makes the permutation the
@@ -88,21 +89,16 @@ k_scan_reduce(const unsigned *__restrict__ count, unsigned cells, unsigned *__re
     if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_partials(unsigned *partials, int nb) {
-    unsigned carry = 0;
-    for (int base = 0; base < nb; base += kScanThreads) {
-        const int idx = base + threadIdx.x;
-        const unsigned v = idx < nb ? partials[idx] : 0u;
-        unsigned total;
-        const unsigned ex = block_excl_scan(v, &total);
-        if (idx < nb) partials[idx] = carry + ex;
-        carry += total;
-    }
-}
-
+// Each block scans its tile of counts and adds the sum of the tiles before it, which it
+// reduces itself from the per-tile totals of k_scan_reduce (a few hundred to a few thousand
+// values), so the scan takes two launches.
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_apply(unsigned *__restrict__ count, unsigned cells, const unsigned *__restrict__ partials,
              unsigned *__restrict__ start) {
+    unsigned before = 0;
+    for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) before += partials[t];
+    unsigned carry;
+    block_excl_scan(before, &carry);
     const unsigned base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     unsigned v[kScanItems];
     unsigned s = 0;
@@ -113,7 +109,7 @@ k_scan_apply(unsigned *__restrict__ count, unsigned cells, const unsigned *__res
         s += v[k];
     }
     unsigned total;
-    unsigned run = block_excl_scan(s, &total) + partials[blockIdx.x];
+    unsigned run = block_excl_scan(s, &total) + carry;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
         unsigned idx = base + k;
@@ -171,7 +167,6 @@ void launch_cell_scan(unsigned *count, unsigned cells, unsigned *partials, unsig
                       cudaStream_t s) {
     const int nb = blocks_for(cells, kScanTile);
     k_scan_reduce<<<nb, kScanThreads, 0, s>>>(count, cells, partials);
-    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, nb);
     k_scan_apply<<<nb, kScanThreads, 0, s>>>(count, cells, partials, start);
 }
 
@@ -186,10 +181,9 @@ void launch_grid_update(const Params &P, const DevBufs &B, int src, int pid_src,
     BBG_PEND(B, s);
     BBG_PBEGIN(B, KID_SCAN, s, -1);
     k_scan_reduce<<<nb, kScanThreads, 0, s>>>(B.count, cells, B.partials);
-    k_scan_partials<<<1, kScanThreads, 0, s>>>(B.partials, nb);
     k_scan_apply<<<nb, kScanThreads, 0, s>>>(B.count, cells, B.partials, B.start);
     BBG_PEND(B, s);
-    if (B.prof && B.prof->on) B.prof->launches += 2;   // three scan kernels in one record
+    if (B.prof && B.prof->on) B.prof->launches += 1;   // two scan kernels in one record
     BBG_PBEGIN(B, KID_PLACE, s, -1);
     k_place<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, B.cell_old, B.sub, B.start,
                                                          B.pid[pid_src], B.tmp);

@@ -82,3 +82,24 @@ def test_smooth_surface_is_closed_and_outward(gpu, small):
     geo = np.cross(b - a, c - a)
     assert np.mean(np.sum(geo * (n[t[:, 0]] + n[t[:, 1]] + n[t[:, 2]]), axis=1) > 0) > 0.99
     assert np.array_equal(tr, t[:, [0, 2, 1]])
+
+
+def test_repeated_calls_reuse_the_solver_scratch(gpu, small):
+    """Post-processing calls take their device buffers from the solver's scratch, which
+    keeps its size between calls and grows when a call needs more: the same results on a
+    solver that ran other, smaller calls before, in any order."""
+    d = np.load(GOLDEN, allow_pickle=False)
+    sc, pos = small
+    args = {name: (d["nodes"], d["origin"], d["spacing"], d[name + "_values"], 0.0) for name in ("blobs", "noise")}
+    with bb.Solver(sc, pos=pos) as fresh:
+        want = {name: fresh.marching_cubes(*a) for name, a in args.items()}
+    nx, ny, nz = (int(v) for v in d["nodes"])
+    part = (nx // 2 + 1, ny // 2 + 1, nz // 2 + 1)   # a corner of the blobs field
+    corner = d["blobs_values"].reshape(nz, ny, nx)[:part[2], :part[1], :part[0]].ravel()
+    with bb.Solver(sc, pos=pos) as s:
+        for name in ("noise", "blobs", "noise"):
+            s.marching_cubes(part, d["origin"], d["spacing"], corner, 0.0)
+            got = s.marching_cubes(*args[name])
+            p, n, t = got
+            wp, wn, wt = want[name]
+            assert same_bits(p, wp) and same_bits(n, wn) and np.array_equal(t, wt)
