@@ -1033,7 +1033,7 @@ def main():
     scene, pos = scenes.config(args.config, seed=args.seed + rank)
     scene["pressure_init"] = {"plain": "zero", "warm": "previous", "learned": "learned"}[args.variant]
     if args.variant == "learned":
-        scene["mlp"] = {"train_substeps": args.prep}
+        scene["mlp"] = dict(scene.get("mlp_training", {}), train_substeps=args.prep)
         for kv in args.mlp:
             k, v = kv.split("=", 1)
             scene["mlp"][k] = float(v) if "." in v or "e" in v else int(v)

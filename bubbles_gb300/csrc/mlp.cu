@@ -49,18 +49,23 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 __device__ __forceinline__ __nv_bfloat162 as_bf2(uint32_t v) { return *reinterpret_cast<__nv_bfloat162 *>(&v); }
 __device__ __forceinline__ uint32_t as_u32(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
 
-// GELU (tanh form) of two BF16 values in BF16 arithmetic: 7 paired operations, one of
-// them on the MUFU pipe (tanh.approx.bf16x2).
-__device__ __forceinline__ uint32_t gelu_bf16x2(uint32_t xv) {
-    const __nv_bfloat162 x = as_bf2(xv);
-    const __nv_bfloat162 a = __float2bfloat162_rn(kGeluA), c = __float2bfloat162_rn(kGeluC);
-    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
-    const __nv_bfloat162 ax2 = __hmul2(a, __hmul2(x, x));
-    const __nv_bfloat162 u = __hmul2(c, __hfma2(ax2, x, x));
+// Inference folds GELU's constants into the weights.  With y = c x (c = sqrt(2 / pi)):
+//   GELU(x) = 0.5 x (1 + tanh(c (x + a x^3))) = (0.5 / c) y (1 + tanh(y + (a / c^2) y^3)),
+// so the packed layer 1 holds c W1, c b1 and yields y1; the hidden activation is
+// h = y (1 + tanh(y + a' y^3)), a' = a / c^2; layer 2 holds 0.5 W2 (= c W2 (0.5 / c)) and
+// c b2 and yields y2; layer 3 holds (0.5 / c) w3.
+constexpr float kGeluAFold = kGeluA / (kGeluC * kGeluC);
+
+// h = y (1 + tanh(y + a' y^3)) of two BF16 values in BF16 arithmetic: 5 paired operations,
+// one of them on the MUFU pipe (tanh.approx.bf16x2).
+__device__ __forceinline__ uint32_t gelu_bf16x2(uint32_t yv) {
+    const __nv_bfloat162 y = as_bf2(yv);
+    const __nv_bfloat162 a = __float2bfloat162_rn(kGeluAFold);
+    const __nv_bfloat162 ay2 = __hmul2(__hmul2(y, y), a);
+    const __nv_bfloat162 u = __hfma2(ay2, y, y);
     uint32_t t;
     asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(as_u32(u)));
-    const __nv_bfloat162 hx = __hmul2(half, x);
-    return as_u32(__hfma2(hx, as_bf2(t), hx));
+    return as_u32(__hfma2(y, as_bf2(t), y));
 }
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
@@ -403,9 +408,9 @@ __global__ void k_mlp_pack(const float *__restrict__ theta, uint32_t *__restrict
     for (int k = tid; k < 8 * 32; k += blockDim.x) {
         const int nt = k / 32, lane = k % 32, g = lane >> 2, t = lane & 3;
         const int col = 8 * nt + g;
-        auto w1 = [&](int r) -> float {
-            if (r < kIn) return theta[kOffW1 + r * kHid + col];
-            if (r == kIn) return theta[kOffB1 + col];
+        auto w1 = [&](int r) -> float {   // c W1, c b1 (the folded GELU)
+            if (r < kIn) return kGeluC * theta[kOffW1 + r * kHid + col];
+            if (r == kIn) return kGeluC * theta[kOffB1 + col];
             return 0.f;
         };
         w1f[k] = pack_bf16(w1(2 * t), w1(2 * t + 1));
@@ -415,11 +420,11 @@ __global__ void k_mlp_pack(const float *__restrict__ theta, uint32_t *__restrict
         const int q = k / 32, lane = k % 32, g = lane >> 2, t = lane & 3;
         const int kc = q / 16, nt = (q / 2) % 8, hh = q & 1;
         const int row = 16 * kc + 8 * hh + 2 * t, col = 8 * nt + g;
-        w2f[k] = pack_bf16(theta[kOffW2 + row * kHid + col], theta[kOffW2 + (row + 1) * kHid + col]);
+        w2f[k] = pack_bf16(0.5f * theta[kOffW2 + row * kHid + col], 0.5f * theta[kOffW2 + (row + 1) * kHid + col]);
     }
     for (int k = tid; k < kHid; k += blockDim.x) {
-        tail[kTailB2 + k] = theta[kOffB2 + k];
-        tail[kTailW3 + k] = __bfloat162float(__float2bfloat16_rn(theta[kOffW3 + k]));
+        tail[kTailB2 + k] = kGeluC * theta[kOffB2 + k];
+        tail[kTailW3 + k] = __bfloat162float(__float2bfloat16_rn((0.5f / kGeluC) * theta[kOffW3 + k]));
     }
     if (tid == 0) {
         tail[kTailB3] = theta[kOffB3];

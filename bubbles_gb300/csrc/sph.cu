@@ -306,18 +306,6 @@ k_density_x2(Params P, float4 *__restrict__ pos, float4 *__restrict__ vel, unsig
         listed = 0;
         atomicAdd(&st->crowded, 1u);
     }
-    {
-        // Rows of the member-major list are written lane by lane; a 32-byte sector holds
-        // the entries of 8 consecutive slots.  Padding each slot's rows up to the longest
-        // list of its 8 (with the slot's own index, never read: the count ends the list)
-        // writes every sector in full, so L2 need not fill partly written sectors from DRAM.
-        const int lane = threadIdx.x & 31;
-        const int live = min(32, P.n - (i - lane));   // lanes of this warp with a particle
-        const unsigned grp = (live >= 32 ? 0xffffffffu : (1u << live) - 1u) & (0xffu << (lane & ~7));
-        const int lim = min(listed, kMaxList);
-        const int gmax = (int)__reduce_max_sync(grp, (unsigned)lim);
-        for (int q = lim; q < gmax; q++) list[(size_t)q * n + (size_t)i] = list_code((unsigned)i, 0u);
-    }
     const float di = s0 * P.std_c * P.mass;
     if (compute_pressure) {
         float p = P.eos_scale_over_exp * (powf(di / P.target_density, P.eos_exp) - 1.f);

@@ -32,28 +32,34 @@ def bf16(x):
     return r.astype(np.uint32).view(np.float32)
 
 
-def gelu_bf16(x):
-    """GELU of BF16 values in BF16 arithmetic, rounding after every operation as the
-    inference kernel's paired BF16 instructions do (the fused multiply-add rounds once)."""
-    a, c, half = bf16(np.float32(GELU_A)), bf16(np.float32(GELU_C)), np.float32(0.5)
-    x = bf16(x)
-    ax2 = bf16(a * bf16(x * x))
-    u = bf16(c * bf16(ax2.astype(np.float64) * x + x))
+GELU_A_FOLD = GELU_A / (GELU_C * GELU_C)
+
+
+def gelu_folded_bf16(y):
+    """The inference kernel's hidden activation h = y (1 + tanh(y + a' y^3)), a' = a / c^2,
+    of y = c x, in BF16 arithmetic: rounding after every operation as its paired BF16
+    instructions do (a fused multiply-add rounds once).  GELU(x) = (0.5 / c) h."""
+    a = bf16(np.float32(GELU_A_FOLD))
+    y = bf16(y)
+    ay2 = bf16(bf16(y * y) * a)
+    u = bf16((ay2.astype(np.float64) * y + y).astype(np.float32))
     t = bf16(np.tanh(u.astype(np.float64)).astype(np.float32))
-    hx = bf16(half * x)
-    return bf16((hx.astype(np.float64) * t + hx).astype(np.float32))
+    return bf16((y.astype(np.float64) * t + y).astype(np.float32))
 
 
 def forward_bf16(theta, x):
-    """What the inference kernel computes: BF16 inputs and weights, FP32 accumulation,
-    BF16 GELU of both hidden layers, BF16 w3 and an FP32 output dot product."""
+    """What the inference kernel computes: GELU's constants folded into the weights (layer 1
+    holds c W1, c b1; layer 2 0.5 W2, c b2; layer 3 (0.5 / c) w3), BF16 inputs and weights,
+    FP32 accumulation, the BF16 activation of both hidden layers, BF16 w3 and an FP32
+    output dot product."""
     w1, b1, w2, b2, w3, b3 = unpack(theta)
+    c = np.float32(GELU_C)
     x = bf16(np.asarray(x, np.float32)).astype(np.float64)
-    z1 = (x @ bf16(w1).astype(np.float64) + bf16(b1).astype(np.float64)).astype(np.float32)
-    h1 = gelu_bf16(z1).astype(np.float64)
-    z2 = (h1 @ bf16(w2).astype(np.float64) + b2.astype(np.float64)).astype(np.float32)
-    h2 = gelu_bf16(z2).astype(np.float64)
-    return (h2 @ bf16(w3).astype(np.float64) + float(b3)).astype(np.float32)
+    y1 = (x @ bf16(c * w1).astype(np.float64) + bf16(c * b1).astype(np.float64)).astype(np.float32)
+    h1 = gelu_folded_bf16(y1).astype(np.float64)
+    y2 = (h1 @ bf16(np.float32(0.5) * w2).astype(np.float64) + (c * b2).astype(np.float64)).astype(np.float32)
+    h2 = gelu_folded_bf16(y2).astype(np.float64)
+    return (h2 @ bf16(np.float32(0.5) / c * w3).astype(np.float64) + float(b3)).astype(np.float32)
 
 
 def loss_and_grad(theta, x, t, expectile=0.5):
