@@ -807,7 +807,7 @@ def run_ours(args, scene, pos):
         #   value: the learned substep replayed as a CUDA graph (device events), which
         #   also carries the run forward.
         dev, pln = StepLog(), StepLog()
-        e2e_s, e2e_iters = 0.0, []
+        e2e_s, e2e_iters, e2e_ms = 0.0, [], []
         cur = args.prep + args.warmup
         for idx in samples:
             while cur < idx:
@@ -825,7 +825,8 @@ def run_ours(args, scene, pos):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             e2e_step()
-            e2e_s += time.perf_counter() - t0
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+            e2e_s += e2e_ms[-1] / 1e3
             e2e_iters.append(g.stats()["iterations"])
             restore(g, warm)
             dev.add(timed_event(stream, flush, lambda: g.advance_time_step(dt)), g.stats())
@@ -920,6 +921,7 @@ def run_ours(args, scene, pos):
                          % (len(samples), first, last, total, args.prep, args.warmup)),
               "corrector_iterations_mean": float(np.mean(dev.iters)),
               "corrector_iterations_mean_e2e": float(np.mean(e2e_iters)),
+              "e2e_ms_per_sample": [round(x, 3) for x in e2e_ms],
               "max_density_error_ratio_max": float(np.max(dev.errs)),
               "substeps_at_max_iterations_above_tolerance": dev.not_converged,
               "state_checks": {"out_of_grid_max": dev.out_of_grid, "crowded_max": dev.crowded},
