@@ -21,6 +21,7 @@ its warm-start MLP online on their (features, converged pressure) pairs.  After
   cpu_baseline  the CPU oracle (restatement of the reference's CPU path) on the box's
              host cores, on a bounded sample of the same workload
   config.plain_same_window  the plain (zero-start) corrector timed on the same substeps
+             (as CUDA graphs, and in the reference's launch sequence: plain_host_loop_value)
 
 `--impl reference` times the reference's CPU implementation of the path (the oracle
 port, all host threads) on the same workload and prints the same line with
@@ -785,6 +786,10 @@ def run_ours(args, scene, pos):
                 if gp is not None:
                     restore(gp, False)
                     gp.advance_time_step(dt)
+                    restore(gp, False)
+                    gp.use_cuda_graphs(False)
+                    gp.advance_time_step(dt)
+                    gp.use_cuda_graphs(True)
                 e2e_step()
                 restore(g, warm)
                 g.profiler_enable(True)
@@ -806,7 +811,7 @@ def run_ours(args, scene, pos):
         #   e2e: the learned substep through bbg_step_host (host buffers, wall clock);
         #   value: the learned substep replayed as a CUDA graph (device events), which
         #   also carries the run forward.
-        dev, pln = StepLog(), StepLog()
+        dev, pln, pln_host = StepLog(), StepLog(), StepLog()
         e2e_s, e2e_iters, e2e_ms = 0.0, [], []
         cur = args.prep + args.warmup
         for idx in samples:
@@ -817,6 +822,12 @@ def run_ours(args, scene, pos):
             if gp is not None:
                 restore(gp, False)
                 pln.add(timed_event(stream, flush, lambda: gp.advance_time_step(dt)), gp.stats())
+                # the same plain substep in the reference's launch sequence: one launch per
+                # pass, the host reading each iteration's error before the next
+                restore(gp, False)
+                gp.use_cuda_graphs(False)
+                pln_host.add(timed_event(stream, flush, lambda: gp.advance_time_step(dt)), gp.stats())
+                gp.use_cuda_graphs(True)
             restore(g, warm)
             g.profiler_enable(True)
             flush.zero_()
@@ -847,6 +858,12 @@ def run_ours(args, scene, pos):
                      "corrector_iterations_mean": float(np.mean(pln.iters)),
                      "max_density_error_ratio_max": float(np.max(pln.errs)),
                      "not_converged": pln.not_converged}
+            ph, _, _ = aggregate(dist, float(n * args.steps), sum(pln_host.ms) / 1e3)
+            plain["host_loop"] = {
+                "value": ph, "ms_per_step": sum(pln_host.ms) / args.steps,
+                "corrector_iterations_mean": float(np.mean(pln_host.iters)),
+                "launches": "one launch per pass, the host reading each corrector iteration's "
+                            "max error before launching the next (the reference's GPU loop)"}
             gp.close()
         final_pos, final_vel = g.download()
         batch_offsets = g.layout() if scene.get("batch") else None
@@ -975,6 +992,8 @@ def run_ours(args, scene, pos):
     }
     if plain is not None:
         line.update({"plain_value": plain["value"], "speedup_vs_plain": value / plain["value"],
+                     "plain_host_loop_value": plain["host_loop"]["value"],
+                     "speedup_vs_plain_host_loop": value / plain["host_loop"]["value"],
                      "corrector_iterations_plain": plain["corrector_iterations_mean"],
                      "not_converged_plain": plain["not_converged"],
                      "max_density_error_ratio_plain": plain["max_density_error_ratio_max"]})
