@@ -80,7 +80,8 @@ class SceneDesc(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("block_size", ctypes.c_int), ("batch_np", ctypes.c_int),
                 ("batch_pd", ctypes.c_int), ("batch_pf", ctypes.c_int), ("prune", ctypes.c_int),
-                ("particles_per_thread", ctypes.c_int), ("batch_worklist", ctypes.c_int)]
+                ("particles_per_thread", ctypes.c_int), ("tile_order", ctypes.c_int),
+                ("batch_worklist", ctypes.c_int)]
 
 
 class Shape(ctypes.Structure):

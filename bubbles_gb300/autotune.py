@@ -10,6 +10,8 @@ same substeps (replayed as CUDA graphs from that state) for candidate settings:
   * whether the density pass leaves out the neighbour cells and rows each particle's
     sphere cannot reach (bitwise the same results): 0, 1;
   * particles per thread of the predicted-density and pressure-force passes: 1, 2;
+  * the order in which blocks take tiles: 0 (block b, tile b) or 1 (the blocks an SM runs
+    take neighbouring tiles);
   * for batches, how the corrector passes cover the scenes: one block per tile of every
     scene (0), one block per tile of the scenes still iterating, from a work list rebuilt
     every iteration (1), or persistent blocks over that work list (2);
@@ -38,6 +40,7 @@ BLOCKS = (64, 128, 256)
 BATCHES = (2, 4, 8)
 PRUNES = (0, 1)
 PPTS = (1, 2)
+TILE_ORDERS = (0, 1)
 WORKLISTS = (0, 1, 2)
 CELL_SCALES = (2.0, 2.5, 3.0)
 
@@ -92,7 +95,7 @@ def tune_launches(g, dt, snap, steps, warm, log):
     best_t = time_substeps(g, dt, snap, steps, warm)
     log.append({"tuning": dict(best), "seconds": best_t})
     knobs = [("block_size", BLOCKS), ("prune", PRUNES), ("batch_pf", BATCHES), ("batch_pd", BATCHES),
-             ("batch_np", BATCHES), ("particles_per_thread", PPTS)]
+             ("batch_np", BATCHES), ("particles_per_thread", PPTS), ("tile_order", TILE_ORDERS)]
     if isinstance(g, BatchSolver):
         knobs.append(("batch_worklist", WORKLISTS))
     for key, values in knobs:

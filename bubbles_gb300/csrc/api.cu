@@ -1674,6 +1674,7 @@ bbg_status bbg_get_tuning(bbg_solver s, bbg_tuning *t) {
     t->batch_pf = s->B.tune.batch_pf;
     t->prune = s->B.tune.prune;
     t->particles_per_thread = s->B.tune.ppt;
+    t->tile_order = s->B.tune.tile_order;
     t->batch_worklist = s->B.tune.worklist;
     return BBG_OK;
 }
@@ -1688,6 +1689,7 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
     if (t->prune != 0 && t->prune != 1) return fail(BBG_ERR_INVALID_ARGUMENT, "prune must be 0 or 1");
     if (t->particles_per_thread != 1 && t->particles_per_thread != 2)
         return fail(BBG_ERR_INVALID_ARGUMENT, "particles_per_thread must be 1 or 2");
+    if (t->tile_order != 0 && t->tile_order != 1) return fail(BBG_ERR_INVALID_ARGUMENT, "tile_order must be 0 or 1");
     if (t->batch_worklist < 0 || t->batch_worklist > 2)
         return fail(BBG_ERR_INVALID_ARGUMENT, "batch_worklist must be 0, 1 or 2");
     CK(cudaStreamSynchronize(s->stream));
@@ -1697,6 +1699,7 @@ bbg_status bbg_set_tuning(bbg_solver s, const bbg_tuning *t) {
     s->B.tune.batch_pf = t->batch_pf;
     s->B.tune.prune = t->prune;
     s->B.tune.ppt = t->particles_per_thread;
+    s->B.tune.tile_order = t->tile_order;
     s->B.tune.worklist = t->batch_worklist;
     if (s->nscenes > 0) update_worklist_grid(s->B);
     s->epoch++;   // captured graphs hold the old launch shapes

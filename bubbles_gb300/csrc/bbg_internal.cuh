@@ -94,6 +94,7 @@ struct Params {
     int *wl_off;                    // nscenes + 1 offsets of the scenes' tile segments
     int *wl_tile;                   // first tile of each scene's segment
     int *wl_ctr;                    // next work item of the two persistent passes
+    int tile_sms;                   // > 0: blocks dealt to tiles SM-strided (tile_of_block)
     int has_sdf;                    // some collider has a signed-distance field
     SdfDev sdf[kMaxSdf];
 };

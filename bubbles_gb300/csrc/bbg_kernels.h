@@ -16,6 +16,7 @@ struct Tuning {
     int batch_pf = 4;      // pressure-force pass
     int prune = 0;         // density pass: walk only the cells each particle's sphere reaches (1)
     int ppt = 1;           // particles per thread of the predicted-density and pressure-force passes (1, 2)
+    int tile_order = 0;    // member-walking passes: 0 block b takes tile b; 1 SM-strided (tile_of_block)
     int worklist = 1;      // batch corrector: 0 all tiles, 1 a block per listed tile, 2 persistent blocks
     int wl_grid_pd = 0;    // batch: resident blocks of the persistent predicted-density and
     int wl_grid_pf = 0;    // pressure-force passes for this shape (update_worklist_grid)

@@ -338,9 +338,11 @@ k_non_pressure(Params P, const float4 *__restrict__ pos, const float4 *__restric
                const unsigned *__restrict__ start, const ListEntry *__restrict__ list, const int *__restrict__ nbr,
                float4 *__restrict__ force, float4 *__restrict__ xstar, float4 *__restrict__ pforce,
                float *__restrict__ press, float *__restrict__ divsum, int predict, float dt, float dt_over_m) {
+    const int s0 = tile_of_block(P, blockIdx.x, (P.n + (int)blockDim.x - 1) / (int)blockDim.x) * blockDim.x;
+    if (s0 >= P.n) return;
     __shared__ TileMap T;
-    tile_setup(P.g, cell, start, P.n, T);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    tile_setup_at(P.g, cell, start, s0, T);
+    const int i = s0 + threadIdx.x;
     if (i >= P.n) return;
     const float4 pi = pos[i];
     const float4 vi = vel[i];
@@ -580,7 +582,7 @@ __device__ __forceinline__ int worklist_next(int *ctr, int *slot, int &parity) {
 // First slot of the block's tile of `slots` slots: the block's own, or with a batch work
 // list (wl) the tile of work item blockIdx.x; -1 for a block past the list's end.
 __device__ __forceinline__ int block_tile(const Params &P, int wl, int slots) {
-    if (!wl) return blockIdx.x * slots;
+    if (!wl) return tile_of_block(P, blockIdx.x, (P.n + slots - 1) / slots) * slots;
     if ((int)blockIdx.x >= worklist_total(P, slots)) return -1;
     return worklist_tile(P, blockIdx.x) * slots;
 }
@@ -1055,12 +1057,29 @@ void launch_density(const Params &P, const DevBufs &B, int buf, int compute_pres
     BBG_PEND(B, s);
 }
 
+// Blocks of a member-walking pass over tiles of `slots` slots, in the tuned tile order
+// (Params::tile_sms of the returned parameters).
+static int tiled_grid(const Params &P, const DevBufs &B, int slots, Params *Q) {
+    *Q = P;
+    Q->tile_sms = 0;
+    const int tiles = blocks_for(P.n, slots);
+    if (B.tune.tile_order != 1 || P.nscenes > 0) return tiles;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) return tiles;
+    Q->tile_sms = sms;
+    return sms * ((tiles + sms - 1) / sms);
+}
+
 template <bool DIV, bool WARM>
-static void non_pressure_nb(const Params &P, const DevBufs &B, int buf, int predict, float dt,
+static void non_pressure_nb(const Params &P0, const DevBufs &B, int buf, int predict, float dt,
                             float dt_over_m, cudaStream_t s, float *divsum) {
     const int t = B.tune.block;
+    Params P;
+    const int grid = tiled_grid(P0, B, t, &P);
 #define NP_LAUNCH(NB)                                                                        \
-    k_non_pressure<DIV, WARM, NB><<<blocks_for(P.n, t), t, 0, s>>>(                          \
+    k_non_pressure<DIV, WARM, NB><<<grid, t, 0, s>>>(                                        \
         P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.xstar, B.pforce, \
         B.press, divsum, predict, dt, dt_over_m)
     switch (B.tune.batch_np) {
@@ -1148,10 +1167,12 @@ void launch_pred_density(const Params &P, const DevBufs &B, int buf, int k, floa
 #undef PD_LAUNCH
     } else {
         const int ppt = corrector_ppt(B);
-#define PD_LAUNCH(NB, PPT)                                                                              \
-    k_pred_density<NB, PPT><<<blocks_for(P.n, t * PPT), t, 0, s>>>(P, B.pos[buf], B.xstar, B.cell, B.start, \
-                                                                   B.list, B.nbr, B.press, B.rhostar,      \
-                                                                   B.derr, B.st, k, delta, clamp_total, wl)
+        Params Q;
+        const int grid = wl ? blocks_for(P.n, t * ppt) : tiled_grid(P, B, t * ppt, &Q);
+        if (wl) Q = P;
+#define PD_LAUNCH(NB, PPT)                                                                        \
+    k_pred_density<NB, PPT><<<grid, t, 0, s>>>(Q, B.pos[buf], B.xstar, B.cell, B.start, B.list, B.nbr, \
+                                               B.press, B.rhostar, B.derr, B.st, k, delta, clamp_total, wl)
         switch (B.tune.batch_pd * 10 + ppt) {
             case 21: PD_LAUNCH(2, 1); break;
             case 81: PD_LAUNCH(8, 1); break;
@@ -1195,9 +1216,12 @@ void launch_pressure_force(const Params &P, const DevBufs &B, int buf, int k, in
 #undef PF_LAUNCH
     } else {
         const int ppt = corrector_ppt(B);
+        Params Q;
+        const int grid = wl ? blocks_for(P.n, t * ppt) : tiled_grid(P, B, t * ppt, &Q);
+        if (wl) Q = P;
 #define PF_LAUNCH(NB, PPT)                                                                             \
-    k_pressure_force<NB, PPT><<<blocks_for(P.n, t * PPT), t, 0, s>>>(                                   \
-        P, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,           \
+    k_pressure_force<NB, PPT><<<grid, t, 0, s>>>(                                                       \
+        Q, B.pos[buf], B.vel[buf], B.cell, B.start, B.list, B.nbr, B.force, B.pforce, B.xstar,           \
         B.pos[1 - buf], B.vel[1 - buf], B.st, k, max_it, dt, dt_over_m, mode, wl)
         switch (B.tune.batch_pf * 10 + ppt) {
             case 21: PF_LAUNCH(2, 1); break;

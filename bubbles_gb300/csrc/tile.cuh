@@ -75,6 +75,18 @@ __device__ __forceinline__ void tile_setup_at(const GridDev &g, const unsigned *
     __syncthreads();
 }
 
+// Tile of block b among `tiles`.  With P.tile_sms = G > 0, blocks b, b + G, b + 2G, ... take
+// consecutive tiles: tile = (b mod G) * per + b / G, per = ceil(tiles / G).  The block
+// scheduler's first waves place those blocks on the same SM (one block per SM per round), so
+// the blocks resident on an SM walk neighbouring tiles and share neighbour records in its L1.
+// The grid is G * per blocks; a block whose tile is past the last one has no work.
+__device__ __forceinline__ int tile_of_block(const Params &P, int b, int tiles) {
+    const int G = P.tile_sms;
+    if (G <= 0) return b;
+    const int per = (tiles + G - 1) / G;
+    return (b % G) * per + b / G;
+}
+
 // The range starts of the block's own tile (slots blockIdx.x * blockDim.x on).
 __device__ __forceinline__ void tile_setup(const GridDev &g, const unsigned *__restrict__ cell,
                                            const unsigned *__restrict__ start, int n, TileMap &T) {

@@ -479,6 +479,8 @@ typedef struct {
     int batch_pf;
     int prune;           /* 0 (default: measured faster on GB300) or 1 */
     int particles_per_thread;  /* predicted-density and pressure-force passes: 1 (default) or 2 */
+    int tile_order;      /* member-walking passes: 0 (default) block b takes tile b; 1 blocks
+                            b, b + S, b + 2S, ... (S = the SM count) take consecutive tiles */
     int batch_worklist;  /* batches: 0 one block per tile of every scene, 1 (default) one block
                             per tile of the scenes whose corrector still runs (a work list
                             rebuilt every iteration), 2 persistent blocks over that list */

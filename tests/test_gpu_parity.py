@@ -509,9 +509,9 @@ def test_gpu_against_reference_fixtures(gpu):
 
 
 @pytest.mark.parametrize("tuning", [dict(block_size=64, batch_np=2, batch_pd=8, batch_pf=2, prune=0,
-                                         particles_per_thread=2, batch_worklist=0),
+                                         particles_per_thread=2, tile_order=1, batch_worklist=0),
                                     dict(block_size=256, batch_np=8, batch_pd=2, batch_pf=8, prune=1,
-                                         particles_per_thread=1, batch_worklist=2)])
+                                         particles_per_thread=1, tile_order=1, batch_worklist=2)])
 def test_launch_tuning_does_not_change_results(gpu, moved, tuning):
     """Block size, gather batches, the density pass's reach test and particles per thread
     change the launch shape, not the arithmetic: the substeps are bitwise identical to the
