@@ -25,7 +25,7 @@
 
 #include "../sph_oracle.h"
 
-/* Normally defined by src/solvers/pcisph_solver2.cpp:7, which this build leaves out. */
+/* Normally defined by src/solvers/pcisph_solver2.cpp:7, which the host-only compile leaves out. */
 extern const Float kDefaultTimeStepLimitScale = 5.0;
 
 /* Non-static reference functions without a header declaration. */

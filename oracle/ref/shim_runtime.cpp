@@ -1,5 +1,5 @@
 /* Definitions behind the host-only CUDA stand-in and the reference's profiler hooks
- * (profiler.h declares them; the profiler itself is not part of this build). */
+ * (profiler.h declares them; the profiler itself is not part of the host-only compile). */
 #include <cuda_runtime.h>
 #include <profiler.h>
 

@@ -1,8 +1,8 @@
 /*
  * sph_oracle.c -- CPU oracle for the Bubbles 3D SPH / PCISPH particle step.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path (see sph_oracle.h for
- * who may load it).  Build with -ffp-contract=off so that x86-64 and aarch64
+ * TEST INFRASTRUCTURE ONLY: the reference result the CUDA path is compared with (see
+ * sph_oracle.h for who may load it).  Build with -ffp-contract=off so that x86-64 and aarch64
  * produce the same bits (the reference itself is compiled without contraction on
  * x86-64).  -DORC_FLOAT=float gives the FP32 oracle, -DORC_FLOAT=double the FP64
  * one.

@@ -1,8 +1,8 @@
 /*
  * sph_oracle.h -- CPU oracle for the Bubbles 3D SPH / PCISPH particle step.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA path is compared
- * against; nothing in the product links it.  Only tests/, __graft_entry__.smoke()
+ * TEST INFRASTRUCTURE ONLY.  This is the reference result that the CUDA path is
+ * compared against; nothing in the product links it.  Only tests/, __graft_entry__.smoke()
  * and bench.py (its cpu_baseline leg and its --impl reference arm) may load it.
  *
  * It restates, in plain C, the reference's CPU implementation of the step:
