@@ -45,6 +45,17 @@ constexpr int kNbrMinBlocks = BBG_NBR_MIN_BLOCKS * kTile / kMaxTile;
 // occupancy for its latency-bound gathers
 constexpr int kPdMinBlocks = BBG_PD_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kPfMinBlocks = BBG_PF_MIN_BLOCKS * kTile / kMaxTile;
+#ifndef BBG_PDWL_MIN_BLOCKS
+#define BBG_PDWL_MIN_BLOCKS 16
+#endif
+#ifndef BBG_PFWL_MIN_BLOCKS
+#define BBG_PFWL_MIN_BLOCKS 12
+#endif
+// register budgets of the persistent batch passes, as the per-tile passes' (measured on
+// config 4: 8 blocks per SM, 48 and 64 registers without spills, lost 6 % to these, which
+// spill a little)
+constexpr int kPdWlMinBlocks = BBG_PDWL_MIN_BLOCKS * kTile / kMaxTile;
+constexpr int kPfWlMinBlocks = BBG_PFWL_MIN_BLOCKS * kTile / kMaxTile;
 constexpr int kDensityMinBlocks = 12 * kTile / kMaxTile;
 #ifndef BBG_DENSITY_MASK
 #define BBG_DENSITY_MASK 1
@@ -618,7 +629,7 @@ k_pred_density(Params P, float4 *pos, const float4 *__restrict__ xstar,
 // Batch: persistent blocks over the work list of the tiles whose scenes still run
 // (launch_worklist), the same per-particle work as k_pred_density.
 template <int NB>
-__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
+__global__ void __launch_bounds__(kMaxTile, kPdWlMinBlocks)
 k_pred_density_wl(Params P, float4 *pos, const float4 *__restrict__ xstar,
                   const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                   const ListEntry *__restrict__ list, const int *__restrict__ nbr, float *__restrict__ press,
@@ -742,7 +753,7 @@ k_pressure_force(Params P, const float4 *__restrict__ pos, const float4 *__restr
 
 // Batch: persistent blocks over the same work list as k_pred_density_wl.
 template <int NB>
-__global__ void __launch_bounds__(kMaxTile, kNbrMinBlocks)
+__global__ void __launch_bounds__(kMaxTile, kPfWlMinBlocks)
 k_pressure_force_wl(Params P, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                     const unsigned *__restrict__ cell, const unsigned *__restrict__ start,
                     const ListEntry *__restrict__ list, const int *__restrict__ nbr, float4 *__restrict__ force,
