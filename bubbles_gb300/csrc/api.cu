@@ -288,7 +288,7 @@ bbg_status mlp_allocate(bbg_solver s, const bbg_mlp_desc &d) {
         CK(mlp_prepare());
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->desc.device));
-        M.infer_blocks = 6 * (sms > 0 ? sms : 1);   // 6 blocks of 128 threads fit an SM
+        M.infer_blocks = kMlpBlocksPerSm * (sms > 0 ? sms : 1);   // the blocks of 128 threads an SM holds
         M.batch = d.batch;
         s->mlp_alloc = true;
     }

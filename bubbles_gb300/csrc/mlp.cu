@@ -108,7 +108,7 @@ __global__ void k_mlp_features(int n, const float4 *__restrict__ vel, const floa
 // clamp(MLP(features), 0, largest training target), rho* = rho, err = 0, pos.w = p / rho^2.
 // Layer-2 B fragments live in shared memory (8 KB per block), the layer-1 fragments,
 // bias and w3 in registers; GELU runs in BF16x2 arithmetic.
-__global__ void __launch_bounds__(128, 6)
+__global__ void __launch_bounds__(128, kMlpBlocksPerSm)
 k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restrict__ w1f,
                  const uint32_t *__restrict__ w2f, const float *__restrict__ tail, float p_unit, float scale,
                  float4 *__restrict__ pos, const float *__restrict__ rho, float *__restrict__ press,
@@ -149,35 +149,39 @@ k_mlp_warm_start(int n, const float4 *__restrict__ feat, const uint32_t *__restr
             h1[kc * 4 + hi * 2 + 0] = gelu_bf16x2(pack_bf16(c[0], c[1]));
             h1[kc * 4 + hi * 2 + 1] = gelu_bf16x2(pack_bf16(c[2], c[3]));
         }
-        // layer 2: 16 x 64 times 64 x 64, accumulators start at the bias
-        float acc[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const float2 b = sB2[4 * nt + t];   // columns 8 nt + 2 t, + 1
-            acc[nt][0] = b.x;
-            acc[nt][1] = b.y;
-            acc[nt][2] = b.x;
-            acc[nt][3] = b.y;
-        }
-#pragma unroll
-        for (int kc = 0; kc < 4; kc++) {
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const uint2 bf = sW2[(kc * 8 + nt) * 32 + lane];
-                mma_bf16(acc[nt], h1[kc * 4 + 0], h1[kc * 4 + 1], h1[kc * 4 + 2], h1[kc * 4 + 3], bf.x, bf.y);
-            }
-        }
-        // layer 3 on the FP32 pipes: rows g (c0, c1) and g + 8 (c2, c3)
+        // layer 2 (16 x 64 times 64 x 64, accumulators starting at the bias) and layer 3 on the
+        // FP32 pipes (rows g: c0, c1 and g + 8: c2, c3), in two halves of 32 output columns so
+        // that half the accumulators are live at a time
         float ya = 0.f, yb = 0.f;
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const float2 w = sW3[4 * nt + t];
-            const float2 ha = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][0], acc[nt][1]))));
-            const float2 hb = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[nt][2], acc[nt][3]))));
-            ya = fmaf(ha.x, w.x, ya);
-            ya = fmaf(ha.y, w.y, ya);
-            yb = fmaf(hb.x, w.x, yb);
-            yb = fmaf(hb.y, w.y, yb);
+        for (int half = 0; half < 2; half++) {
+            float acc[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float2 b = sB2[4 * (4 * half + q) + t];   // columns 8 nt + 2 t, + 1
+                acc[q][0] = b.x;
+                acc[q][1] = b.y;
+                acc[q][2] = b.x;
+                acc[q][3] = b.y;
+            }
+#pragma unroll
+            for (int kc = 0; kc < 4; kc++) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint2 bf = sW2[(kc * 8 + 4 * half + q) * 32 + lane];
+                    mma_bf16(acc[q], h1[kc * 4 + 0], h1[kc * 4 + 1], h1[kc * 4 + 2], h1[kc * 4 + 3], bf.x, bf.y);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float2 w = sW3[4 * (4 * half + q) + t];
+                const float2 ha = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[q][0], acc[q][1]))));
+                const float2 hb = __bfloat1622float2(as_bf2(gelu_bf16x2(pack_bf16(acc[q][2], acc[q][3]))));
+                ya = fmaf(ha.x, w.x, ya);
+                ya = fmaf(ha.y, w.y, ya);
+                yb = fmaf(hb.x, w.x, yb);
+                yb = fmaf(hb.y, w.y, yb);
+            }
         }
         ya += __shfl_xor_sync(0xffffffffu, ya, 1);
         ya += __shfl_xor_sync(0xffffffffu, ya, 2);

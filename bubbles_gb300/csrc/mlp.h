@@ -40,6 +40,13 @@ struct MlpBufs {
     int infer_blocks = 1;      // persistent inference grid
 };
 
+#ifndef BBG_MLP_MIN_BLOCKS
+#define BBG_MLP_MIN_BLOCKS 8
+#endif
+// resident 128-thread blocks per SM of the inference kernel (its register budget; build-time
+// tuning knob) and the size of its persistent grid per SM
+constexpr int kMlpBlocksPerSm = BBG_MLP_MIN_BLOCKS;
+
 cudaError_t mlp_prepare();
 void launch_mlp_features(const Params &P, const DevBufs &B, const MlpBufs &M, int buf, float dt,
                          float p_unit, cudaStream_t s);
