@@ -999,8 +999,12 @@ def run_ours(args, scene, pos):
                      "max_density_error_ratio_plain": plain["max_density_error_ratio_max"]})
     if sph1 is not None:
         line["sph_config1"] = sph1
+        line["sph_config1_value"] = sph1["particle_updates_per_s"]   # flat copies of the extras' figures
     if batch4 is not None:
         line["batched_config4"] = batch4
+        line["batched_config4_value"] = batch4["learned_value"]
+        line["batched_config4_plain_value"] = batch4["plain_value"]
+        line["batched_config4_speedup_vs_plain"] = batch4["speedup_vs_plain"]
     if frames is not None:
         line["frame_io"] = frames
     if seeds is not None:
