@@ -990,6 +990,9 @@ def run_ours(args, scene, pos):
                                        torch.cuda.get_device_properties(local).multi_processor_count,
                                        clocks.get("sm_mhz")),
     }
+    if roof is not None and roof["kernel"] in line["kernel_bounds"]:
+        # the dominant kernel's other bound: its share of the SMs' issue slots
+        roof["issue_frac"] = line["kernel_bounds"][roof["kernel"]].get("issue_frac")
     if plain is not None:
         line.update({"plain_value": plain["value"], "speedup_vs_plain": value / plain["value"],
                      "plain_host_loop_value": plain["host_loop"]["value"],
